@@ -1,0 +1,68 @@
+/* libtropigpu: GB300 (sm_103a) Rank DP evaluators behind a C ABI.
+ *
+ * Every pointer named T, buf_* or *_dev is a DEVICE pointer (cudaMalloc / torch CUDA memory);
+ * hist, value, ops and info are HOST pointers.  Calls are stream-ordered: the reference-style
+ * per-op functions (dp_*) run on the stream set by tg_set_stream (default: the legacy default
+ * stream) and return before the GPU finishes, except dp_hist, which waits for its result.
+ * Status codes: 0 ok, -1 bad argument, -2 CUDA error, -3 out of device memory, -4 beyond a
+ * documented maximum, -5 a bounded device wait ran out, -6 wrong state; tg_last_error() has the
+ * text of the last failure of the calling thread.  No entry point exits the process or traps
+ * the device.
+ */
+#ifndef TROPIDIST_GB300_H
+#define TROPIDIST_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- library */
+int tg_version(void);
+const char *tg_last_error(void);
+int tg_sm_count(void);
+void tg_set_stream(void *stream);   /* cudaStream_t used by the dp_* per-op functions */
+
+/* ---------------------------------------------------------------- dense Rank DP, per op
+ * Drop-in for the ctypes binding of cdist/viterbi.c (cdist/kernel.py:52-69), on device tables
+ * of n = 2^bits uint8 entries, INF = 255, saturating additions. */
+void dp_update(uint8_t *T, uint64_t n, uint64_t h);                 /* cdist/viterbi.c:73  */
+void dp_expand_update(uint8_t *T, uint64_t n, uint64_t hl);         /* cdist/viterbi.c:122 (T holds 2n) */
+uint64_t dp_select(uint8_t *T, uint64_t n, int pos, int target);    /* cdist/viterbi.c:155 (in place) */
+void dp_fill(uint8_t *T, uint64_t n, uint8_t v);                    /* cdist/viterbi.c:174 */
+void dp_hist(const uint8_t *T, uint64_t n, uint64_t *hist);         /* cdist/viterbi.c:182 (hist: host[256]) */
+int dp_num_threads(void);                                           /* cdist/viterbi.c:195 (SM count) */
+void dp_update_w(uint8_t *T, uint64_t n, uint64_t h, int w);        /* cdist/viterbi.c:204 */
+
+/* uint16 tables (INF = 65535), the same rules; no counterpart in the reference, which has
+ * 8-bit dense tables only (cdist/kernel.py:13) */
+int dp16_update(uint16_t *T, uint64_t n, uint64_t h, int w);
+int dp16_expand_update(uint16_t *T, uint64_t n, uint64_t hl, int w);
+uint64_t dp16_select(uint16_t *T, uint64_t n, int pos, int target);
+
+/* ---------------------------------------------------------------- dense Rank DP, whole plan
+ * Replaces the executor loop of cdist/kernel.py:94-138 (run_plan).  ops: nops rows of int64
+ * (code, a, b): (0, 0, 0) expand, (1, mask, w) update, (2, pos, target) select, i.e. the
+ * trellis Plan.ops of cdist/trellis.py:125-182 encoded row by row.  entry_bytes: 1 (uint8) or
+ * 2 (uint16).  buf_a and buf_b each hold 2^peak_bits entries; the tables ping-pong between them.
+ * ckpt_ops: op counts k after which the table (2^width(k) entries) is copied to ckpt_bufs[i]. */
+void *tg_dense_plan(const int64_t *ops, int64_t nops, int entry_bytes, const int64_t *ckpt_ops,
+                    int64_t nckpt, int *status);
+int tg_dense_plan_info(void *plan, int64_t *info, int ninfo);
+/* info: peak_bits, segments, fused passes, shared-memory sweeps, final buffer (0 a / 1 b),
+ *       update ops, pass bytes, sweep bytes */
+int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg);
+void tg_dense_plan_free(void *plan);
+int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, void *stream);
+int tg_dense_result(void *plan, void *buf_a, void *buf_b, uint32_t *value, void *stream);
+int tg_dense_run(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
+                 uint32_t *value, void *stream);
+int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16);
+/* Runs a scheduled plan on HOST buffers with the launch parameters and index arithmetic of the
+ * kernels; for checking the scheduler on a machine without a GPU.  Not an evaluator. */
+int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,58 @@
+"""Host planning: the trellis op streams are identical to the reference's."""
+from helpers import golden, ops_from_json, sha, unhex
+import numpy as np
+from tropidist_gb300 import auto, synth, trellis
+from tropidist_gb300.problem import Problem
+
+
+def test_plans_identical_to_reference_random():
+    for case in golden("dense_random.json"):
+        plan = trellis.build_plan(case["h"], case["l"], case["obs_mask"], case["order"], case["m"])
+        assert plan.feasible == case["feasible"]
+        assert plan.ops == ops_from_json(case["ops"])
+        assert plan.peak_bits == case["peak_bits"] and plan.work() == case["work"]
+
+
+def test_plans_identical_to_reference_big():
+    for case in golden("dense_big.json"):
+        plan = trellis.build_plan(case["h"], case["l"], 1, list(range(len(case["h"]))), case["m"])
+        assert plan.ops == ops_from_json(case["ops"])
+
+
+def test_synth_problems_reproduce_and_plan_identically():
+    for case in golden("dense_synth.json"):
+        p = synth.dense_small(case["seed"])
+        assert [format(x, "x") for x in p.h] == case["h"] and [format(x, "x") for x in p.l] == case["l"]
+        plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+        assert sha(plan.encode()) == case["ops_sha"] and len(plan.ops) == case["nops"]
+
+
+def test_codes_cut_rank():
+    for case in golden("codes.json"):
+        h = unhex(case["h"])
+        assert max(trellis.cut_profile(h, case["order"])) == case["cut_rank"]
+
+
+def test_encode_roundtrip_and_limits():
+    p = synth.dense_small(0)
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    enc = plan.encode()
+    assert enc.shape == (len(plan.ops), 3) and enc.dtype == np.int64
+    for row, op in zip(enc, plan.ops):
+        assert row[0] == {"expand": 0, "update": 1, "select": 2}[op[0]]
+    import pytest
+    with pytest.raises(ValueError):
+        trellis.encode_ops([("update", 1 << 63)])
+
+
+def test_infeasible_query():
+    p = Problem("no logical", 1, 1, [1, 1], [1, 1], [(0, 0)])
+    plan = trellis.build_plan(p.h, p.l, 1, [0, 1], p.nrows)
+    assert not plan.feasible
+
+
+def test_estimate_counts_work():
+    p = synth.dense_small(1)
+    est = auto.estimate(p, list(range(p.ncols)))
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    assert est["work"] == plan.work() and est["peak_bits"] == plan.peak_bits

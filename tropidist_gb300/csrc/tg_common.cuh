@@ -1,0 +1,140 @@
+// Shared device helpers of libtropigpu (sm_103a).
+//
+// Tables hold minimum weights as uint8 (INF = 255) or uint16 (INF = 65535).  The min-plus rule of
+// one column is  T[s] = min(T[s], sat(T[s ^ h] + w))  with saturation at INF.  Because every entry
+// is <= INF, min(a, sat(b + w)) == min(a, b + w) whenever b + w is computed without wrapping, so the
+// kernels widen entries by one size class (u8 -> u16 lanes, u16 -> u32 lanes) and use the DPX
+// add-then-min instructions, which need no saturation step at all.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define TG_INF8 255u
+#define TG_INF16 65535u
+
+// status codes shared by every C-ABI entry point
+#define TG_OK 0
+#define TG_ERR_ARG -1          // bad argument (sizes, masks, op stream)
+#define TG_ERR_CUDA -2         // a CUDA runtime call failed (tg_last_error has the text)
+#define TG_ERR_NOMEM -3        // a device allocation failed
+#define TG_ERR_TOO_BIG -4      // a size beyond a documented maximum
+#define TG_ERR_TIMEOUT -5      // a bounded device wait ran out
+#define TG_ERR_STATE -6        // called in the wrong state (e.g. a freed handle)
+
+namespace tg {
+
+template <typename E> struct Entry;
+template <> struct Entry<uint8_t> {
+    static constexpr int CB = 4;                 // log2 entries per 16-byte chunk
+    static constexpr uint32_t INF = TG_INF8;
+    static constexpr uint32_t INF_WORD = 0xFFFFFFFFu;
+};
+template <> struct Entry<uint16_t> {
+    static constexpr int CB = 3;
+    static constexpr uint32_t INF = TG_INF16;
+    static constexpr uint32_t INF_WORD = 0xFFFFFFFFu;
+};
+
+// per byte: min(a, b + w), for packed uint8 words (w <= 255 - 0, no wrap in u16 lanes)
+__device__ __forceinline__ uint32_t minplus_u8x4(uint32_t a, uint32_t b, uint32_t w2) {
+    uint32_t alo = __byte_perm(a, 0u, 0x4140), ahi = __byte_perm(a, 0u, 0x4342);
+    uint32_t blo = __byte_perm(b, 0u, 0x4140), bhi = __byte_perm(b, 0u, 0x4342);
+    uint32_t rlo = __viaddmin_u16x2(blo, w2, alo);
+    uint32_t rhi = __viaddmin_u16x2(bhi, w2, ahi);
+    return __byte_perm(rlo, rhi, 0x6420);
+}
+
+// both directions of a pair of packed uint8 words: a' = min(a, b + w), b' = min(b, a + w)
+__device__ __forceinline__ void minplus_pair_u8x4(uint32_t &a, uint32_t &b, uint32_t w2) {
+    uint32_t alo = __byte_perm(a, 0u, 0x4140), ahi = __byte_perm(a, 0u, 0x4342);
+    uint32_t blo = __byte_perm(b, 0u, 0x4140), bhi = __byte_perm(b, 0u, 0x4342);
+    uint32_t ralo = __viaddmin_u16x2(blo, w2, alo), rahi = __viaddmin_u16x2(bhi, w2, ahi);
+    uint32_t rblo = __viaddmin_u16x2(alo, w2, blo), rbhi = __viaddmin_u16x2(ahi, w2, bhi);
+    a = __byte_perm(ralo, rahi, 0x6420);
+    b = __byte_perm(rblo, rbhi, 0x6420);
+}
+
+// per halfword: min(a, b + w) for packed uint16 words (computed in 32-bit lanes: no wrap)
+__device__ __forceinline__ uint32_t minplus_u16x2(uint32_t a, uint32_t b, uint32_t w) {
+    uint32_t lo = min(a & 0xFFFFu, (b & 0xFFFFu) + w);
+    uint32_t hi = min(a >> 16, (b >> 16) + w);
+    return lo | (hi << 16);
+}
+
+// byte permutation of a word: byte i <- byte i ^ x (x < 4)
+__device__ __forceinline__ uint32_t xor_bytes(uint32_t v, uint32_t x) {
+    const uint32_t sel = (0u ^ x) | ((1u ^ x) << 4) | ((2u ^ x) << 8) | ((3u ^ x) << 12);
+    return __byte_perm(v, 0u, sel);
+}
+
+// 16-byte chunk as 4 words
+struct Chunk { uint32_t w[4]; };
+
+__device__ __forceinline__ Chunk ld_chunk(const void *p) {
+    uint4 v = *reinterpret_cast<const uint4 *>(p);
+    Chunk c; c.w[0] = v.x; c.w[1] = v.y; c.w[2] = v.z; c.w[3] = v.w; return c;
+}
+__device__ __forceinline__ void st_chunk(void *p, const Chunk &c) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(c.w[0], c.w[1], c.w[2], c.w[3]);
+}
+__device__ __forceinline__ Chunk ldg_chunk(const void *p) {
+    uint4 v = __ldcs(reinterpret_cast<const uint4 *>(p));   // streamed once: evict-first
+    Chunk c; c.w[0] = v.x; c.w[1] = v.y; c.w[2] = v.z; c.w[3] = v.w; return c;
+}
+__device__ __forceinline__ void stg_chunk(void *p, const Chunk &c) {
+    __stcs(reinterpret_cast<uint4 *>(p), make_uint4(c.w[0], c.w[1], c.w[2], c.w[3]));
+}
+
+// entry permutation inside a chunk: entry i <- entry i ^ m (m < entries per chunk)
+template <typename E> __device__ __forceinline__ Chunk chunk_xor(const Chunk &c, uint32_t m);
+template <> __device__ __forceinline__ Chunk chunk_xor<uint8_t>(const Chunk &c, uint32_t m) {
+    Chunk r;
+    const uint32_t wx = m >> 2, bx = m & 3u;
+#pragma unroll
+    for (int k = 0; k < 4; k++) r.w[k] = xor_bytes(c.w[k ^ wx], bx);
+    return r;
+}
+template <> __device__ __forceinline__ Chunk chunk_xor<uint16_t>(const Chunk &c, uint32_t m) {
+    Chunk r;
+    const uint32_t wx = m >> 1, hx = m & 1u;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t v = c.w[k ^ wx];
+        r.w[k] = hx ? __byte_perm(v, 0u, 0x1032) : v;
+    }
+    return r;
+}
+
+// chunk-wise min-plus: a' = min(a, b + w) entrywise
+template <typename E> __device__ __forceinline__ Chunk chunk_minplus(const Chunk &a, const Chunk &b, uint32_t w);
+template <> __device__ __forceinline__ Chunk chunk_minplus<uint8_t>(const Chunk &a, const Chunk &b, uint32_t w) {
+    Chunk r;
+    const uint32_t w2 = w | (w << 16);
+#pragma unroll
+    for (int k = 0; k < 4; k++) r.w[k] = minplus_u8x4(a.w[k], b.w[k], w2);
+    return r;
+}
+template <> __device__ __forceinline__ Chunk chunk_minplus<uint16_t>(const Chunk &a, const Chunk &b, uint32_t w) {
+    Chunk r;
+#pragma unroll
+    for (int k = 0; k < 4; k++) r.w[k] = minplus_u16x2(a.w[k], b.w[k], w);
+    return r;
+}
+
+// scalar rule on one entry
+template <typename E> __device__ __forceinline__ E minplus1(E a, E b, uint32_t w) {
+    uint32_t x = (uint32_t)b + w;
+    return (E)min((uint32_t)a, x);
+}
+
+// index with a zero bit inserted at position b
+__device__ __forceinline__ uint32_t insert_zero(uint32_t p, int b) {
+    uint32_t lo = p & ((1u << b) - 1u);
+    return ((p ^ lo) << 1) | lo;
+}
+__device__ __forceinline__ uint64_t insert_zero64(uint64_t p, int b) {
+    uint64_t lo = p & ((1ull << b) - 1ull);
+    return ((p ^ lo) << 1) | lo;
+}
+
+}  // namespace tg
