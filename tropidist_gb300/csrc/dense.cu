@@ -69,11 +69,10 @@ __global__ void k_update_chunks(E *__restrict__ T, int bits, uint64_t h, uint32_
     const int hb = 63 - __clzll(hhi);
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < nch / 2; p += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t c = insert_zero64(p, hb), c2 = c ^ hhi;
-        Chunk a = ld_chunk(C + c), b = ld_chunk(C + c2);
-        Chunk na = chunk_minplus<E>(a, chunk_xor<E>(b, hlo), w);
-        Chunk nb = chunk_minplus<E>(b, chunk_xor<E>(a, hlo), w);
-        st_chunk(C + c, na);
-        st_chunk(C + c2, nb);
+        Chunk a = ld_chunk(C + c), pb = chunk_xor<E>(ld_chunk(C + c2), hlo);
+        chunk_minplus_pair<E>(a, pb, w);
+        st_chunk(C + c, a);
+        st_chunk(C + c2, chunk_xor<E>(pb, hlo));
     }
 }
 
@@ -192,11 +191,13 @@ __device__ __forceinline__ void smem_update(E *T, int bits, uint32_t m, uint32_t
             }
         } else {
             const int hb = 31 - __clz(mhi);
+            // perm(b') = min(perm(b), a + w): both directions from one unpacking of a and perm(b)
             for (uint32_t p = threadIdx.x; p < nch / 2; p += blockDim.x) {
                 uint32_t c = insert_zero(p, hb), c2 = c ^ mhi;
-                Chunk a = C[c], b = C[c2];
-                C[c] = chunk_minplus<E>(a, chunk_xor<E>(b, mlo), w);
-                C[c2] = chunk_minplus<E>(b, chunk_xor<E>(a, mlo), w);
+                Chunk a = C[c], pb = chunk_xor<E>(C[c2], mlo);
+                chunk_minplus_pair<E>(a, pb, w);
+                C[c] = a;
+                C[c2] = chunk_xor<E>(pb, mlo);
             }
         }
     } else {
@@ -327,13 +328,14 @@ __global__ void __launch_bounds__(FP_THREADS) k_fused_pass(const __grid_constant
         // load the input part of the tile, INF over the rows expanded in this pass
         for (uint32_t c = tid; c < nch_in; c += FP_THREADS) {
             uint64_t off = ib + tid_in + pdep_w64(c >> FP_TBITS, P.loc_in + CB + FP_TBITS, nb_in - tb_in);
-            TC[c] = ldg_chunk(in + off);
+            cp_async16(TC + c, in + off);
         }
         for (uint32_t c = nch_in + tid; c < nch_all; c += FP_THREADS) {
             Chunk inf;
             inf.w[0] = inf.w[1] = inf.w[2] = inf.w[3] = 0xFFFFFFFFu;
             TC[c] = inf;
         }
+        cp_async_wait_all();
         __syncthreads();
         for (int u = 0; u < P.nupd; u++) {
             smem_update<E>(T, P.d, P.upd_mask[u], P.upd_w[u]);
@@ -348,10 +350,15 @@ __global__ void __launch_bounds__(FP_THREADS) k_fused_pass(const __grid_constant
             if (P.fast_out) {
                 v = TC[sidx >> CB];
             } else {
-                E tmp[16 / sizeof(E)];
+                constexpr int PER_WORD = 4 / sizeof(E);
 #pragma unroll
-                for (int i = 0; i < (int)(16 / sizeof(E)); i++) tmp[i] = T[sidx + P.pat[i]];
-                v = *reinterpret_cast<Chunk *>(tmp);
+                for (int k = 0; k < 4; k++) {
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int e = 0; e < PER_WORD; e++)
+                        word |= (uint32_t)T[sidx + P.pat[k * PER_WORD + e]] << (8 * sizeof(E) * e);
+                    v.w[k] = word;
+                }
             }
             stg_chunk(out + off, v);
         }
@@ -698,14 +705,40 @@ static int set_attrs() {
     return TG_OK;
 }
 
+// resident blocks per SM of a kernel at a block size and dynamic shared memory (cached)
+static int resident_blocks(const void *fn, int threads, size_t smem) {
+    static std::vector<std::pair<std::pair<const void *, size_t>, int>> cache;
+    for (auto &c : cache)
+        if (c.first.first == fn && c.first.second == smem) return c.second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess || n < 1) n = 1;
+    cache.push_back({{fn, smem}, n});
+    return n;
+}
+
+static std::vector<cudaEvent_t> g_events;
+
+static int ensure_events(size_t n) {
+    while (g_events.size() < n) {
+        cudaEvent_t ev;
+        int e = cuda_check(cudaEventCreate(&ev), "event create");
+        if (e) return e;
+        g_events.push_back(ev);
+    }
+    return TG_OK;
+}
+
 template <typename E>
-static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStream_t st) {
+static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStream_t st, bool timed = false) {
     int e = set_attrs();
     if (e) return e;
+    if (timed && (e = ensure_events(2 * P.segs.size()))) return e;
     E *bufs[2] = {a, b};
     int cur = 0;
+    size_t si = 0;
     for (const Seg &S : P.segs) {
         E *src = bufs[cur], *dst = bufs[cur ^ 1];
+        if (timed) cudaEventRecord(g_events[2 * si], st);
         if (S.kind == 2) {
             const uint64_t items = ((uint64_t)1 << S.w_in) >> Entry<E>::CB;
             k_single_op<E><<<grid_for(items, 256), 256, 0, st>>>(src, dst, S.w_in, S.op_code, S.op_a, S.op_b);
@@ -714,13 +747,14 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
             k_sweep_smem<E><<<1, 512, sm, st>>>(S.sp, src, dst);
         } else {
             size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
-            int per_sm = std::max(1, (int)((220u << 10) / std::max<size_t>(sm, 1)));
-            per_sm = std::min(per_sm, 4);
+            int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
             uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
             k_fused_pass<E><<<(unsigned)grid, FP_THREADS, sm, st>>>(S.pp, src, dst);
         }
         e = cuda_check(cudaGetLastError(), "dense launch");
         if (e) return e;
+        if (timed) cudaEventRecord(g_events[2 * si + 1], st);
+        si++;
         cur ^= 1;
         if (S.ckpt >= 0 && ckpt_bufs && ckpt_bufs[S.ckpt]) {
             e = cuda_check(cudaMemcpyAsync(ckpt_bufs[S.ckpt], bufs[cur], ((size_t)1 << S.w_out) * sizeof(E),
@@ -951,6 +985,35 @@ int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, voi
     if (P.nops == 0) return TG_OK;
     if (P.eb == 1) return launch_plan<uint8_t>(P, (uint8_t *)buf_a, (uint8_t *)buf_b, ckpt_bufs, st);
     return launch_plan<uint16_t>(P, (uint16_t *)buf_a, (uint16_t *)buf_b, ckpt_bufs, st);
+}
+
+int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, double *out, int nout) {
+    // out: per segment kind (0 sweep, 1 fused pass, 2 one-op pass): launches, total ms, bytes
+    if (!plan || !buf_a || !buf_b || !out) return set_error(TG_ERR_ARG, "null argument");
+    const DensePlan &P = *static_cast<DensePlan *>(plan);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int e = cuda_check(cudaMemsetAsync(buf_a, 0, P.eb, st), "init");
+    if (e) return e;
+    if (P.eb == 1) e = launch_plan<uint8_t>(P, (uint8_t *)buf_a, (uint8_t *)buf_b, nullptr, st, true);
+    else e = launch_plan<uint16_t>(P, (uint16_t *)buf_a, (uint16_t *)buf_b, nullptr, st, true);
+    if (e) return e;
+    if (P.segs.empty()) return TG_OK;
+    e = cuda_check(cudaEventSynchronize(g_events[2 * P.segs.size() - 1]), "event sync");
+    if (e) return e;
+    double acc[9] = {0};
+    for (size_t k = 0; k < P.segs.size(); k++) {
+        const Seg &S = P.segs[k];
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, g_events[2 * k], g_events[2 * k + 1]);
+        int kk = S.kind;
+        acc[3 * kk] += 1;
+        acc[3 * kk + 1] += ms;
+        double bytes = S.kind == 0 ? (double)P.eb * ((S.sp.has_in ? (1ull << S.w_in) : 0) + (1ull << S.w_out))
+                                   : (double)P.eb * ((1ull << S.w_in) + (1ull << S.w_out));
+        acc[3 * kk + 2] += bytes;
+    }
+    for (int k = 0; k < nout && k < 9; k++) out[k] = acc[k];
+    return TG_OK;
 }
 
 int tg_dense_result(void *plan, void *buf_a, void *buf_b, uint32_t *value, void *stream) {

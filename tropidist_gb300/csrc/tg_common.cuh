@@ -85,22 +85,36 @@ __device__ __forceinline__ void stg_chunk(void *p, const Chunk &c) {
     __stcs(reinterpret_cast<uint4 *>(p), make_uint4(c.w[0], c.w[1], c.w[2], c.w[3]));
 }
 
+// word permutation of a chunk: word k <- word k ^ wx (selects, no dynamic register indexing)
+__device__ __forceinline__ void chunk_xor_words(uint32_t &x0, uint32_t &x1, uint32_t &x2, uint32_t &x3, uint32_t wx) {
+    uint32_t t;
+    if (wx & 1u) { t = x0; x0 = x1; x1 = t; t = x2; x2 = x3; x3 = t; }
+    if (wx & 2u) { t = x0; x0 = x2; x2 = t; t = x1; x1 = x3; x3 = t; }
+}
+
 // entry permutation inside a chunk: entry i <- entry i ^ m (m < entries per chunk)
 template <typename E> __device__ __forceinline__ Chunk chunk_xor(const Chunk &c, uint32_t m);
 template <> __device__ __forceinline__ Chunk chunk_xor<uint8_t>(const Chunk &c, uint32_t m) {
+    uint32_t x0 = c.w[0], x1 = c.w[1], x2 = c.w[2], x3 = c.w[3];
+    chunk_xor_words(x0, x1, x2, x3, m >> 2);
+    const uint32_t bx = m & 3u;
     Chunk r;
-    const uint32_t wx = m >> 2, bx = m & 3u;
-#pragma unroll
-    for (int k = 0; k < 4; k++) r.w[k] = xor_bytes(c.w[k ^ wx], bx);
+    if (bx) {
+        r.w[0] = xor_bytes(x0, bx); r.w[1] = xor_bytes(x1, bx); r.w[2] = xor_bytes(x2, bx); r.w[3] = xor_bytes(x3, bx);
+    } else {
+        r.w[0] = x0; r.w[1] = x1; r.w[2] = x2; r.w[3] = x3;
+    }
     return r;
 }
 template <> __device__ __forceinline__ Chunk chunk_xor<uint16_t>(const Chunk &c, uint32_t m) {
+    uint32_t x0 = c.w[0], x1 = c.w[1], x2 = c.w[2], x3 = c.w[3];
+    chunk_xor_words(x0, x1, x2, x3, m >> 1);
     Chunk r;
-    const uint32_t wx = m >> 1, hx = m & 1u;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        uint32_t v = c.w[k ^ wx];
-        r.w[k] = hx ? __byte_perm(v, 0u, 0x1032) : v;
+    if (m & 1u) {
+        r.w[0] = __byte_perm(x0, 0u, 0x1032); r.w[1] = __byte_perm(x1, 0u, 0x1032);
+        r.w[2] = __byte_perm(x2, 0u, 0x1032); r.w[3] = __byte_perm(x3, 0u, 0x1032);
+    } else {
+        r.w[0] = x0; r.w[1] = x1; r.w[2] = x2; r.w[3] = x3;
     }
     return r;
 }
@@ -120,6 +134,29 @@ template <> __device__ __forceinline__ Chunk chunk_minplus<uint16_t>(const Chunk
     for (int k = 0; k < 4; k++) r.w[k] = minplus_u16x2(a.w[k], b.w[k], w);
     return r;
 }
+
+// both directions at once on aligned chunks: a <- min(a, b + w), b <- min(b, a + w)
+template <typename E> __device__ __forceinline__ void chunk_minplus_pair(Chunk &a, Chunk &b, uint32_t w);
+template <> __device__ __forceinline__ void chunk_minplus_pair<uint8_t>(Chunk &a, Chunk &b, uint32_t w) {
+    const uint32_t w2 = w | (w << 16);
+#pragma unroll
+    for (int k = 0; k < 4; k++) minplus_pair_u8x4(a.w[k], b.w[k], w2);
+}
+template <> __device__ __forceinline__ void chunk_minplus_pair<uint16_t>(Chunk &a, Chunk &b, uint32_t w) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t x = a.w[k], y = b.w[k];
+        a.w[k] = minplus_u16x2(x, y, w);
+        b.w[k] = minplus_u16x2(y, x, w);
+    }
+}
+
+// asynchronous 16-byte global -> shared copies (L2 only)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // scalar rule on one entry
 template <typename E> __device__ __forceinline__ E minplus1(E a, E b, uint32_t w) {
