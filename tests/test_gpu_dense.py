@@ -26,6 +26,13 @@ def gpu():
 TUNINGS = [(16, 15, 15, 14), (12, 11, 10, 9), (8, 7, 6, 5), (6, 5, 4, 3)]
 
 
+@pytest.fixture(autouse=True)
+def default_tuning():
+    from tropidist_gb300 import _lib
+    _lib.lib().tg_dense_set_tuning(*TUNINGS[0])
+    yield
+
+
 def gpu_tables(plan, ks, dtype="u8"):
     from tropidist_gb300 import kernel
     cp = kernel.CompiledPlan(plan, dtype, ks)

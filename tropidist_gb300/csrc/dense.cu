@@ -16,6 +16,7 @@
 // stored to their positions in the output layout.
 #include "tg_common.cuh"
 #include "tg_capi.h"
+#include "fused_u8.cuh"
 
 #include <algorithm>
 #include <cstdio>
@@ -286,6 +287,16 @@ struct PassParams {
     uint32_t upd_mask[FP_MAXU];
     uint8_t upd_w[FP_MAXU];
     uint16_t pat[16];                  // smem index of the low compacted entries (generic store)
+    // uint8 register-group form of the same updates (k_fused_pass_u8)
+    int use_groups, ngroups;
+    int store_mode;                    // output chunk from: 0 one smem chunk, 1 two chunks without local
+                                       // bit sel_low (< 4), 2 byte gathers through pat
+    int sel_low;
+    int nslow;                         // updates with in-chunk bits, applied in shared memory
+    uint8_t slow_idx[FP_MAXU];
+    GroupDesc groups[FP_MAXG];
+    uint8_t ucode[FP_MAXU];
+    uint8_t uw[FP_MAXU];
 };
 
 __device__ __forceinline__ uint64_t pdep_w64(uint32_t x, const uint64_t *wt, int nb) {
@@ -364,6 +375,126 @@ __global__ void __launch_bounds__(FP_THREADS) k_fused_pass(const __grid_constant
         }
         __syncthreads();
     }
+}
+
+// uint8 tables: the same pass with the updates applied in register-resident groups.  One
+// persistent CTA per SM over a contiguous range of tiles; the tile loads are double-buffered
+// (cp.async into one half of shared memory while the other half is computed and stored).
+// Chunk c of a tile is handled by thread c % 256 in iteration c / 256: its offsets are the
+// thread's own part (computed once) plus an iteration part that is the same for every thread
+// (tables in shared memory), and the tile bases advance by a carry table (tile t+1 differs from
+// tile t in the bits up to the lowest zero bit of t).
+#define FP_MAXIT 16
+__global__ void __launch_bounds__(FP_THREADS, 1) k_fused_pass_u8(const __grid_constant__ PassParams P,
+                                                                const uint8_t *__restrict__ in,
+                                                                uint8_t *__restrict__ out) {
+    constexpr int CB = 4;
+    extern __shared__ uint4 smem_raw[];
+    __shared__ uint64_t s_in_hi[FP_MAXIT], s_out_hi[FP_MAXIT];
+    __shared__ uint32_t s_sm_hi[FP_MAXIT];
+    __shared__ int64_t s_cin[FP_MAXOUTER], s_cout[FP_MAXOUTER];
+    const uint32_t tid = threadIdx.x;
+    const int nb_in = P.d_in - CB, nb_out = P.d_out - CB;
+    const int tb_in = min(nb_in, FP_TBITS), tb_out = min(nb_out, FP_TBITS);
+    const uint32_t nch_in = 1u << nb_in, nch_all = 1u << (P.d - CB), nch_out = 1u << nb_out;
+    const uint32_t it_in = (nch_in + FP_THREADS - 1) / FP_THREADS, it_out = (nch_out + FP_THREADS - 1) / FP_THREADS;
+    if (tid < it_in) s_in_hi[tid] = pdep_w64(tid, P.loc_in + CB + FP_TBITS, nb_in - tb_in);
+    if (tid < it_out) {
+        s_out_hi[tid] = pdep_w64(tid, P.cmp_out + CB + FP_TBITS, nb_out - tb_out);
+        s_sm_hi[tid] = pdep_w32(tid, P.cmp_smem + CB + FP_TBITS, nb_out - tb_out);
+    }
+    if (tid < (uint32_t)P.n_outer) {
+        // carry table: base(t + 1) - base(t) when bit tid is the lowest zero bit of t
+        int64_t ci = (int64_t)P.outer_in[tid], co = (int64_t)P.outer_out[tid];
+        for (uint32_t k = 0; k < tid; k++) { ci -= (int64_t)P.outer_in[k]; co -= (int64_t)P.outer_out[k]; }
+        s_cin[tid] = ci;
+        s_cout[tid] = co;
+    }
+    const uint64_t tid_in = pdep_w64(tid, P.loc_in + CB, tb_in);
+    const uint64_t tid_out = pdep_w64(tid, P.cmp_out + CB, tb_out);
+    const uint32_t tid_sm = pdep_w32(tid, P.cmp_smem + CB, tb_out) + P.sel_bits;
+    const bool in_full = nch_in >= FP_THREADS, out_full = nch_out >= FP_THREADS;
+
+    // this CTA's contiguous range of tiles
+    const uint64_t per = P.ntiles / gridDim.x, rem = P.ntiles % gridDim.x;
+    const uint64_t t0 = blockIdx.x * per + ((uint64_t)blockIdx.x < rem ? (uint64_t)blockIdx.x : rem);
+    const uint64_t t1 = t0 + per + (blockIdx.x < rem ? 1 : 0);
+    uint64_t ib0 = 0, ob0 = 0;
+    for (int k = 0; k < P.n_outer; k++)
+        if ((t0 >> k) & 1ull) { ib0 += P.outer_in[k]; ob0 += P.outer_out[k]; }
+    __syncthreads();
+
+    const uint8_t *inb = in + tid_in;
+    auto issue_load = [&](uint64_t ib, uint4 *TC) {
+        const uint8_t *src = inb + ib;
+        if (in_full) {
+            for (uint32_t it = 0; it < it_in; it++) cp_async16(TC + it * FP_THREADS + tid, src + s_in_hi[it]);
+        } else if (tid < nch_in) {
+            cp_async16(TC + tid, src);
+        }
+        for (uint32_t c = nch_in + tid; c < nch_all; c += FP_THREADS) TC[c] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        cp_async_commit();
+    };
+    auto advance = [&](uint64_t t, uint64_t &ib, uint64_t &ob) {   // bases of tile t + 1 from tile t
+        const int k = __ffsll((long long)~t) - 1;
+        ib += s_cin[k];
+        ob += s_cout[k];
+    };
+
+    uint4 *const buf0 = smem_raw, *const buf1 = smem_raw + nch_all;
+    int cur = 0;
+    uint64_t ib = ib0, ob = ob0, ibn = ib0, obn = ob0;
+    if (t0 < t1) issue_load(ib, buf0);
+    for (uint64_t tile = t0; tile < t1; tile++) {
+        if (tile + 1 < t1) {
+            advance(tile, ibn, obn);
+            issue_load(ibn, cur ? buf0 : buf1);
+            cp_async_wait_group<1>();
+        } else {
+            cp_async_wait_group<0>();
+        }
+        __syncthreads();
+        uint4 *TC = cur ? buf1 : buf0;
+        const uint8_t *T = reinterpret_cast<const uint8_t *>(TC);
+        for (int g = 0; g < P.ngroups; g++) {
+            run_group<FP_THREADS>(TC, P.d, P.groups[g], P.ucode, P.uw);
+            __syncthreads();
+        }
+        for (int u = 0; u < P.nslow; u++) {
+            const int k = P.slow_idx[u];
+            smem_update<uint8_t>(reinterpret_cast<uint8_t *>(TC), P.d, P.upd_mask[k], P.upd_w[k]);
+            __syncthreads();
+        }
+        uint8_t *dstb = out + ob + tid_out;
+        for (uint32_t it = 0; it < it_out; it++) {
+            const uint32_t q = it * FP_THREADS + tid;
+            if (!out_full && q >= nch_out) break;
+            const uint32_t sidx = tid_sm + s_sm_hi[it];
+            uint4 v;
+            if (P.store_mode == 0) {
+                v = TC[sidx >> CB];
+            } else if (P.store_mode == 1) {
+                const uint32_t base = (sidx >> 5) << 1;
+                v = gather_one_select(TC[base], TC[base + 1], P.sel_low, (sidx >> P.sel_low) & 1u);
+            } else {
+                uint32_t wd[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) word |= (uint32_t)T[sidx + P.pat[4 * k + e]] << (8 * e);
+                    wd[k] = word;
+                }
+                v = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+            }
+            __stcs(reinterpret_cast<uint4 *>(dstb + s_out_hi[it]), v);
+        }
+        __syncthreads();
+        cur ^= 1;
+        ib = ibn;
+        ob = obn;
+    }
+    (void)ib;
 }
 
 // ------------------------------------------------------------------ one op, out of place (wide masks)
@@ -460,6 +591,145 @@ struct Layout {
 // tunables (set by tg_dense_set_tuning)
 static int g_dmax8 = 16, g_dmax16 = 15;          // fused tile bits
 static int g_sweep_bits8 = 15, g_sweep_bits16 = 14; // shared-memory sweep capacity (bits)
+static bool g_relayout = true;                       // uint8 layout planning between passes
+
+// Groups of the pass's chunk-level updates (no bit below 4) whose chunk masks span <= 3
+// dimensions (see fused_u8.cuh); updates with in-chunk bits are listed for the shared-memory
+// path.  Also the store mode.  use_groups = 0 when the register form does not apply.
+static void build_groups(PassParams &pp, uint32_t selmask) {
+    const int CB = 4;
+    (void)selmask;
+    pp.use_groups = 0;
+    const int nb = pp.d - CB;
+    if (nb < 3) return;
+    struct G { std::vector<uint32_t> basis; std::vector<int> ups; };
+    std::vector<G> gs;
+    auto reduce = [](uint32_t v, const std::vector<uint32_t> &basis) {
+        for (uint32_t b : basis) {
+            int pv = 31 - __builtin_clz(b);
+            if ((v >> pv) & 1u) v ^= b;
+        }
+        return v;
+    };
+    auto add_vec = [&](std::vector<uint32_t> &basis, uint32_t v) {
+        v = reduce(v, basis);
+        if (!v) return;
+        int pv = 31 - __builtin_clz(v);
+        for (uint32_t &b : basis)
+            if ((b >> pv) & 1u) b ^= v;
+        basis.push_back(v);
+    };
+    pp.nslow = 0;
+    for (int u = 0; u < pp.nupd; u++) {
+        const uint32_t m = pp.upd_mask[u];
+        if (m & 15u) {
+            pp.slow_idx[pp.nslow++] = (uint8_t)u;
+            continue;
+        }
+        const uint32_t c = m >> CB;
+        bool placed = false;
+        for (G &g : gs) {
+            if (!reduce(c, g.basis) || g.basis.size() < 3) {
+                add_vec(g.basis, c);
+                g.ups.push_back(u);
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) {
+            G g;
+            add_vec(g.basis, c);
+            g.ups.push_back(u);
+            gs.push_back(g);
+        }
+    }
+    if ((int)gs.size() > FP_MAXG) return;
+    int code_i = 0;
+    for (size_t gi = 0; gi < gs.size(); gi++) {
+        G &g = gs[gi];
+        for (int b = nb - 1; b >= 0 && g.basis.size() < 3; b--) add_vec(g.basis, 1u << b);
+        std::sort(g.basis.begin(), g.basis.end(), [](uint32_t a, uint32_t b) { return __builtin_clz(a) > __builtin_clz(b); });
+        GroupDesc &D = pp.groups[gi];
+        memset(&D, 0, sizeof(D));
+        for (int j = 0; j < 3; j++) D.piv[j] = (uint8_t)(31 - __builtin_clz(g.basis[j]));
+        for (int x = 0; x < 8; x++) {
+            uint32_t o = 0;
+            for (int j = 0; j < 3; j++)
+                if ((x >> j) & 1) o ^= g.basis[j];
+            D.xoff[x] = o;
+        }
+        D.first = (uint8_t)code_i;
+        D.count = (uint8_t)g.ups.size();
+        for (int u : g.ups) {
+            const uint32_t mhi = pp.upd_mask[u] >> CB;
+            uint32_t y = 0;
+            for (int j = 0; j < 3; j++)
+                if ((mhi >> D.piv[j]) & 1u) y |= 1u << j;
+            pp.ucode[code_i] = (uint8_t)y;
+            pp.uw[code_i] = pp.upd_w[u];
+            code_i++;
+        }
+    }
+    pp.ngroups = (int)gs.size();
+    // store mode from the smem weights of the four lowest output positions
+    bool ident = true;
+    for (int b = 0; b < CB; b++) ident = ident && pp.cmp_smem[b] == (1u << b);
+    pp.store_mode = 2;
+    if (ident) {
+        pp.store_mode = 0;
+    } else {
+        for (int sb = 0; sb < CB; sb++) {
+            bool ok = true;
+            int k = 0;
+            for (int b = 0; b <= CB; b++) {
+                if (b == sb) continue;
+                ok = ok && pp.cmp_smem[k++] == (1u << b);
+            }
+            if (ok) { pp.store_mode = 1; pp.sel_low = sb; break; }
+        }
+    }
+    pp.use_groups = 1;
+}
+
+// Row bookkeeping of an op stream: which rows each op touches (rows are numbered in order of
+// their expand op), and for each row the ops that update or close it.
+struct RowInfo {
+    std::vector<std::vector<int>> upd_rows;     // per op: rows of an update
+    std::vector<int> sel_row, exp_row;          // per op: row closed / opened (-1)
+    std::vector<std::vector<int64_t>> uses;     // per row: ops that update or close it (ascending)
+    int64_t next_use(int row, int64_t after) const {
+        const auto &u = uses[row];
+        auto it = std::lower_bound(u.begin(), u.end(), after);
+        return it == u.end() ? INT64_MAX : *it;
+    }
+};
+
+static void row_info(const std::vector<HostOp> &hops, RowInfo &R) {
+    const int64_t n = (int64_t)hops.size();
+    R.upd_rows.assign(n, {});
+    R.sel_row.assign(n, -1);
+    R.exp_row.assign(n, -1);
+    std::vector<int> canon;
+    int next = 0;
+    for (int64_t i = 0; i < n; i++) {
+        const HostOp &o = hops[i];
+        if (o.code == 0) {
+            R.exp_row[i] = next;
+            canon.push_back(next++);
+            R.uses.emplace_back();
+        } else if (o.code == 1) {
+            for (int p = 0; p < (int)canon.size(); p++)
+                if ((o.a >> p) & 1ull) { R.upd_rows[i].push_back(canon[p]); R.uses[canon[p]].push_back(i); }
+        } else {
+            R.sel_row[i] = canon[o.a];
+            R.uses[canon[o.a]].push_back(i);
+            canon.erase(canon.begin() + o.a);
+        }
+    }
+}
+
+static inline bool has_row(const std::vector<int> &v, int r) { return std::find(v.begin(), v.end(), r) != v.end(); }
+static inline int index_of(const std::vector<int> &v, int r) { return (int)(std::find(v.begin(), v.end(), r) - v.begin()); }
 
 static int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt,
                             DensePlan &P) {
@@ -471,6 +741,7 @@ static int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int6
     const int CB = eb == 1 ? 4 : 3;
     const int DMAX = eb == 1 ? g_dmax8 : g_dmax16;
     const int SWB = eb == 1 ? g_sweep_bits8 : g_sweep_bits16;
+    const bool relayout = eb == 1 && g_relayout;
     P.eb = eb;
     P.peak_bits = peak;
     P.nops = nops;
@@ -481,22 +752,187 @@ static int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int6
         if (c < 0 || c > nops) return set_error(TG_ERR_ARG, "checkpoint outside the op stream");
     std::vector<char> is_ckpt(nops + 1, 0);
     for (auto c : P.ckpt_ops) is_ckpt[c] = 1;
+    RowInfo RI;
+    row_info(hops, RI);
 
-    std::vector<int> active;   // position -> row id
-    int next_row = 0;
+    std::vector<int> canon;    // canonical order: position -> row (the positions the ops refer to)
+    std::vector<int> phys;     // physical order of the table in memory
     int64_t i = 0;
     int buf = 0;
-    // a checkpoint at op 0 means the start table {0: 0}: it lives in buffer a (written by the caller)
+    auto apply_canon = [&](int64_t k, std::vector<int> &c) {
+        const HostOp &o = hops[k];
+        if (o.code == 0) c.push_back(RI.exp_row[k]);
+        else if (o.code == 2) c.erase(c.begin() + o.a);
+    };
+    auto sweep_next = [&](int w, int64_t k) {       // would a segment starting at op k be a sweep?
+        return k < nops && (w < SWB || (w == SWB && hops[k].code != 0));
+    };
+    auto must_canon = [&](int64_t jend, const std::vector<int> &c) {
+        return !relayout || is_ckpt[jend] || jend == nops || sweep_next((int)c.size(), jend);
+    };
+    // one fused pass over the ops [i0, j0) (possibly none: a relayout to the canonical order)
+    auto build_pass = [&](int64_t i0, int64_t j0, const std::vector<int> &touched, bool force_all, Seg &S) -> int {
+        const int w_in = (int)canon.size();
+        const std::vector<int> lin = phys;
+        std::vector<int> inchunk(lin.begin(), lin.begin() + std::min<int>(CB, (int)lin.size()));
+            // ---- the run's rows
+            std::vector<int> exp_rows, sel_rows, sel_tg;
+            std::vector<std::pair<std::vector<int>, int>> upd;
+            std::vector<int> cout_ = canon;
+            for (int64_t k = i0; k < j0; k++) {
+                const HostOp &o = hops[k];
+                if (o.code == 0) exp_rows.push_back(RI.exp_row[k]);
+                else if (o.code == 1) { upd.push_back({RI.upd_rows[k], (int)o.b}); P.n_updates++; }
+                else { sel_rows.push_back(RI.sel_row[k]); sel_tg.push_back((int)o.b); }
+                apply_canon(k, cout_);
+            }
+            const bool force = force_all || must_canon(j0, cout_);
+            std::vector<int> trows = touched;
+            for (int r : inchunk) if (!has_row(trows, r)) trows.push_back(r);
+            if (force)
+                for (int p = 0; p < CB && p < (int)cout_.size(); p++)
+                    if (!has_row(trows, cout_[p])) trows.push_back(cout_[p]);
+            // eviction of one in-chunk row (uint8 layout planning)
+            int evict = -1, cand = -1;
+            std::vector<int> sel_in;
+            for (int r : inchunk) if (has_row(sel_rows, r)) sel_in.push_back(r);
+            if (!force && relayout && sel_in.size() <= 1) {
+                if (sel_in.size() == 1) {
+                    evict = sel_in[0];
+                } else {
+                    int64_t best = INT64_MAX;
+                    const int64_t look = std::max<int64_t>(8, j0 - i0);
+                    for (int r : inchunk) {
+                        int64_t nu = RI.next_use(r, j0);
+                        if (nu < j0 + look && nu < best) { best = nu; evict = r; }
+                    }
+                }
+                if (evict >= 0) {
+                    // the input row with the furthest next use enters the in-chunk positions
+                    int64_t far = -1;
+                    auto consider = [&](int r) {
+                        if (has_row(inchunk, r) || has_row(sel_rows, r) || !has_row(lin, r)) return;
+                        int64_t nu = RI.next_use(r, j0);
+                        if (nu > far) { far = nu; cand = r; }
+                    };
+                    for (int r : trows) consider(r);
+                    if (cand < 0 && (int)trows.size() < DMAX)
+                        for (int r : lin) consider(r);
+                    if (cand < 0) evict = -1;
+                    else if (!has_row(trows, cand)) trows.push_back(cand);
+                }
+            }
+            // pad with the lowest input positions (larger contiguous loads, >= 7 local bits)
+            const int w_total = w_in + (int)exp_rows.size();
+            int want = std::min(DMAX, std::max((int)trows.size(), std::max(7, std::min(13, w_total - 9))));
+            for (int p = 0; p < (int)lin.size() && (int)trows.size() < want; p++)
+                if (!has_row(trows, lin[p])) trows.push_back(lin[p]);
+            // the four lowest output positions must hold tile rows that survive the pass
+            auto survivors = [&]() {
+                int n = 0;
+                for (int r : trows) n += !has_row(sel_rows, r);
+                return n + (int)exp_rows.size() - (int)std::count_if(exp_rows.begin(), exp_rows.end(),
+                                                                      [&](int r) { return has_row(trows, r); });
+            };
+            for (int p = 0; p < (int)lin.size() && survivors() < CB; p++)
+                if (!has_row(trows, lin[p])) trows.push_back(lin[p]);
+            // local order: in-chunk rows, the entering row, other input rows by input position, expanded rows
+            std::vector<int> local(inchunk.begin(), inchunk.end());
+            if (cand >= 0) local.push_back(cand);
+            for (int r : lin) if (has_row(trows, r) && !has_row(local, r)) local.push_back(r);
+            const int d_in = (int)local.size();
+            for (int r : exp_rows) local.push_back(r);
+            const int d = (int)local.size();
+            if (d > FP_MAXD || d > std::max(DMAX, 2 * CB)) return set_error(TG_ERR_TOO_BIG, "fused tile too large");
+            // output order
+            std::vector<int> out;
+            if (force) {
+                out = cout_;
+            } else {
+                std::vector<int> lowrows;
+                if (evict >= 0) {
+                    for (int b = 0; b <= CB && b < d; b++) if (local[b] != evict) lowrows.push_back(local[b]);
+                } else {
+                    for (int b = 0; b < CB; b++) if (!has_row(sel_rows, local[b])) lowrows.push_back(local[b]);
+                }
+                for (int r : lowrows) out.push_back(r);
+                for (int r : local) if (!has_row(out, r) && !has_row(sel_rows, r)) out.push_back(r);
+                for (int r : lin) if (!has_row(out, r) && !has_row(sel_rows, r)) out.push_back(r);
+            }
+            if ((int)out.size() != (int)cout_.size()) return set_error(TG_ERR_STATE, "output layout lost a row");
+            // the lowest output positions must be tile rows
+            for (int p = 0; p < CB && p < (int)out.size(); p++)
+                if (!has_row(local, out[p])) return set_error(TG_ERR_STATE, "output chunk rows outside the tile");
+            PassParams &pp = S.pp;
+            memset(&pp, 0, sizeof(pp));
+            pp.d = d;
+            pp.d_in = d_in;
+            for (int b = 0; b < d_in; b++) pp.loc_in[b] = 1ull << index_of(lin, local[b]);
+            uint32_t selmask = 0;
+            for (size_t k = 0; k < sel_rows.size(); k++) {
+                int lb = index_of(local, sel_rows[k]);
+                selmask |= 1u << lb;
+                if (sel_tg[k]) pp.sel_bits |= 1u << lb;
+            }
+            // compacted order = output order of the tile rows
+            int dout = 0;
+            for (int q = 0; q < (int)out.size(); q++) {
+                if (!has_row(local, out[q])) continue;
+                pp.cmp_out[dout] = 1ull << q;
+                pp.cmp_smem[dout] = 1u << index_of(local, out[q]);
+                dout++;
+            }
+            pp.d_out = dout;
+            for (int b = 0; b < CB; b++) {
+                if (pp.loc_in[b] != (1ull << b)) return set_error(TG_ERR_STATE, "input tile not contiguous");
+                if (pp.cmp_out[b] != (1ull << b)) return set_error(TG_ERR_STATE, "output tile not contiguous");
+            }
+            bool ident = true;
+            for (int b = 0; b < CB; b++) ident = ident && pp.cmp_smem[b] == (1u << b);
+            pp.fast_out = ident;
+            for (int q = 0; q < (1 << CB); q++) {
+                uint32_t sm = 0;
+                for (int b = 0; b < CB; b++) if ((q >> b) & 1) sm += pp.cmp_smem[b];
+                pp.pat[q] = (uint16_t)sm;
+            }
+            int no = 0;
+            for (int p = 0; p < (int)lin.size(); p++) {
+                if (has_row(local, lin[p])) continue;
+                if (no >= FP_MAXOUTER) return set_error(TG_ERR_TOO_BIG, "too many outer rows");
+                pp.outer_in[no] = 1ull << p;
+                pp.outer_out[no] = 1ull << index_of(out, lin[p]);
+                no++;
+            }
+            pp.n_outer = no;
+            pp.ntiles = 1ull << no;
+            pp.nupd = (int)upd.size();
+            for (int u = 0; u < pp.nupd; u++) {
+                uint32_t m = 0;
+                for (int r : upd[u].first) m |= 1u << index_of(local, r);
+                pp.upd_mask[u] = m;
+                pp.upd_w[u] = (uint8_t)upd[u].second;
+            }
+            if (eb == 1) build_groups(pp, selmask);
+            phys = out;
+            canon = cout_;
+            S.kind = 1;
+            S.w_out = (int)canon.size();
+            S.op_end = j0;
+            P.pass_bytes += (double)eb * ((1ull << w_in) + (1ull << S.w_out));
+
+        return TG_OK;
+    };
     while (i < nops) {
-        const int w_in = (int)active.size();
-        // stop at the next checkpoint
+        const int w_in = (int)canon.size();
         int64_t limit = nops;
         for (int64_t k = i + 1; k <= nops; k++)
             if (is_ckpt[k]) { limit = k; break; }
         Seg S;
         S.w_in = w_in;
-        if (w_in < SWB || (w_in == SWB && hops[i].code != 0)) {
-            // shared-memory sweep while the width stays within capacity
+        if (sweep_next(w_in, i) && phys != canon) {
+            e = build_pass(i, i, {}, true, S);
+            if (e) return e;
+        } else if (sweep_next(w_in, i)) {
             SweepParams &sp = S.sp;
             memset(&sp, 0, sizeof(sp));
             sp.w_in = w_in;
@@ -509,177 +945,95 @@ static int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int6
                 if (o.code == 0) {
                     if (w + 1 > SWB) break;
                     sp.ops[sp.nops++] = 0u;
-                    active.push_back(next_row++);
                     w++;
                 } else if (o.code == 1) {
                     sp.ops[sp.nops++] = (1u << 30) | ((uint32_t)o.b << 20) | (uint32_t)o.a;
                     P.n_updates++;
                 } else {
                     sp.ops[sp.nops++] = (2u << 30) | ((uint32_t)o.b << 6) | (uint32_t)o.a;
-                    active.erase(active.begin() + o.a);
                     w--;
                 }
+                apply_canon(j, canon);
                 j++;
             }
             if (j == i) return set_error(TG_ERR_STATE, "scheduler made no progress");
+            phys = canon;
             S.kind = 0;
             S.w_out = w;
             S.op_end = j;
             P.sweep_bytes += (double)eb * ((sp.has_in ? (1ull << w_in) : 0) + (1ull << w));
             i = j;
         } else {
-            // fused pass: grow the run of ops while the tile fits
-            const std::vector<int> lin = active;
-            auto in_set = [](const std::vector<int> &v, int r) { return std::find(v.begin(), v.end(), r) != v.end(); };
-            auto tile_rows = [&](const std::vector<int> &t, const std::vector<int> &lout) {
-                std::vector<int> s = t;
-                for (int p = 0; p < CB && p < (int)lin.size(); p++) if (!in_set(s, lin[p])) s.push_back(lin[p]);
-                for (int p = 0; p < CB && p < (int)lout.size(); p++) if (!in_set(s, lout[p])) s.push_back(lout[p]);
-                return s;
-            };
-            std::vector<int> cur = active, touched;
-            int nr = next_row, nupd = 0;
+            // ---- fused pass: grow the run of ops while the tile fits
+            const std::vector<int> lin = phys;
+            std::vector<int> inchunk(lin.begin(), lin.begin() + std::min<int>(CB, (int)lin.size()));
+            std::vector<int> cur = canon, touched;
+            int nupd = 0;
             int64_t j = i;
             while (j < limit && nupd < FP_MAXU) {
                 const HostOp &o = hops[j];
                 std::vector<int> t2 = touched, cur2 = cur;
-                if (o.code == 0) {
-                    cur2.push_back(nr);
-                    t2.push_back(nr);
-                } else if (o.code == 1) {
-                    for (int p = 0; p < (int)cur.size(); p++)
-                        if (((o.a >> p) & 1ull) && !in_set(t2, cur[p])) t2.push_back(cur[p]);
-                } else {
-                    if (!in_set(t2, cur[o.a])) t2.push_back(cur[o.a]);
-                    cur2.erase(cur2.begin() + o.a);
+                if (o.code == 0) t2.push_back(RI.exp_row[j]);
+                else if (o.code == 1) {
+                    for (int r : RI.upd_rows[j]) if (!has_row(t2, r)) t2.push_back(r);
+                } else if (!has_row(t2, RI.sel_row[j])) t2.push_back(RI.sel_row[j]);
+                apply_canon(j, cur2);
+                if ((int)cur2.size() < CB) break;
+                std::vector<int> need = t2;
+                for (int r : inchunk) if (!has_row(need, r)) need.push_back(r);
+                if (must_canon(j + 1, cur2)) {
+                    for (int p = 0; p < CB; p++) if (!has_row(need, cur2[p])) need.push_back(cur2[p]);
+                } else if (relayout) {
+                    need.push_back(-1);       // room for a row entering the in-chunk positions
                 }
-                if ((int)tile_rows(t2, cur2).size() > DMAX || (int)cur2.size() < CB) break;
+                if ((int)need.size() > DMAX) break;
                 touched.swap(t2);
                 cur.swap(cur2);
-                if (o.code == 0) nr++;
-                else if (o.code == 1) nupd++;
+                if (o.code == 1) nupd++;
                 j++;
             }
             if (j == i) {
-                // the op's rows do not fit a tile: one out-of-place pass for it alone
+                // the op's rows do not fit a tile: one out-of-place pass on the physical layout
                 const HostOp &o = hops[i];
                 S.kind = 2;
                 S.op_code = o.code;
-                S.op_a = o.a;
                 S.op_b = (uint32_t)o.b;
-                if (o.code == 0) active.push_back(next_row++);
-                else if (o.code == 2) active.erase(active.begin() + o.a);
-                else P.n_updates++;
-                S.w_out = (int)active.size();
+                if (o.code == 0) {
+                    S.op_a = 0;
+                    phys.push_back(RI.exp_row[i]);
+                } else if (o.code == 1) {
+                    uint64_t m = 0;
+                    for (int r : RI.upd_rows[i]) m |= 1ull << index_of(phys, r);
+                    S.op_a = m;
+                    P.n_updates++;
+                } else {
+                    int pp_ = index_of(phys, RI.sel_row[i]);
+                    S.op_a = (uint64_t)pp_;
+                    phys.erase(phys.begin() + pp_);
+                }
+                apply_canon(i, canon);
+                S.w_out = (int)canon.size();
                 S.op_end = i + 1;
                 P.pass_bytes += (double)eb * ((1ull << w_in) + (1ull << S.w_out));
                 i = i + 1;
-                buf ^= 1;
-                if (is_ckpt[S.op_end]) {
-                    for (size_t c = 0; c < P.ckpt_ops.size(); c++)
-                        if (P.ckpt_ops[c] == S.op_end) { S.ckpt = (int)c; break; }
-                }
-                P.segs.push_back(S);
-                continue;
+            } else {
+                e = build_pass(i, j, touched, false, S);
+                if (e) return e;
+                i = j;
             }
-            // the run's rows: expanded, selected (with targets) and the rows of every update
-            std::vector<int> lay = lin;
-            std::vector<int> exp_rows, sel_rows, sel_tg;
-            std::vector<std::pair<std::vector<int>, int>> upd;
-            for (int64_t k = i; k < j; k++) {
-                const HostOp &o = hops[k];
-                if (o.code == 0) {
-                    lay.push_back(next_row);
-                    exp_rows.push_back(next_row);
-                    next_row++;
-                } else if (o.code == 1) {
-                    std::vector<int> rr;
-                    for (int p = 0; p < (int)lay.size(); p++) if ((o.a >> p) & 1ull) rr.push_back(lay[p]);
-                    upd.push_back({rr, (int)o.b});
-                    P.n_updates++;
-                } else {
-                    sel_rows.push_back(lay[o.a]);
-                    sel_tg.push_back((int)o.b);
-                    lay.erase(lay.begin() + o.a);
-                }
-            }
-            const std::vector<int> &lout = lay;
-            std::vector<int> trows = tile_rows(touched, lout);
-            // pad with the lowest input positions for larger contiguous loads
-            const int w_total = w_in + (int)exp_rows.size();
-            int want = std::min(DMAX, std::max((int)trows.size(), std::min(13, w_total - 9)));
-            for (int p = 0; p < (int)lin.size() && (int)trows.size() < want; p++)
-                if (!in_set(trows, lin[p])) trows.push_back(lin[p]);
-            // local order: input rows by input position, then expanded rows in expand order
-            std::vector<int> local;
-            for (int p = 0; p < (int)lin.size(); p++) if (in_set(trows, lin[p])) local.push_back(lin[p]);
-            const int d_in = (int)local.size();
-            for (int r : exp_rows) local.push_back(r);
-            const int d = (int)local.size();
-            if (d > FP_MAXD || d > DMAX) return set_error(TG_ERR_TOO_BIG, "fused tile too large");
-            auto local_of = [&](int r) { return (int)(std::find(local.begin(), local.end(), r) - local.begin()); };
-            PassParams &pp = S.pp;
-            memset(&pp, 0, sizeof(pp));
-            pp.d = d;
-            pp.d_in = d_in;
-            for (int jb = 0; jb < d_in; jb++) {
-                int pos = (int)(std::find(lin.begin(), lin.end(), local[jb]) - lin.begin());
-                pp.loc_in[jb] = 1ull << pos;
-            }
-            uint32_t selmask = 0;
-            for (size_t k = 0; k < sel_rows.size(); k++) {
-                int lb = local_of(sel_rows[k]);
-                selmask |= 1u << lb;
-                if (sel_tg[k]) pp.sel_bits |= 1u << lb;
-            }
-            int dout = 0;
-            for (int jb = 0; jb < d; jb++) {
-                if ((selmask >> jb) & 1u) continue;
-                int pos = (int)(std::find(lout.begin(), lout.end(), local[jb]) - lout.begin());
-                pp.cmp_out[dout] = 1ull << pos;
-                pp.cmp_smem[dout] = 1u << jb;
-                dout++;
-            }
-            pp.d_out = dout;
-            // contiguity checks
-            for (int jb = 0; jb < CB; jb++) {
-                if (pp.loc_in[jb] != (1ull << jb)) return set_error(TG_ERR_STATE, "input tile not contiguous");
-                if (pp.cmp_out[jb] != (1ull << jb)) return set_error(TG_ERR_STATE, "output tile not contiguous");
-            }
-            pp.fast_out = (selmask & ((1u << CB) - 1)) == 0;
-            for (int q = 0; q < (1 << CB); q++) {
-                uint32_t s = 0;
-                for (int jb = 0; jb < CB; jb++) if ((q >> jb) & 1) s += pp.cmp_smem[jb];
-                pp.pat[q] = (uint16_t)s;
-            }
-            // outer rows: input rows outside the tile
-            int no = 0;
-            for (int p = 0; p < (int)lin.size(); p++) {
-                if (in_set(trows, lin[p])) continue;
-                if (no >= FP_MAXOUTER) return set_error(TG_ERR_TOO_BIG, "too many outer rows");
-                int po = (int)(std::find(lout.begin(), lout.end(), lin[p]) - lout.begin());
-                pp.outer_in[no] = 1ull << p;
-                pp.outer_out[no] = 1ull << po;
-                no++;
-            }
-            pp.n_outer = no;
-            pp.ntiles = 1ull << no;
-            pp.nupd = (int)upd.size();
-            for (int u = 0; u < pp.nupd; u++) {
-                uint32_t m = 0;
-                for (int r : upd[u].first) m |= 1u << local_of(r);
-                pp.upd_mask[u] = m;
-                pp.upd_w[u] = (uint8_t)upd[u].second;
-            }
-            active = lout;
-            S.kind = 1;
-            S.w_out = (int)lout.size();
-            S.op_end = j;
-            P.pass_bytes += (double)eb * ((1ull << w_in) + (1ull << S.w_out));
-            i = j;
         }
         buf ^= 1;
+        if (is_ckpt[S.op_end] && phys != canon) {
+            P.segs.push_back(S);
+            Seg R;
+            R.w_in = (int)canon.size();
+            e = build_pass(S.op_end, S.op_end, {}, true, R);
+            if (e) return e;
+            S = R;
+            buf ^= 1;
+        }
         if (is_ckpt[S.op_end]) {
+            if (phys != canon) return set_error(TG_ERR_STATE, "checkpoint with a non-canonical layout");
             for (size_t c = 0; c < P.ckpt_ops.size(); c++)
                 if (P.ckpt_ops[c] == S.op_end) { S.ckpt = (int)c; break; }
         }
@@ -700,6 +1054,8 @@ static int set_attrs() {
     e = cuda_check(cudaFuncSetAttribute(k_fused_pass<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 17), "attr");
     if (e) return e;
     e = cuda_check(cudaFuncSetAttribute(k_fused_pass<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 17), "attr");
+    if (e) return e;
+    e = cuda_check(cudaFuncSetAttribute(k_fused_pass_u8, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 17), "attr");
     if (e) return e;
     g_attr_done = true;
     return TG_OK;
@@ -747,9 +1103,15 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
             k_sweep_smem<E><<<1, 512, sm, st>>>(S.sp, src, dst);
         } else {
             size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
-            int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
-            uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
-            k_fused_pass<E><<<(unsigned)grid, FP_THREADS, sm, st>>>(S.pp, src, dst);
+            if (sizeof(E) == 1 && S.pp.use_groups) {
+                // persistent: one CTA per SM, two tile buffers
+                uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());
+                k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 2 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
+            } else {
+                int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
+                uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
+                k_fused_pass<E><<<(unsigned)grid, FP_THREADS, sm, st>>>(S.pp, src, dst);
+            }
         }
         e = cuda_check(cudaGetLastError(), "dense launch");
         if (e) return e;
@@ -770,6 +1132,61 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
 // Executes a scheduled plan on host memory with the kernels' own parameters and index
 // arithmetic (entry-level arithmetic instead of packed chunks).  Used by the CPU test-suite to
 // check the scheduler; the evaluators never call it.
+// the register-group update of k_fused_pass_u8 on host memory: same cosets, register model,
+// codes and lane arithmetic as run_group / grp_update
+static void emulate_groups(const PassParams &pp, uint8_t *T) {
+    const uint32_t ncos = 1u << (pp.d - 4 - 3);
+    for (int g = 0; g < pp.ngroups; g++) {
+        const GroupDesc &G = pp.groups[g];
+        for (uint32_t k = 0; k < ncos; k++) {
+            uint32_t c0 = k;
+            for (int j = 0; j < 3; j++) {
+                uint32_t lo = c0 & ((1u << G.piv[j]) - 1);
+                c0 = ((c0 ^ lo) << 1) | lo;
+            }
+            uint32_t R[64];
+            for (int x = 0; x < 8; x++) {
+                const uint8_t *ch = T + 16 * (size_t)(c0 ^ G.xoff[x]);
+                for (int wd = 0; wd < 4; wd++) {
+                    R[8 * x + 2 * wd] = ch[4 * wd] | ((uint32_t)ch[4 * wd + 2] << 16);
+                    R[8 * x + 2 * wd + 1] = ch[4 * wd + 1] | ((uint32_t)ch[4 * wd + 3] << 16);
+                }
+            }
+            auto sw = [](uint32_t v) { return (v >> 16) | (v << 16); };
+            auto addmin = [](uint32_t b, uint32_t w, uint32_t a) {
+                uint32_t lo = std::min((b & 0xFFFFu) + w, a & 0xFFFFu);
+                uint32_t hi = std::min((b >> 16) + w, a >> 16);
+                return lo | (hi << 16);
+            };
+            for (int u = 0; u < G.count; u++) {
+                uint32_t w = pp.uw[G.first + u];
+                uint32_t Y = (uint32_t)pp.ucode[G.first + u] << 3, HS = 0;
+                for (uint32_t i = 0; i < 64; i++) {
+                    uint32_t j = i ^ Y;
+                    if (Y == 0) {
+                        R[i] = addmin(sw(R[i]), w, R[i]);
+                    } else if (i < j) {
+                        uint32_t a = R[i], q = HS ? sw(R[j]) : R[j];
+                        uint32_t na = addmin(q, w, a), nq = addmin(a, w, q);
+                        R[i] = na;
+                        R[j] = HS ? sw(nq) : nq;
+                    }
+                }
+            }
+            for (int x = 0; x < 8; x++) {
+                uint8_t *ch = T + 16 * (size_t)(c0 ^ G.xoff[x]);
+                for (int wd = 0; wd < 4; wd++) {
+                    uint32_t e = R[8 * x + 2 * wd], o = R[8 * x + 2 * wd + 1];
+                    ch[4 * wd] = (uint8_t)(e & 0xFF);
+                    ch[4 * wd + 2] = (uint8_t)(e >> 16);
+                    ch[4 * wd + 1] = (uint8_t)(o & 0xFF);
+                    ch[4 * wd + 3] = (uint8_t)(o >> 16);
+                }
+            }
+        }
+    }
+}
+
 template <typename E>
 static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
     const int CB = Entry<E>::CB;
@@ -839,15 +1256,32 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
                 }
                 for (uint32_t c = nch_in; c < nch_all; c++)
                     for (int e = 0; e < (1 << CB); e++) T[((size_t)c << CB) + e] = (E)INF;
-                for (int u = 0; u < pp.nupd; u++) {
-                    uint32_t m = pp.upd_mask[u], w = pp.upd_w[u];
-                    int hb = 31 - __builtin_clz(m);
-                    for (uint32_t s = 0; s < (1u << pp.d); s++) {
-                        if ((s >> hb) & 1) continue;
-                        uint32_t t = s ^ m;
-                        E x = T[s], y = T[t];
-                        T[s] = (E)std::min<uint32_t>(x, (uint32_t)y + w);
-                        T[t] = (E)std::min<uint32_t>(y, (uint32_t)x + w);
+                const bool groups = sizeof(E) == 1 && pp.use_groups;
+                if (groups) {
+                    emulate_groups(pp, reinterpret_cast<uint8_t *>(T.data()));
+                    for (int u2 = 0; u2 < pp.nslow; u2++) {
+                        const int k2 = pp.slow_idx[u2];
+                        uint32_t m = pp.upd_mask[k2], w = pp.upd_w[k2];
+                        int hb = 31 - __builtin_clz(m);
+                        for (uint32_t s = 0; s < (1u << pp.d); s++) {
+                            if ((s >> hb) & 1) continue;
+                            uint32_t t = s ^ m;
+                            E x = T[s], y = T[t];
+                            T[s] = (E)std::min<uint32_t>(x, (uint32_t)y + w);
+                            T[t] = (E)std::min<uint32_t>(y, (uint32_t)x + w);
+                        }
+                    }
+                } else {
+                    for (int u = 0; u < pp.nupd; u++) {
+                        uint32_t m = pp.upd_mask[u], w = pp.upd_w[u];
+                        int hb = 31 - __builtin_clz(m);
+                        for (uint32_t s = 0; s < (1u << pp.d); s++) {
+                            if ((s >> hb) & 1) continue;
+                            uint32_t t = s ^ m;
+                            E x = T[s], y = T[t];
+                            T[s] = (E)std::min<uint32_t>(x, (uint32_t)y + w);
+                            T[t] = (E)std::min<uint32_t>(y, (uint32_t)x + w);
+                        }
                     }
                 }
                 for (uint32_t q = 0; q < nch_out; q++) {
@@ -855,8 +1289,20 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
                     uint32_t sidx = pp.sel_bits;
                     for (int j = 0; j < pp.d_out - CB; j++)
                         if ((q >> j) & 1) { off += pp.cmp_out[CB + j]; sidx += pp.cmp_smem[CB + j]; }
+                    if (groups && pp.store_mode == 1) {
+                        // output entry e <- the 32-entry span without local bit sel_low (value t)
+                        const int sb = pp.sel_low;
+                        const uint32_t t = (sidx >> sb) & 1u, base = (sidx >> 5) << 5;
+                        for (uint32_t e = 0; e < 16; e++) {
+                            uint32_t lo = e & ((1u << sb) - 1);
+                            uint32_t src_e = ((e ^ lo) << 1) | lo | (t << sb);
+                            dst[off + e] = T[base + src_e];
+                        }
+                        continue;
+                    }
+                    const bool fast = groups ? pp.store_mode == 0 : pp.fast_out;
                     for (int e = 0; e < (1 << CB); e++) {
-                        uint32_t si = pp.fast_out ? sidx + e : sidx + pp.pat[e];
+                        uint32_t si = fast ? sidx + e : sidx + pp.pat[e];
                         dst[off + e] = T[si];
                     }
                 }
@@ -954,18 +1400,22 @@ int tg_dense_plan_info(void *plan, int64_t *info, int ninfo) {
 }
 
 int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg) {
-    // per segment: kind, w_in, w_out, op_end, tile bits (or sweep capacity), updates in the segment
+    // per segment: kind, w_in, w_out, op_end, tile bits (or sweep capacity), updates in the segment,
+    // register groups (0: shared-memory updates), store mode
     if (!plan) return set_error(TG_ERR_ARG, "null plan");
     const DensePlan &P = *static_cast<DensePlan *>(plan);
     int64_t k = 0;
     for (const Seg &S : P.segs) {
         if (k >= maxseg) break;
-        out[6 * k + 0] = S.kind;
-        out[6 * k + 1] = S.w_in;
-        out[6 * k + 2] = S.w_out;
-        out[6 * k + 3] = S.op_end;
-        out[6 * k + 4] = S.kind == 1 ? S.pp.d : S.kind == 0 ? S.sp.max_bits : -1;
-        out[6 * k + 5] = S.kind == 1 ? S.pp.nupd : S.kind == 0 ? S.sp.nops : (S.op_code == 1);
+        int64_t *o = out + 8 * k;
+        o[0] = S.kind;
+        o[1] = S.w_in;
+        o[2] = S.w_out;
+        o[3] = S.op_end;
+        o[4] = S.kind == 1 ? S.pp.d : S.kind == 0 ? S.sp.max_bits : -1;
+        o[5] = S.kind == 1 ? S.pp.nupd : S.kind == 0 ? S.sp.nops : (S.op_code == 1);
+        o[6] = S.kind == 1 && S.pp.use_groups ? S.pp.ngroups : 0;
+        o[7] = S.kind == 1 ? S.pp.store_mode : -1;
         k++;
     }
     return (int)k;
@@ -1050,7 +1500,7 @@ int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_h
 }
 
 int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16) {
-    if (dmax8 < 5 || dmax8 > 17 || dmax16 < 4 || dmax16 > 16 || sweep_bits8 < 4 || sweep_bits8 > 16 ||
+    if (dmax8 < 5 || dmax8 > 16 || dmax16 < 4 || dmax16 > 16 || sweep_bits8 < 4 || sweep_bits8 > 16 ||
         sweep_bits16 < 3 || sweep_bits16 > 15)
         return set_error(TG_ERR_ARG, "tuning out of range");
     g_dmax8 = dmax8; g_dmax16 = dmax16; g_sweep_bits8 = sweep_bits8; g_sweep_bits16 = sweep_bits16;

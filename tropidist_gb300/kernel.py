@@ -57,7 +57,7 @@ class CompiledPlan:
         self.pass_bytes, self.sweep_bytes = int(info[6]), int(info[7])
 
     def segments(self):
-        out = np.zeros((self.nsegs, 6), dtype=np.int64)
+        out = np.zeros((self.nsegs, 8), dtype=np.int64)
         _lib.lib().tg_dense_plan_segments(self.handle, out.ctypes.data, self.nsegs)
         return out
 

@@ -79,12 +79,16 @@ def banded(m, n, window, col_weight=3, nobs=1, seed=0, p_logical=0.5, name=None)
         h.append(int(sum(1 << int(r) for r in rows)))
     basis = _basis(_rows_of(h, m, n))
     lrows = []
+    if len(basis) >= n:
+        raise ValueError("H has full column rank: every logical row is in its row space")
     for _ in range(nobs):
-        while True:
+        for _attempt in range(10000):
             bits = rng.random(n) < p_logical
             v = int(sum(1 << j for j in np.flatnonzero(bits).tolist()))
             if v and not _row_space_member(basis, v):
                 break
+        else:
+            raise ValueError("no logical row outside the row space of H was drawn")
         lrows.append(v)
     l = [0] * n
     for o, v in enumerate(lrows):
