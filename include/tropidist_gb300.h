@@ -60,6 +60,8 @@ int tg_dense_result(void *plan, void *buf_a, void *buf_b, uint32_t *value, void 
 /* execute with a CUDA event pair around every launch (on `stream`), waits for the end; out[9]:
  * for shared-memory sweeps, fused passes and one-op passes: launches, total ms, table bytes */
 int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, double *out, int nout);
+/* per-segment launch times (ms) of the plan's last timed execution; returns the count */
+int tg_dense_segment_ms(void *plan, float *out, int64_t maxseg);
 int tg_dense_run(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
                  uint32_t *value, void *stream);
 int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16);

@@ -312,8 +312,8 @@ __device__ __forceinline__ uint32_t pdep_w32(uint32_t x, const uint32_t *wt, int
     return r;
 }
 
-#define FP_THREADS 256
-#define FP_TBITS 8
+#define FP_THREADS 512
+#define FP_TBITS 9
 
 template <typename E>
 __global__ void __launch_bounds__(FP_THREADS) k_fused_pass(const __grid_constant__ PassParams P,
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(FP_THREADS) k_fused_pass(const __grid_constant
 // thread's own part (computed once) plus an iteration part that is the same for every thread
 // (tables in shared memory), and the tile bases advance by a carry table (tile t+1 differs from
 // tile t in the bits up to the lowest zero bit of t).
-#define FP_MAXIT 16
+#define FP_MAXIT 8
 __global__ void __launch_bounds__(FP_THREADS, 1) k_fused_pass_u8(const __grid_constant__ PassParams P,
                                                                 const uint8_t *__restrict__ in,
                                                                 uint8_t *__restrict__ out) {
@@ -441,20 +441,26 @@ __global__ void __launch_bounds__(FP_THREADS, 1) k_fused_pass_u8(const __grid_co
         ob += s_cout[k];
     };
 
-    uint4 *const buf0 = smem_raw, *const buf1 = smem_raw + nch_all;
+    // three tile buffers: tiles t + 1 and t + 2 load while tile t is computed and stored
+    uint4 *const buf0 = smem_raw, *const buf1 = smem_raw + nch_all, *const buf2 = smem_raw + 2 * nch_all;
     int cur = 0;
-    uint64_t ib = ib0, ob = ob0, ibn = ib0, obn = ob0;
-    if (t0 < t1) issue_load(ib, buf0);
+    uint64_t ob = ob0, ibn = ib0, dummy = 0;
+    uint64_t tl = t0;          // next tile to load (ibn: its input base)
+    if (tl < t1) { issue_load(ibn, buf0); tl++; }
+    if (tl < t1) { advance(tl - 1, ibn, dummy); issue_load(ibn, buf1); tl++; }
     for (uint64_t tile = t0; tile < t1; tile++) {
-        if (tile + 1 < t1) {
-            advance(tile, ibn, obn);
-            issue_load(ibn, cur ? buf0 : buf1);
-            cp_async_wait_group<1>();
-        } else {
-            cp_async_wait_group<0>();
+        if (tl < t1) {
+            advance(tl - 1, ibn, dummy);
+            const int slot = (cur + 2) % 3;
+            issue_load(ibn, slot == 0 ? buf0 : slot == 1 ? buf1 : buf2);
+            tl++;
         }
+        const uint64_t ahead = tl - 1 - tile;        // loads still allowed in flight
+        if (ahead >= 2) cp_async_wait_group<2>();
+        else if (ahead == 1) cp_async_wait_group<1>();
+        else cp_async_wait_group<0>();
         __syncthreads();
-        uint4 *TC = cur ? buf1 : buf0;
+        uint4 *TC = cur == 0 ? buf0 : cur == 1 ? buf1 : buf2;
         const uint8_t *T = reinterpret_cast<const uint8_t *>(TC);
         for (int g = 0; g < P.ngroups; g++) {
             run_group<FP_THREADS>(TC, P.d, P.groups[g], P.ucode, P.uw);
@@ -490,11 +496,9 @@ __global__ void __launch_bounds__(FP_THREADS, 1) k_fused_pass_u8(const __grid_co
             __stcs(reinterpret_cast<uint4 *>(dstb + s_out_hi[it]), v);
         }
         __syncthreads();
-        cur ^= 1;
-        ib = ibn;
-        ob = obn;
+        cur = cur == 2 ? 0 : cur + 1;
+        if (tile + 1 < t1) advance(tile, dummy, ob);
     }
-    (void)ib;
 }
 
 // ------------------------------------------------------------------ one op, out of place (wide masks)
@@ -555,6 +559,7 @@ struct DensePlan {
     int final_buf;          // buffer holding the final table (0: a, 1: b)
     int64_t n_updates;
     double pass_bytes;      // algorithmic bytes moved by the fused passes
+    std::vector<float> seg_ms;  // per-segment launch time of the last timed execution
     double sweep_bytes;     // bytes read + written by the shared-memory sweeps
 };
 
@@ -824,7 +829,7 @@ static int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int6
             }
             // pad with the lowest input positions (larger contiguous loads, >= 7 local bits)
             const int w_total = w_in + (int)exp_rows.size();
-            int want = std::min(DMAX, std::max((int)trows.size(), std::max(7, std::min(13, w_total - 9))));
+            int want = std::min(DMAX, std::max((int)trows.size(), std::max(7, w_total - 10)));
             for (int p = 0; p < (int)lin.size() && (int)trows.size() < want; p++)
                 if (!has_row(trows, lin[p])) trows.push_back(lin[p]);
             // the four lowest output positions must hold tile rows that survive the pass
@@ -1055,7 +1060,7 @@ static int set_attrs() {
     if (e) return e;
     e = cuda_check(cudaFuncSetAttribute(k_fused_pass<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 17), "attr");
     if (e) return e;
-    e = cuda_check(cudaFuncSetAttribute(k_fused_pass_u8, cudaFuncAttributeMaxDynamicSharedMemorySize, 1 << 17), "attr");
+    e = cuda_check(cudaFuncSetAttribute(k_fused_pass_u8, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 << 16), "attr");
     if (e) return e;
     g_attr_done = true;
     return TG_OK;
@@ -1104,9 +1109,9 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
         } else {
             size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
             if (sizeof(E) == 1 && S.pp.use_groups) {
-                // persistent: one CTA per SM, two tile buffers
+                // persistent: one CTA per SM, three tile buffers
                 uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());
-                k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 2 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
+                k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 3 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
             } else {
                 int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
                 uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
@@ -1423,6 +1428,14 @@ int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg) {
 
 void tg_dense_plan_free(void *plan) { delete static_cast<DensePlan *>(plan); }
 
+int tg_dense_segment_ms(void *plan, float *out, int64_t maxseg) {
+    if (!plan || !out) return set_error(TG_ERR_ARG, "null argument");
+    const DensePlan &P = *static_cast<DensePlan *>(plan);
+    int64_t k = 0;
+    for (; k < maxseg && k < (int64_t)P.seg_ms.size(); k++) out[k] = P.seg_ms[k];
+    return (int)k;
+}
+
 int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, void *stream) {
     if (!plan || !buf_a || !buf_b) return set_error(TG_ERR_ARG, "null plan or buffer");
     const DensePlan &P = *static_cast<DensePlan *>(plan);
@@ -1451,10 +1464,13 @@ int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, d
     e = cuda_check(cudaEventSynchronize(g_events[2 * P.segs.size() - 1]), "event sync");
     if (e) return e;
     double acc[9] = {0};
+    DensePlan &PM = *static_cast<DensePlan *>(plan);
+    PM.seg_ms.assign(P.segs.size(), 0.f);
     for (size_t k = 0; k < P.segs.size(); k++) {
         const Seg &S = P.segs[k];
         float ms = 0.f;
         cudaEventElapsedTime(&ms, g_events[2 * k], g_events[2 * k + 1]);
+        PM.seg_ms[k] = ms;
         int kk = S.kind;
         acc[3 * kk] += 1;
         acc[3 * kk + 1] += ms;

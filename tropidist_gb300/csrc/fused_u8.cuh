@@ -9,11 +9,11 @@
 // (8 chunks = 128 entries) into registers, applies every update of the group there and writes it
 // back: one shared-memory round trip per group instead of one per update.
 //
-// Register file: R[8 * x + k], k = 2 * word + parity, holds the entries 4 * word + parity and
-// 4 * word + parity + 2 of chunk x as two 16-bit lanes (bytes widened to halfwords).  A group
+// Register file: R[4 * x + k] holds word k (entries 4k .. 4k+3, packed bytes) of chunk x.  A group
 // holds only updates without in-chunk bits (the scheduler keeps rows that are being updated out
 // of the four in-chunk positions; the rare others run in shared memory), so an update with chunk
-// coordinates y (b-basis) pairs R[8x + k] with R[8(x ^ y) + k].  y is dispatched through a switch
+// coordinates y (b-basis) pairs chunk x with chunk x ^ y word for word; each word pair is widened
+// to 16-bit lanes once for both directions (minplus_pair_u8x4).  y is dispatched through a switch
 // to code unrolled by template recursion: every register index is a compile-time constant.
 #pragma once
 #include "tg_common.cuh"
@@ -38,24 +38,21 @@ __device__ __forceinline__ void unpack_eo(uint32_t w, uint32_t &e, uint32_t &o) 
 }
 __device__ __forceinline__ uint32_t pack_eo(uint32_t e, uint32_t o) { return e | (o << 8); }
 
-// chunk-level update: R[8x + k] pairs with R[8(x ^ Y) + k], unrolled by template recursion
+// chunk-level update on packed words: chunk X (R[4X .. 4X+3]) pairs with chunk X ^ Y, unrolled
+// by template recursion (every register index is a compile-time constant)
 template <int Y, int X>
 struct GrpPairs {
-    static __device__ __forceinline__ void run(uint32_t (&R)[64], uint32_t w2) {
+    static __device__ __forceinline__ void run(uint32_t (&R)[32], uint32_t w2) {
         if constexpr (X < (X ^ Y)) {
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-                const uint32_t a = R[8 * X + k], b = R[8 * (X ^ Y) + k];
-                R[8 * X + k] = __viaddmin_u16x2(b, w2, a);
-                R[8 * (X ^ Y) + k] = __viaddmin_u16x2(a, w2, b);
-            }
+            for (int k = 0; k < 4; k++) minplus_pair_u8x4(R[4 * X + k], R[4 * (X ^ Y) + k], w2);
         }
         if constexpr (X < 7) GrpPairs<Y, X + 1>::run(R, w2);
     }
 };
 
 // y in 1..7: the update's chunk mask in the coset basis
-__device__ __forceinline__ void grp_dispatch(uint32_t y, uint32_t (&R)[64], uint32_t w2) {
+__device__ __forceinline__ void grp_dispatch(uint32_t y, uint32_t (&R)[32], uint32_t w2) {
     switch (y) {
         case 1: GrpPairs<1, 0>::run(R, w2); break;
         case 2: GrpPairs<2, 0>::run(R, w2); break;
@@ -76,29 +73,19 @@ __device__ __forceinline__ void run_group(uint4 *TC, int d, const GroupDesc &g, 
     const int p0 = g.piv[0], p1 = g.piv[1], p2 = g.piv[2];
     for (uint32_t k = threadIdx.x; k < ncos; k += NT) {
         // coset representative: k with zero bits inserted at the pivots (ascending)
-        uint32_t c0 = insert_zero(insert_zero(insert_zero(k, p0), p1), p2);
-        uint32_t R[64];
+        const uint32_t c0 = insert_zero(insert_zero(insert_zero(k, p0), p1), p2);
+        uint32_t R[32];
 #pragma unroll
         for (int x = 0; x < 8; x++) {
-            uint4 v = TC[c0 ^ g.xoff[x]];
-            unpack_eo(v.x, R[8 * x + 0], R[8 * x + 1]);
-            unpack_eo(v.y, R[8 * x + 2], R[8 * x + 3]);
-            unpack_eo(v.z, R[8 * x + 4], R[8 * x + 5]);
-            unpack_eo(v.w, R[8 * x + 6], R[8 * x + 7]);
+            const uint4 v = TC[c0 ^ g.xoff[x]];
+            R[4 * x + 0] = v.x; R[4 * x + 1] = v.y; R[4 * x + 2] = v.z; R[4 * x + 3] = v.w;
         }
         for (int u = 0; u < g.count; u++) {
             const uint32_t w = uw[g.first + u];
             grp_dispatch(ucode[g.first + u], R, w | (w << 16));
         }
 #pragma unroll
-        for (int x = 0; x < 8; x++) {
-            uint4 v;
-            v.x = pack_eo(R[8 * x + 0], R[8 * x + 1]);
-            v.y = pack_eo(R[8 * x + 2], R[8 * x + 3]);
-            v.z = pack_eo(R[8 * x + 4], R[8 * x + 5]);
-            v.w = pack_eo(R[8 * x + 6], R[8 * x + 7]);
-            TC[c0 ^ g.xoff[x]] = v;
-        }
+        for (int x = 0; x < 8; x++) TC[c0 ^ g.xoff[x]] = make_uint4(R[4 * x], R[4 * x + 1], R[4 * x + 2], R[4 * x + 3]);
     }
 }
 
