@@ -65,6 +65,23 @@ int tg_dense_segment_ms(void *plan, float *out, int64_t maxseg);
 int tg_dense_run(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
                  uint32_t *value, void *stream);
 int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16);
+
+/* Allocation-free whole-plan run (uint8 tables).  No counterpart in the reference: its C kernels
+ * never allocate, because numpy owns the one table buffer (cdist/kernel.py:101-103), whereas the
+ * GPU executor needs a second, ping-pong table.  This variant is for callers that cannot allocate
+ * device memory, such as a runtime that owns the whole device-memory budget, or a caller on a stream
+ * where a synchronizing cudaMalloc would stall concurrent work.  It takes the second table from a
+ * 4 MiB array held in device memory by the library itself.  Limits and rules:
+ *   - plans up to peak_bits = 22; wider plans return -4 (TG_ERR_TOO_BIG) and launch nothing;
+ *   - table_dev (device, >= 2^peak_bits bytes) is the caller's first table and is overwritten;
+ *   - value (host) receives the final entry (255 = INF), and the call waits for it;
+ *   - no device memory is allocated or freed;
+ *   - the first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *   - every call shares the one array, so calls that overlap on the GPU (other streams, other
+ *     host threads) race: run them one after another. */
+int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, uint64_t table_entries,
+                         uint32_t *value, void *stream);
 /* Runs a scheduled plan on HOST buffers with the launch parameters and index arithmetic of the
  * kernels; for checking the scheduler on a machine without a GPU.  Not an evaluator. */
 int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_host);

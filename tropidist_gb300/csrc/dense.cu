@@ -1319,6 +1319,35 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
     }
 }
 
+// ------------------------------------------------------------------ allocation-free entry point
+// Some callers cannot allocate device memory: a runtime that owns the whole device-memory budget
+// and hands out only the buffers it planned for (a serving engine's pool, another framework's
+// arena), or a caller on a latency-critical stream where cudaMalloc / cudaFree would synchronize
+// the device and stall concurrent work.  For them, tg_dense_run_noalloc runs a whole plan with
+// the second (ping-pong) table in this file-scope array instead of a caller-provided buffer.  Every
+// GPU that loads the library holds the array until the process exits.
+#define TG_NOALLOC_MAX_BITS 22
+static __device__ __align__(256) uint8_t g_noalloc_scratch[1u << TG_NOALLOC_MAX_BITS];
+#define TG_NOALLOC_MAX_DEVICES 64
+static uint8_t *g_noalloc_ptr[TG_NOALLOC_MAX_DEVICES];
+
+// device address of the scratch array on the current device (looked up once per device; the
+// array's name in host code is only a stand-in, not an address a kernel may use)
+static int noalloc_scratch(uint8_t **out) {
+    int dev = 0;
+    int e = cuda_check(cudaGetDevice(&dev), "get device");
+    if (e) return e;
+    if (dev < 0 || dev >= TG_NOALLOC_MAX_DEVICES) return set_error(TG_ERR_TOO_BIG, "device index beyond the table");
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "scratch symbol address");
+        if (e) return e;
+        g_noalloc_ptr[dev] = static_cast<uint8_t *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return TG_OK;
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -1512,6 +1541,37 @@ int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_h
     const DensePlan &P = *static_cast<DensePlan *>(plan);
     if (P.eb == 1) emulate_plan<uint8_t>(P, (uint8_t *)host_a, (uint8_t *)host_b, ckpt_host);
     else emulate_plan<uint16_t>(P, (uint16_t *)host_a, (uint16_t *)host_b, ckpt_host);
+    return TG_OK;
+}
+
+int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, uint64_t table_entries,
+                         uint32_t *value, void *stream) {
+    if (!value || (nops > 0 && !ops) || nops < 0) return set_error(TG_ERR_ARG, "bad op stream or result pointer");
+    if (!table_dev) return set_error(TG_ERR_ARG, "null table");
+    DensePlan P;
+    int e = build_dense_plan(ops, nops, 1, nullptr, 0, P);
+    if (e) return e;
+    if (P.peak_bits > TG_NOALLOC_MAX_BITS)
+        return set_error(TG_ERR_TOO_BIG, "plan wider than the 2^22-entry scratch of tg_dense_run_noalloc");
+    if (table_entries < (1ull << P.peak_bits)) return set_error(TG_ERR_ARG, "table buffer smaller than 2^peak_bits");
+    uint8_t *scratch = nullptr;
+    e = noalloc_scratch(&scratch);
+    if (e) return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the start table {0: 0} is the first entry of the caller's table; the scratch needs no
+    // clearing: every launch writes its whole output table before anything reads it
+    e = cuda_check(cudaMemsetAsync(table_dev, 0, 1, st), "init");
+    if (e) return e;
+    if (nops > 0) {
+        e = launch_plan<uint8_t>(P, table_dev, scratch, nullptr, st);
+        if (e) return e;
+    }
+    uint32_t v = 0;
+    e = cuda_check(cudaMemcpyAsync(&v, P.final_buf ? scratch : table_dev, 1, cudaMemcpyDeviceToHost, st), "result copy");
+    if (e) return e;
+    e = cuda_check(cudaStreamSynchronize(st), "result sync");
+    if (e) return e;
+    *value = v;
     return TG_OK;
 }
 
