@@ -306,7 +306,9 @@ def main():
                 "algorithmic_bytes_per_launch": bytes_fp / n_fp if n_fp else None,
                 "avg_launch_us": 1e3 * ms_fp / n_fp if n_fp else None, "launches": int(n_fp),
                 "share_of_gpu_time": ms_fp / ms if ms else None,
-                "traffic": (tr or {}).get("bytes_per_launch_at_bench") if tr else None}
+                "traffic": (tr["ratio"] * bytes_fp / n_fp) if (tr and n_fp) else None,
+                "traffic_source": ("ncu DRAM bytes / algorithmic bytes = %.3f on %s, scaled to the average launch"
+                                   % (tr["ratio"], tr["source"])) if tr else None}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded banded problem)",
