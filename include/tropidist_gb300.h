@@ -86,6 +86,26 @@ int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, u
  * kernels; for checking the scheduler on a machine without a GPU.  Not an evaluator. */
 int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_host);
 
+/* ---------------------------------------------------------------- sparse Rank DP (device tables)
+ * A table: n packed states key | value << 56 (key = row-slot parities, <= 56 slots; value 0..254),
+ * the format of the reference's C tables (cdist/sparse_dp.c:3-4), in a device array, plus a device
+ * index of 2^lg slots (open addressing, empty slot = all ones).  counters: device uint64[4] =
+ * new keys, changed states, error flags (1 index full, 2 changed list full, 4 array full), states
+ * written.  These replace sp_candidates + sp_merge (cdist/sparse_dp.c:118-202, bound by
+ * cdist/sparse_dp.py:487-497) with one step on device tables. */
+int tg_sp_clear(void *H, uint64_t cap, void *stream);
+int tg_sp_step(const void *A, uint64_t n, const void *Hold, int lg_old, void *Hnew, int lg_new, void *Anew,
+               uint64_t anew_cap, void *changed, uint64_t changed_cap, uint64_t upd, uint64_t sel_mask,
+               uint64_t sel_bits, int cap, int keep_below, int w, int want_changed, int use_h, int K, int ncls,
+               const uint64_t *masks, const int64_t *weights, int64_t extra, uint64_t tmask, void *counters,
+               void *stream);
+int tg_sp_build(const void *A, uint64_t n, void *H, int lg, int below, void *kept, void *counters, void *stream);
+/* replaces sp_join (cdist/sparse_dp.c:207-236): result (device uint64) = min (total << 56 | fkey) */
+int tg_sp_join(const void *F, uint64_t nf, const void *Hb, int lgb, uint64_t tmask, void *result, void *stream);
+int tg_sp_lookup(const void *H, int lg, const void *keys, uint64_t n, void *vals, void *stream);
+/* replaces sp_hist (cdist/sparse_dp.c:239-242): hist is a device uint64[256] */
+int tg_sp_hist(const void *A, uint64_t n, void *hist, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

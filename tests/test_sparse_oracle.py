@@ -1,0 +1,117 @@
+"""Sparse Rank DP host driver (Trellis, Sweep, query) with the numpy oracle tables, against the
+reference's own outputs: slots and masks, per-cut tables, query values and valid witnesses."""
+import itertools
+
+import numpy as np
+
+from helpers import golden, sha, unhex
+from oracle.sparse import NumpyTables, bound
+from tropidist_gb300 import sparse_dp, synth
+from tropidist_gb300.problem import Problem
+
+
+def _problem(case):
+    return Problem("rand", case["m"], case["k"], case["h"], case["l"])
+
+
+def check_witness(p, cols, value, obs=None):
+    s = lg = 0
+    for j in cols:
+        s ^= p.h[j]
+        lg ^= p.l[j]
+    assert s == 0 and len(cols) == value == len(set(cols))
+    assert ((lg >> obs) & 1) if obs is not None else lg != 0
+
+
+def test_trellis_matches_reference():
+    for case in golden("sparse_random.json"):
+        tr = sparse_dp.Trellis.for_query(_problem(case), case["obs"], case["order"])
+        assert tr.feasible == case["feasible"]
+        if tr.feasible:
+            assert tr.nslots == case["nslots"] and tr.slot == case["slot"]
+            assert tr.tmask == case["tmask"] and tr.col == case["col"]
+
+
+def test_query_values_with_oracle_tables():
+    checked = 0
+    for case in golden("sparse_random.json"):
+        if not case["feasible"]:
+            continue
+        p = _problem(case)
+        tr = sparse_dp.Trellis.for_query(p, case["obs"], case["order"])
+        for run in case["runs"]:
+            r = sparse_dp.query(tr, run["K"], mode=run["mode"], split=run["split"], use_h=run["use_h"],
+                                backend=NumpyTables(tr))
+            assert r["value"] == run["value"], run
+            assert r["peak_states"] == run["peak_states"], run
+            if run["value"] is not None:
+                check_witness(p, r["witness"], run["value"], case["obs"])
+            checked += 1
+    assert checked > 1000
+
+
+def test_tables_at_every_cut_match_reference():
+    for case in golden("sparse_tables.json"):
+        p = Problem("t", case["nrows"], 1, unhex(case["h"]), unhex(case["l"]))
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        sw = sparse_dp.Sweep(tr, +1 if case["forward"] else -1, case["K"], case["K"], use_h=case["use_h"], every=1,
+                             backend=NumpyTables(tr))
+        sw.run()
+        assert sw.counts == case["counts"]
+        for c, (n, hk, hv) in case["tables"].items():
+            keys, vals = sw.ckpt[int(c)]
+            assert keys.size == n and sha(keys) == hk and sha(vals) == hv, c
+
+
+def test_lookahead_is_admissible():
+    """The bound never exceeds the exact remaining cost (the untruncated sweep from the other side)."""
+    p = synth.dense_small(3)
+    tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+    for fwd in (True, False):
+        exact = sparse_dp.Sweep(tr, -1 if fwd else +1, 40, 40, use_h=False, every=1, backend=NumpyTables(tr))
+        exact.run()
+        hd = tr.bound_data(fwd)
+        for c in range(0, tr.N + 1, 7):
+            keys, vals = exact.ckpt[c]
+            h = bound(keys ^ np.uint64(tr.tmask[c]), tr.tmask[c], hd[c])
+            assert (h <= vals.astype(np.int64)).all(), (fwd, c)
+
+
+def brute(p, obs, weights=None):
+    best = None
+    for w in range(1, p.ncols + 1):
+        if weights is None and best is not None:
+            break
+        for cols in itertools.combinations(range(p.ncols), w):
+            s = lg = 0
+            for j in cols:
+                s ^= p.h[j]
+                lg ^= p.l[j]
+            if s == 0 and (lg >> obs) & 1:
+                c = w if weights is None else sum(weights[j] for j in cols)
+                best = c if best is None else min(best, c)
+    return best
+
+
+def test_weighted_columns_against_brute_force():
+    import random
+    rng = random.Random(17)
+    for _ in range(40):
+        n, m = rng.randint(2, 10), rng.randint(1, 6)
+        h = [sum(1 << r for r in range(m) if rng.random() < 0.35) for _ in range(n)]
+        l = [rng.randrange(0, 2) for _ in range(n)]
+        wts = [rng.randint(1, 3) for _ in range(n)]
+        p = Problem("w", m, 1, h, l, weights=wts)
+        order = list(range(n))
+        rng.shuffle(order)
+        tr = sparse_dp.Trellis.for_query(p, 0, order)
+        truth = brute(p, 0, wts)
+        if not tr.feasible:
+            assert truth is None
+            continue
+        K = sum(wts) + 1
+        for mode in ("forward", "mitm"):
+            r = sparse_dp.query(tr, K, mode=mode, backend=NumpyTables(tr))
+            assert r["value"] == truth, (mode, r["value"], truth)
+            if truth is not None:
+                assert sum(wts[j] for j in r["witness"]) == truth

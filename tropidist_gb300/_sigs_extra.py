@@ -1,2 +1,14 @@
 """ctypes signatures of the sparse-DP, completion-table and batching entry points."""
-SIGNATURES = {}
+import ctypes as c
+
+vp, u64, i64, ci = c.c_void_p, c.c_uint64, c.c_int64, c.c_int
+
+SIGNATURES = {
+    "tg_sp_clear": (ci, [vp, u64, vp]),
+    "tg_sp_step": (ci, [vp, u64, vp, ci, vp, ci, vp, u64, vp, u64, u64, u64, u64, ci, ci, ci, ci, ci, ci, ci,
+                        vp, vp, i64, u64, vp, vp]),
+    "tg_sp_build": (ci, [vp, u64, vp, ci, ci, vp, vp, vp]),
+    "tg_sp_join": (ci, [vp, u64, vp, ci, u64, vp, vp]),
+    "tg_sp_lookup": (ci, [vp, ci, vp, u64, vp, vp]),
+    "tg_sp_hist": (ci, [vp, u64, vp, vp]),
+}

@@ -1,0 +1,328 @@
+// Sparse (weight-truncated) Rank DP on the GPU: device hash tables of packed states.
+//
+// A state is packed like the reference's C tables (cdist/sparse_dp.c:3-4): key | value << 56, the
+// key being the partial parities of the row slots (at most 56).  A table lives in two forms:
+//   - an array of its n packed states (any order; a table is a set), and
+//   - an open-addressing hash index of capacity 2^lg (linear probing, EMPTY = all ones), holding the
+//     same packed states, used for lookups.
+// One column step (cdist/sparse_dp.py:338-403, NumpyTables.step) is three kernels:
+//   clear  the new index;
+//   step   for every old state (key, v): the old state itself, if it passes the closing-row filter
+//          ((key & sel_mask) == sel_bits, then those bits cleared), the cap and the lookahead bound,
+//          is inserted with atomicMin; its candidate key ^ upd with value v + w (from v < cap) goes
+//          through the same filters; a candidate is "changed" when no old state with its key has a
+//          value <= its own (looked up in the OLD index), it is inserted when it improves an old
+//          state or when it is new and below keep_below;
+//   compact  the new index's occupied slots into the new array.
+// Because the step's result is a set of per-key minima, it does not depend on the order in which
+// threads insert: the tables equal the reference's entry for entry (as sets).
+#include "tg_common.cuh"
+#include "tg_capi.h"
+
+#include <cstring>
+#include <vector>
+
+namespace tg {
+
+#define SP_EMPTY 0xFFFFFFFFFFFFFFFFull
+#define SP_KEYMASK ((1ull << 56) - 1)
+#define SP_QW 720720ll          // the lookahead weights are multiples of 1/QW (cdist/sparse_dp.py:48)
+#define SP_MAXCLS 48
+
+struct BoundParams {
+    int on;                     // 0: no lookahead
+    int ncls;
+    int K;
+    int pad;
+    int64_t extra;
+    uint64_t tmask;
+    uint64_t mask[SP_MAXCLS];
+    int64_t w[SP_MAXCLS];
+};
+
+// ceil((extra + sum_c w_c * |(key ^ tmask) & mask_c|) / QW)   (cdist/sparse_dp.py:208-217)
+__device__ __forceinline__ int64_t sp_hbound(const BoundParams &b, uint64_t key) {
+    const uint64_t u = key ^ b.tmask;
+    int64_t tot = b.extra;
+    for (int c = 0; c < b.ncls; c++) tot += b.w[c] * (int64_t)__popcll(u & b.mask[c]);
+    return (tot + SP_QW - 1) / SP_QW;
+}
+
+__device__ __forceinline__ bool sp_keep(const BoundParams &b, uint64_t key, uint32_t v) {
+    return !b.on || (int64_t)v + sp_hbound(b, key) <= (int64_t)b.K;
+}
+
+__device__ __forceinline__ uint32_t sp_slot(uint64_t key, int lg) {
+    return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - lg));
+}
+
+// insert (key, v) keeping the smaller value; returns 1 if the key was new, 0 if present, -1 if the
+// index is full (the error flag is raised by the caller)
+__device__ __forceinline__ int sp_insert_min(unsigned long long *H, int lg, uint64_t key, uint32_t v) {
+    const unsigned long long packed = key | ((unsigned long long)v << 56);
+    const uint32_t mask = (1u << lg) - 1u;
+    uint32_t i = sp_slot(key, lg);
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        unsigned long long cur = H[i];
+        if (cur == SP_EMPTY) {
+            unsigned long long prev = atomicCAS(H + i, SP_EMPTY, packed);
+            if (prev == SP_EMPTY) return 1;
+            cur = prev;
+        }
+        if ((cur & SP_KEYMASK) == key) {
+            atomicMin(H + i, packed);
+            return 0;
+        }
+        i = (i + 1) & mask;
+    }
+    return -1;
+}
+
+// value of key in the index (255 = absent)
+__device__ __forceinline__ uint32_t sp_lookup(const unsigned long long *H, int lg, uint64_t key) {
+    if (!H) return 255;
+    const uint32_t mask = (1u << lg) - 1u;
+    uint32_t i = sp_slot(key, lg);
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        const unsigned long long cur = H[i];
+        if (cur == SP_EMPTY) return 255;
+        if ((cur & SP_KEYMASK) == key) return (uint32_t)(cur >> 56);
+        i = (i + 1) & mask;
+    }
+    return 255;
+}
+
+__global__ void k_sp_fill(unsigned long long *H, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        H[i] = SP_EMPTY;
+}
+
+struct StepParams {
+    uint64_t upd, sel_mask, sel_bits;
+    int cap;                    // largest value kept
+    int keep_below;             // new states with value >= keep_below go to `changed` only (-1: none)
+    int w;                      // column weight (1 in the reference)
+    int want_changed;
+    int lg_old, lg_new;
+};
+
+// counters: [0] new keys inserted, [1] changed states, [2] error flags (1: index full, 2: changed overflow)
+__global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_constant__ BoundParams B,
+                          const unsigned long long *__restrict__ A, uint64_t n, const unsigned long long *Hold,
+                          unsigned long long *Hnew, unsigned long long *changed, uint64_t changed_cap,
+                          unsigned long long *counters) {
+    const uint64_t clr = ~P.sel_mask & SP_KEYMASK;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = A[i];
+        const uint64_t key = x & SP_KEYMASK;
+        const uint32_t v = (uint32_t)(x >> 56);
+        // the old state
+        if ((key & P.sel_mask) == P.sel_bits) {
+            const uint64_t k2 = key & clr;
+            if ((int)v <= P.cap && sp_keep(B, k2, v)) {
+                const int r = sp_insert_min(Hnew, P.lg_new, k2, v);
+                if (r > 0) atomicAdd(counters + 0, 1ull);
+                else if (r < 0) atomicOr(counters + 2, 1ull);
+            }
+        }
+        // its candidate through the column
+        if (P.upd && (int)v < P.cap) {
+            const uint64_t t = key ^ P.upd;
+            const uint32_t vc = v + (uint32_t)P.w;
+            if ((t & P.sel_mask) == P.sel_bits) {
+                const uint64_t t2 = t & clr;
+                if ((int)vc <= P.cap && sp_keep(B, t2, vc)) {
+                    const uint32_t vo = sp_lookup(Hold, P.lg_old, t);
+                    const bool hit = vo != 255u;
+                    if (vc < vo && P.want_changed) {
+                        const unsigned long long slot = atomicAdd(counters + 1, 1ull);
+                        if (slot < changed_cap) changed[slot] = t2 | ((unsigned long long)vc << 56);
+                        else atomicOr(counters + 2, 2ull);
+                    }
+                    if (hit || P.keep_below < 0 || (int)vc < P.keep_below) {
+                        const int r = sp_insert_min(Hnew, P.lg_new, t2, vc);
+                        if (r > 0) atomicAdd(counters + 0, 1ull);
+                        else if (r < 0) atomicOr(counters + 2, 1ull);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// the occupied slots of an index into an array; counters[3] = states written
+__global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t cap, unsigned long long *out,
+                             uint64_t out_cap, unsigned long long *counters) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = H[i];
+        if (x != SP_EMPTY) {
+            const unsigned long long s = atomicAdd(counters + 3, 1ull);
+            if (s < out_cap) out[s] = x;
+            else atomicOr(counters + 2, 4ull);
+        }
+    }
+}
+
+// index of an array of distinct packed states (values kept; entries with value >= below dropped
+// from the copy written to `kept` when below >= 0)
+__global__ void k_sp_build(const unsigned long long *__restrict__ A, uint64_t n, unsigned long long *H, int lg,
+                           int below, unsigned long long *kept, unsigned long long *counters) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = A[i];
+        if (below >= 0 && (int)(x >> 56) >= below) continue;
+        const int r = sp_insert_min(H, lg, x & SP_KEYMASK, (uint32_t)(x >> 56));
+        if (r < 0) atomicOr(counters + 2, 1ull);
+        if (kept) kept[atomicAdd(counters + 3, 1ull)] = x;
+    }
+}
+
+// join (cdist/sparse_dp.c:207-236): least f.value + b.value over changed forward states f and
+// backward states b with key(b) = key(f) ^ tmask; result packed (total << 56 | forward key), the
+// smallest total and, among equal totals, the smallest forward key
+__global__ void k_sp_join(const unsigned long long *__restrict__ F, uint64_t nf, const unsigned long long *Hb, int lgb,
+                          uint64_t tmask, unsigned long long *result) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nf; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = F[i];
+        const uint64_t key = x & SP_KEYMASK;
+        const uint32_t bv = sp_lookup(Hb, lgb, key ^ tmask);
+        if (bv != 255u) {
+            const unsigned long long tot = (x >> 56) + bv;
+            atomicMin(result, (tot << 56) | key);
+        }
+    }
+}
+
+__global__ void k_sp_lookup(const unsigned long long *H, int lg, const unsigned long long *keys, uint64_t n,
+                            uint8_t *vals) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        vals[i] = (uint8_t)sp_lookup(H, lg, keys[i] & SP_KEYMASK);
+}
+
+// value histogram of an array (hist[256], values 0..255)
+__global__ void k_sp_hist(const unsigned long long *__restrict__ A, uint64_t n, unsigned long long *hist) {
+    __shared__ unsigned int loc[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) loc[i] = 0;
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&loc[A[i] >> 56], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (loc[i]) atomicAdd(hist + i, (unsigned long long)loc[i]);
+}
+
+static unsigned sp_grid(uint64_t items) {
+    uint64_t g = (items + 255) / 256;
+    uint64_t cap = (uint64_t)sm_count() * 16;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+static int load_bound(BoundParams &B, int on, int K, int ncls, const uint64_t *masks, const int64_t *w, int64_t extra,
+                      uint64_t tmask) {
+    memset(&B, 0, sizeof(B));
+    B.on = on;
+    B.K = K;
+    B.extra = extra;
+    B.tmask = tmask;
+    if (!on) return TG_OK;
+    if (ncls < 0 || ncls > SP_MAXCLS) return set_error(TG_ERR_TOO_BIG, "more lookahead classes than the kernel holds");
+    B.ncls = ncls;
+    for (int c = 0; c < ncls; c++) { B.mask[c] = masks[c]; B.w[c] = w[c]; }
+    return TG_OK;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" {
+
+// Fill an index with EMPTY.
+int tg_sp_clear(void *H, uint64_t cap, void *stream) {
+    if (!H || cap == 0) return set_error(TG_ERR_ARG, "null index");
+    k_sp_fill<<<sp_grid(cap), 256, 0, (cudaStream_t)stream>>>((unsigned long long *)H, cap);
+    return cuda_check(cudaGetLastError(), "sparse clear");
+}
+
+// One column step (see the file comment).  A: old array (n states), Hold: old index (2^lg_old
+// slots, may be null when n == 0 or upd == 0), Hnew: new index (2^lg_new slots, cleared by the
+// call), Anew: new array (room for anew_cap), changed: changed states (room for changed_cap);
+// counters (device, 4 x uint64): zeroed by the call; [0] new keys, [1] changed, [2] error flags,
+// [3] states in Anew.  bound: ncls classes (masks, weights in 1/720720 units), extra, tmask, K.
+int tg_sp_step(const void *A, uint64_t n, const void *Hold, int lg_old, void *Hnew, int lg_new, void *Anew,
+               uint64_t anew_cap, void *changed, uint64_t changed_cap, uint64_t upd, uint64_t sel_mask,
+               uint64_t sel_bits, int cap, int keep_below, int w, int want_changed, int use_h, int K, int ncls,
+               const uint64_t *masks, const int64_t *weights, int64_t extra, uint64_t tmask, void *counters,
+               void *stream) {
+    if (lg_new < 1 || lg_new > 40 || (n && !A) || !Hnew || !Anew || !counters) return set_error(TG_ERR_ARG, "bad sparse step");
+    if (cap > 254 || w < 1 || w > 254) return set_error(TG_ERR_ARG, "values beyond 8 bits");
+    StepParams P;
+    P.upd = upd & SP_KEYMASK;
+    P.sel_mask = sel_mask;
+    P.sel_bits = sel_bits;
+    P.cap = cap;
+    P.keep_below = keep_below;
+    P.w = w;
+    P.want_changed = want_changed && changed;
+    P.lg_old = lg_old;
+    P.lg_new = lg_new;
+    BoundParams B;
+    int e = load_bound(B, use_h, K, ncls, masks, weights, extra, tmask);
+    if (e) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    e = cuda_check(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st), "counters");
+    if (e) return e;
+    const uint64_t capn = 1ull << lg_new;
+    k_sp_fill<<<sp_grid(capn), 256, 0, st>>>((unsigned long long *)Hnew, capn);
+    if (n) k_sp_step<<<sp_grid(n), 256, 0, st>>>(P, B, (const unsigned long long *)A, n, (const unsigned long long *)Hold,
+                                                (unsigned long long *)Hnew, (unsigned long long *)changed, changed_cap,
+                                                (unsigned long long *)counters);
+    k_sp_compact<<<sp_grid(capn), 256, 0, st>>>((const unsigned long long *)Hnew, capn, (unsigned long long *)Anew,
+                                                anew_cap, (unsigned long long *)counters);
+    return cuda_check(cudaGetLastError(), "sparse step");
+}
+
+// Index (2^lg slots, cleared by the call) of an array of distinct packed states.  below >= 0:
+// only states with value < below are indexed, and copied to `kept` (room for n) when it is given.
+int tg_sp_build(const void *A, uint64_t n, void *H, int lg, int below, void *kept, void *counters, void *stream) {
+    if (lg < 1 || lg > 40 || !H || !counters || (n && !A)) return set_error(TG_ERR_ARG, "bad index build");
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = cuda_check(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st), "counters");
+    if (e) return e;
+    const uint64_t cap = 1ull << lg;
+    k_sp_fill<<<sp_grid(cap), 256, 0, st>>>((unsigned long long *)H, cap);
+    if (n) k_sp_build<<<sp_grid(n), 256, 0, st>>>((const unsigned long long *)A, n, (unsigned long long *)H, lg, below,
+                                                 (unsigned long long *)kept, (unsigned long long *)counters);
+    return cuda_check(cudaGetLastError(), "index build");
+}
+
+// Join of nf changed states F against a backward index; result (device, 1 x uint64) is set to
+// all ones by the call and holds the packed minimum afterwards (all ones: no pair).
+int tg_sp_join(const void *F, uint64_t nf, const void *Hb, int lgb, uint64_t tmask, void *result, void *stream) {
+    if (!result || (nf && (!F || !Hb))) return set_error(TG_ERR_ARG, "bad join");
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = cuda_check(cudaMemsetAsync(result, 0xFF, sizeof(unsigned long long), st), "join init");
+    if (e) return e;
+    if (nf) k_sp_join<<<sp_grid(nf), 256, 0, st>>>((const unsigned long long *)F, nf, (const unsigned long long *)Hb, lgb,
+                                                  tmask & SP_KEYMASK, (unsigned long long *)result);
+    return cuda_check(cudaGetLastError(), "join");
+}
+
+// Values (255 = absent) of n keys in an index.
+int tg_sp_lookup(const void *H, int lg, const void *keys, uint64_t n, void *vals, void *stream) {
+    if (!H || (n && (!keys || !vals))) return set_error(TG_ERR_ARG, "bad lookup");
+    if (n) k_sp_lookup<<<sp_grid(n), 256, 0, (cudaStream_t)stream>>>((const unsigned long long *)H, lg,
+                                                                     (const unsigned long long *)keys, n, (uint8_t *)vals);
+    return cuda_check(cudaGetLastError(), "lookup");
+}
+
+// Value histogram of an array into hist (device, 256 x uint64, zeroed by the call).
+int tg_sp_hist(const void *A, uint64_t n, void *hist, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = cuda_check(cudaMemsetAsync(hist, 0, 256 * sizeof(unsigned long long), st), "hist clear");
+    if (e) return e;
+    if (n) k_sp_hist<<<sp_grid(n), 256, 0, st>>>((const unsigned long long *)A, n, (unsigned long long *)hist);
+    return cuda_check(cudaGetLastError(), "hist");
+}
+
+}  // extern "C"

@@ -1,0 +1,839 @@
+"""Weight-truncated sparse Rank DP with device hash tables (drop-in for cdist/sparse_dp.py).
+
+The host side keeps the reference's structure and API:
+  Trellis          fixed row slots by interval colouring, per-position column / selection masks,
+                   active rows and the lookahead data (cdist/sparse_dp.py:63-205)
+  Sweep            one truncated sweep with checkpoints every isqrt(N) cuts, segment recomputation
+                   and traceback (cdist/sparse_dp.py:621-819)
+  choose_split / choose_schedule   probe sweeps and the split DP (cdist/sparse_dp.py:823-981)
+  query, distance  forward / meet-in-the-middle queries, iterative deepening (cdist/sparse_dp.py:985-1151)
+The tables live on the GPU: BACKENDS["gpu"] (GpuTables) stores a table as packed states
+key | value << 56 in a device array plus an open-addressing device index, and runs a column step,
+a join and lookups as kernels of libtropigpu (csrc/sparse.cu).  Any object with the backend
+interface of cdist/sparse_dp.py:300-445 can be passed as `backend`.
+
+Differences from the reference: the dense fallback of Sweep (`dense=`) is accepted and not used
+(the device tables handle dense cuts); columns may carry integer weights (Trellis(weights=...)),
+which the reference does not have.
+"""
+from __future__ import annotations
+
+import ctypes
+import heapq
+import math
+import time
+
+import numpy as np
+
+from . import _lib, device, trellis
+
+INF = 255
+MAX_WEIGHT = INF - 1
+Q = 720720                      # lcm(1..16): lookahead weights are multiples of 1/Q (rounded down)
+U64 = np.uint64
+KEYMASK = (1 << 56) - 1
+MAX_SLOTS = 56                  # row slots of a packed device state
+
+
+def _bits(x):
+    out = []
+    while x:
+        low = x & -x
+        out.append(low.bit_length() - 1)
+        x ^= low
+    return out
+
+
+class Trellis:
+    """Minimal-span trellis of one query min{|e| : H e = 0, (L e)_obs = 1} in a column order, with
+    fixed row slots so that a state means the same in both sweep directions.  Cut c separates
+    positions [0, c) from [c, N).  weights: optional per-column integer weights (problem indices)."""
+
+    def __init__(self, h, lrow, order, nrows, name="", weights=None):
+        self.name = name
+        self.order = list(order)
+        self.N = N = len(self.order)
+        self.cw = [1] * N if weights is None else [int(weights[j]) for j in self.order]
+        hrows = trellis.minimal_span_form(trellis.rows_from_columns(h, self.order, nrows))
+        lr = trellis.reduce_target_row(lrow, hrows)
+        self.feasible = lr != 0
+        if not self.feasible:
+            return
+        rows = list(hrows) + [lr]
+        self.rows = rows
+        self.target = [0] * len(hrows) + [1]
+        self.L = len(rows) - 1
+        self.start = [trellis.lowbit(r) for r in rows]
+        self.end = [r.bit_length() - 1 for r in rows]
+        # interval colouring: rows whose closed spans overlap get distinct slots; the smallest free
+        # slot is reused (cdist/sparse_dp.py:85-99)
+        slot = [0] * len(rows)
+        free, busy, nslots = [], [], 0
+        for r in sorted(range(len(rows)), key=lambda r: self.start[r]):
+            while busy and busy[0][0] < self.start[r]:
+                heapq.heappush(free, heapq.heappop(busy)[1])
+            if free:
+                s = heapq.heappop(free)
+            else:
+                s, nslots = nslots, nslots + 1
+            slot[r] = s
+            heapq.heappush(busy, (self.end[r], s))
+        if nslots > 64:
+            raise ValueError("trellis needs %d bits per state (at most 64 supported)" % nslots)
+        self.slot, self.nslots = slot, nslots
+        col = [0] * N
+        for r, row in enumerate(rows):
+            for p in _bits(row):
+                col[p] |= 1 << slot[r]
+        self.col = col
+        fsm, fsb, bsm, bsb = [0] * N, [0] * N, [0] * N, [0] * N
+        starts_at, ends_at = [[] for _ in range(N)], [[] for _ in range(N)]
+        for r in range(len(rows)):
+            b = 1 << slot[r]
+            fsm[self.end[r]] |= b              # a forward sweep checks a row where it ends
+            bsm[self.start[r]] |= b            # a backward sweep where it starts
+            if self.target[r]:
+                fsb[self.end[r]] |= b
+                bsb[self.start[r]] |= b
+            starts_at[self.start[r]].append((slot[r], self.target[r]))
+            ends_at[self.end[r]].append((slot[r], self.target[r]))
+        self.fsel_mask, self.fsel_bits, self.bsel_mask, self.bsel_bits = fsm, fsb, bsm, bsb
+        self.starts_at, self.ends_at = starts_at, ends_at
+        enter = [[] for _ in range(N + 2)]
+        leave = [[] for _ in range(N + 2)]
+        for r in range(len(rows)):
+            enter[self.start[r] + 1].append(r)
+            leave[self.end[r] + 1].append(r)
+        act, cur = [], set()
+        for c in range(N + 1):
+            cur.update(enter[c])
+            cur.difference_update(leave[c])
+            act.append(sorted(cur))
+        self.active_rows = act
+        self.active = [sum(1 << slot[r] for r in a) for a in act]
+        self.width = [len(a) for a in act]
+        ls = 1 << slot[self.L]
+        self.tmask = [ls if self.L in a else 0 for a in act]
+        self._bd = {}
+
+    @classmethod
+    def for_query(cls, p, obs, order):
+        lrow = 0
+        for pos, j in enumerate(order):
+            if (p.l[j] >> obs) & 1:
+                lrow |= 1 << pos
+        return cls(p.h, lrow, order, p.nrows, name="%s obs %d" % (getattr(p, "name", ""), obs),
+                   weights=getattr(p, "weights", None))
+
+    # ------------------------------------------------------------------ lookahead bound
+    def _bound_data(self, forward):
+        """Per cut: (masks, weights, extra) of h(s) = ceil((extra + sum_k w_k |(s ^ tmask) & mask_k|) / Q).
+        Row r relevant at cut c gets weight y_r = 1 / max over remaining columns j containing r of
+        |supp(j) ∩ relevant rows| (a dual solution of the covering LP), rounded down to 1/Q; the
+        target row counts while it lies wholly on the remaining side (cdist/sparse_dp.py:148-192)."""
+        N, rows = self.N, self.rows
+        S = np.zeros((len(rows), N), dtype=np.int32)
+        for r, row in enumerate(rows):
+            S[r, _bits(row)] = 1
+        out = []
+        for c in range(N + 1):
+            rel = list(self.active_rows[c])
+            lone = (forward and self.start[self.L] >= c) or (not forward and self.end[self.L] < c)
+            if lone:
+                rel.append(self.L)
+            if not rel:
+                out.append(((), (), 0))
+                continue
+            if forward:
+                lo, hi = c, max(self.end[r] for r in rel) + 1
+            else:
+                lo, hi = min(self.start[r] for r in rel), c
+            sub = S[rel, lo:hi]
+            per_col = sub.sum(axis=0)
+            worst = (sub * per_col).max(axis=1)
+            assert (worst >= 1).all()
+            wts = Q // worst
+            masks, extra = {}, 0
+            for r, wr in zip(rel, wts.tolist()):
+                if lone and r == self.L:
+                    extra = wr
+                else:
+                    masks[wr] = masks.get(wr, 0) | (1 << self.slot[r])
+            ks = sorted(masks)
+            out.append((tuple(U64(masks[k]) for k in ks), tuple(np.int64(k) for k in ks), extra))
+        return out
+
+    def bound_data(self, forward):
+        if forward not in self._bd:
+            self._bd[forward] = self._bound_data(forward)
+        return self._bd[forward]
+
+    def bound_arrays(self, forward):
+        """bound_data as contiguous arrays: per cut (masks uint64, weights int64, extra)."""
+        key = ("arrays", forward)
+        if key not in self._bd:
+            self._bd[key] = [(np.array(m, dtype=U64), np.array(w, dtype=np.int64), int(e))
+                             for m, w, e in self.bound_data(forward)]
+        return self._bd[key]
+
+
+def bound(keys, tmask, hd):
+    """The lookahead lower bound for an array of states (host helper, cdist/sparse_dp.py:208-217)."""
+    masks, weights, extra = hd
+    if not len(masks):
+        return np.full(keys.shape, (extra + Q - 1) // Q, dtype=np.int64)
+    u = keys ^ U64(tmask)
+    tot = np.full(keys.shape, extra, dtype=np.int64)
+    for m, w in zip(masks, weights):
+        tot += np.int64(w) * np.bitwise_count(u & U64(m)).astype(np.int64)
+    return (tot + (Q - 1)) // Q
+
+
+# ---------------------------------------------------------------------- device tables
+class _Tab:
+    """A device table: `arr` holds its n packed states (int64 tensor), `H` its index (2^lg slots)."""
+    __slots__ = ("arr", "n", "H", "lg")
+
+    def __init__(self, arr, n, H, lg):
+        self.arr, self.n, self.H, self.lg = arr, n, H, lg
+
+
+class _Changed:
+    __slots__ = ("arr", "n")
+
+    def __init__(self, arr, n):
+        self.arr, self.n = arr, n
+
+
+def _lg_for(n_states):
+    """Index size for up to n_states states at load <= 1/2."""
+    return max(6, int(2 * max(1, n_states) - 1).bit_length() + 1)
+
+
+class GpuTables:
+    """Sparse tables on the GPU (packed states + device index).  Tables are immutable: a step returns
+    new device buffers, so every table a sweep keeps stays valid."""
+    name = "gpu"
+
+    def __init__(self, tr):
+        device.require_gpu()
+        if tr.nslots > MAX_SLOTS:
+            raise ValueError("the device tables hold at most %d row slots (this trellis needs %d)"
+                             % (MAX_SLOTS, tr.nslots))
+        self.tr = tr
+        self.L = _lib.lib()
+        import torch
+        self.torch = torch
+        self.counters = torch.zeros(4, dtype=torch.int64, device="cuda")
+        self.host = torch.zeros(4, dtype=torch.int64).pin_memory()
+        self.result = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+    # ------------------------------------------------------------------ helpers
+    def _empty(self, n):
+        return self.torch.empty(max(1, int(n)), dtype=self.torch.int64, device="cuda")
+
+    def _read_counters(self):
+        self.host.copy_(self.counters)
+        self.torch.cuda.current_stream().synchronize()
+        c = [int(x) for x in self.host.tolist()]
+        if c[2]:
+            raise RuntimeError("device table overflow (flags %d)" % c[2])
+        return c
+
+    def _build(self, arr, n, below=-1):
+        lg = _lg_for(n)
+        H = self._empty(1 << lg)
+        kept = self._empty(n) if below >= 0 else None
+        _lib.check(self.L.tg_sp_build(arr.data_ptr() if n else None, n, H.data_ptr(), lg, below,
+                                      kept.data_ptr() if kept is not None else None, self.counters.data_ptr(),
+                                      device.stream_ptr()))
+        if below >= 0:
+            m = self._read_counters()[3]
+            return _Tab(kept[:m], m, H, lg)
+        return _Tab(arr[:n], n, H, lg)
+
+    # ------------------------------------------------------------------ backend interface
+    def start(self):
+        arr = self.torch.zeros(1, dtype=self.torch.int64, device="cuda")
+        return self._build(arr, 1)
+
+    @staticmethod
+    def size(tab):
+        return tab.n
+
+    @staticmethod
+    def nbytes(tab):
+        return 8 * tab.n
+
+    @staticmethod
+    def changed_size(ch):
+        return ch.n
+
+    @staticmethod
+    def persistent(tab):
+        return tab
+
+    def arrays(self, tab):
+        """(keys uint64, vals uint8) of a table, sorted by key (host copies)."""
+        if tab.n == 0:
+            return np.zeros(0, dtype=U64), np.zeros(0, dtype=np.uint8)
+        x = tab.arr[:tab.n].cpu().numpy().view(U64)
+        keys = x & U64(KEYMASK)
+        o = np.argsort(keys, kind="stable")
+        return keys[o], (x[o] >> U64(56)).astype(np.uint8)
+
+    def from_arrays(self, keys, vals):
+        packed = (np.asarray(keys, dtype=U64) & U64(KEYMASK)) | (np.asarray(vals).astype(U64) << U64(56))
+        arr = self.torch.from_numpy(packed.view(np.int64).copy()).cuda() if packed.size else self._empty(1)
+        return self._build(arr, int(packed.size))
+
+    def lookup(self, tab, s):
+        if int(s) >> 56 or tab.n == 0:
+            return INF
+        keys = self.torch.tensor([int(s)], dtype=self.torch.int64).cuda()
+        vals = self.torch.empty(1, dtype=self.torch.uint8, device="cuda")
+        _lib.check(self.L.tg_sp_lookup(tab.H.data_ptr(), tab.lg, keys.data_ptr(), 1, vals.data_ptr(),
+                                       device.stream_ptr()))
+        return int(vals.item())
+
+    def lookup_many(self, tab, keys):
+        keys = np.asarray(keys, dtype=U64)
+        if not keys.size:
+            return np.zeros(0, dtype=np.uint8)
+        kt = self.torch.from_numpy(keys.view(np.int64).copy()).cuda()
+        vals = self.torch.empty(keys.size, dtype=self.torch.uint8, device="cuda")
+        _lib.check(self.L.tg_sp_lookup(tab.H.data_ptr(), tab.lg, kt.data_ptr(), keys.size, vals.data_ptr(),
+                                       device.stream_ptr()))
+        return vals.cpu().numpy()
+
+    def truncate(self, tab, below):
+        return self._build(tab.arr, tab.n, below=int(below))
+
+    def step(self, tab, upd, sel_mask, sel_bits, cap, K, tmask, hd, keep_below=None, want_changed=False, w=1):
+        """One column (as cdist/sparse_dp.py:338-403): T'[s] = min(T[s], T[s ^ upd] + w), then the
+        closing rows' filter and clear, values above cap and states failing the lookahead (hd)
+        dropped; returns (table, changed).  New states with value >= keep_below go to changed only."""
+        n = tab.n
+        lg = _lg_for(2 * n)
+        H = self._empty(1 << lg)
+        A = self._empty(2 * n)
+        ch = self._empty(n) if want_changed else None
+        if hd is None:
+            ncls, mp, wp, extra, use_h = 0, None, None, 0, 0
+        else:
+            m_arr, w_arr, extra = hd
+            m_arr = np.ascontiguousarray(m_arr, dtype=U64)
+            w_arr = np.ascontiguousarray(w_arr, dtype=np.int64)
+            ncls, mp, wp, use_h = len(m_arr), m_arr.ctypes.data, w_arr.ctypes.data, 1
+        _lib.check(self.L.tg_sp_step(tab.arr.data_ptr(), n, tab.H.data_ptr(), tab.lg, H.data_ptr(), lg, A.data_ptr(),
+                                     2 * n, ch.data_ptr() if ch is not None else None, n, int(upd) & KEYMASK,
+                                     int(sel_mask), int(sel_bits), int(cap),
+                                     -1 if keep_below is None else int(keep_below), int(w), int(bool(want_changed)),
+                                     use_h, int(K), ncls, mp, wp, int(extra), int(tmask), self.counters.data_ptr(),
+                                     device.stream_ptr()))
+        c = self._read_counters()
+        new = _Tab(A[:c[3]], c[3], H, lg)
+        changed = _Changed(ch[:c[1]], c[1]) if want_changed else None
+        return new, changed
+
+    def join(self, ch, btab, tmask):
+        """Least f.value + b.value over changed forward states f and backward states b with
+        key(b) = key(f) ^ tmask: (total, forward key, forward value, backward key), or None."""
+        if ch is None or not ch.n or not btab.n:
+            return None
+        _lib.check(self.L.tg_sp_join(ch.arr.data_ptr(), ch.n, btab.H.data_ptr(), btab.lg, int(tmask),
+                                     self.result.data_ptr(), device.stream_ptr()))
+        r = int(self.result.item()) & 0xFFFFFFFFFFFFFFFF
+        if r == 0xFFFFFFFFFFFFFFFF:
+            return None
+        total, fkey = r >> 56, r & KEYMASK
+        bkey = fkey ^ int(tmask)
+        bval = self.lookup(btab, bkey)
+        return total, fkey, total - bval, bkey
+
+    def hist(self, tab):
+        import torch
+        h = torch.zeros(256, dtype=torch.int64, device="cuda")
+        _lib.check(self.L.tg_sp_hist(tab.arr.data_ptr() if tab.n else None, tab.n, h.data_ptr(),
+                                     device.stream_ptr()))
+        return h.cpu().numpy()
+
+
+BACKENDS = {"gpu": GpuTables}
+
+
+class BudgetExceeded(RuntimeError):
+    """A table outgrew max_states (kind "states") or a sweep passed its deadline (kind "deadline")."""
+
+    def __init__(self, message, kind):
+        super().__init__(message)
+        self.kind = kind
+
+
+def _backend(backend, tr):
+    if isinstance(backend, str):
+        return BACKENDS[backend](tr)
+    return backend
+
+
+# ---------------------------------------------------------------------- sweeps
+class Sweep:
+    """One direction of the truncated sweep of a trellis, with tables at checkpoints
+    (cdist/sparse_dp.py:621-819).  direction +1: cuts 0 -> N from {0: 0}; -1: N -> 0.  caps: the
+    largest weight kept at each cut (non-increasing in the sweep direction).  frontier (forward
+    sweeps of the meet in the middle): the step out of cut p keeps weights <= caps[p] - 1 and returns
+    the new or improved states of weight <= caps[p] as `changed`; where caps drops, the table before
+    the drop is returned as `extra` to be joined in full."""
+
+    def __init__(self, tr, direction, K, cap=None, use_h=True, every=None, frontier=False, backend="gpu",
+                 dense=None, dense_max=1 << 30, max_states=None, deadline=None, caps=None):
+        self.tr, self.direction, self.K = tr, direction, K
+        self.caps = [min(int(x), K) for x in caps] if caps is not None else [min(cap, K)] * (tr.N + 1)
+        if max(self.caps) > MAX_WEIGHT:
+            raise ValueError("a sweep keeping weights up to %d: the tables hold at most %d (8-bit values)"
+                             % (max(self.caps), MAX_WEIGHT))
+        pairs = list(zip(self.caps, self.caps[1:]))
+        if direction > 0:
+            assert all(x >= y for x, y in pairs), "forward caps must not increase"
+        else:
+            assert all(x <= y for x, y in pairs), "backward caps must not decrease"
+        self.use_h = use_h
+        self.frontier = frontier
+        self.be = _backend(backend, tr)
+        self.hd = tr.bound_arrays(direction > 0) if use_h else None
+        self.every = every or max(1, int(math.isqrt(tr.N)))
+        self.dense = None
+        self.max_states, self.deadline = max_states, deadline
+        self.ckpt = {}
+        self.counts = [0] * (tr.N + 1)
+        self.changed_counts = [0] * (tr.N + 1)
+        self.dense_cuts = 0
+        self.peak = 0
+        self.peak_bytes = 0
+        self.steps_done = 0
+
+    def first(self):
+        return (0 if self.direction > 0 else self.tr.N), self.be.start()
+
+    def _step(self, tab, p, want_changed):
+        tr, fwd = self.tr, self.direction > 0
+        cut = p + 1 if fwd else p
+        sm, sb = (tr.fsel_mask[p], tr.fsel_bits[p]) if fwd else (tr.bsel_mask[p], tr.bsel_bits[p])
+        self.steps_done += 1
+        cap, kb = self.caps[cut], None
+        if self.frontier:
+            cap = kb = self.caps[p]
+        kw = {} if tr.cw[p] == 1 else {"w": tr.cw[p]}
+        tab, ch = self.be.step(tab, tr.col[p], sm, sb, cap, self.K, tr.tmask[cut],
+                               self.hd[cut] if self.hd else None, kb, want_changed, **kw)
+        if self.frontier and self.caps[cut] < cap:
+            return cut, self.be.truncate(tab, self.caps[cut]), ch, tab
+        return cut, tab, ch, None
+
+    def _walk(self, cut, tab, stop, want_changed=False):
+        rng = range(cut, stop) if self.direction > 0 else range(cut - 1, stop - 1, -1)
+        for p in rng:
+            c, tab, ch, extra = self._step(tab, p, want_changed)
+            yield c, tab, ch, extra
+
+    def is_ckpt(self, c):
+        return c % self.every == 0 or c == 0 or c == self.tr.N
+
+    def run(self, on_cut=None):
+        """Full sweep keeping checkpoints and per-cut counts; on_cut(cut, table, changed, extra) may
+        return True to stop.  Returns the last cut reached."""
+        c0, tab = self.first()
+        self.ckpt[c0] = tab
+        self.counts[c0] = self.changed_counts[c0] = 1
+        self.peak = 1
+        if on_cut and on_cut(c0, tab, _as_changed(self.be, tab), None):
+            return c0
+        stop = self.tr.N if self.direction > 0 else 0
+        ck_bytes = self.be.nbytes(tab)
+        for c, tab, ch, extra in self._walk(c0, tab, stop, want_changed=on_cut is not None):
+            n = self.be.size(tab)
+            self.counts[c] = n
+            nc = self.be.changed_size(ch) if ch is not None else 0
+            self.changed_counts[c] = nc
+            self.peak = max(self.peak, n, nc)
+            if self.is_ckpt(c):
+                self.ckpt[c] = self.be.persistent(tab)
+                ck_bytes += self.be.nbytes(tab)
+            self.peak_bytes = max(self.peak_bytes, ck_bytes + self.be.nbytes(tab))
+            if self.max_states is not None and max(n, nc) > self.max_states:
+                raise BudgetExceeded("%d states at cut %d" % (max(n, nc), c), "states")
+            if self.deadline is not None and time.monotonic() > self.deadline:
+                raise BudgetExceeded("deadline at cut %d" % c, "deadline")
+            if on_cut and on_cut(c, tab, ch, extra):
+                return c
+        return stop
+
+    def segment(self, lo, hi):
+        """Tables at the cuts lo..hi, recomputed from the nearest checkpoint: {cut: table}."""
+        out = {}
+        if self.direction > 0:
+            c0 = max(c for c in self.ckpt if c <= lo)
+            tab = self.ckpt[c0]
+            if c0 >= lo:
+                out[c0] = tab
+            for c, tab, _, _ in self._walk(c0, tab, hi):
+                if c >= lo:
+                    out[c] = self.be.persistent(tab)
+        else:
+            c0 = min(c for c in self.ckpt if c >= hi)
+            tab = self.ckpt[c0]
+            if c0 <= hi:
+                out[c0] = tab
+            for c, tab, _, _ in self._walk(c0, tab, lo):
+                if c <= hi:
+                    out[c] = self.be.persistent(tab)
+        return out
+
+    def table(self, c, cache):
+        """Table at cut c for cuts requested against the sweep's direction (cache reused between calls)."""
+        if c not in cache:
+            cache.clear()
+            if self.direction < 0:
+                cache.update(self.segment(c, min(x for x in self.ckpt if x >= c)))
+            else:
+                cache.update(self.segment(max(x for x in self.ckpt if x <= c), c))
+        return cache[c]
+
+    def traceback(self, cut, state, value):
+        """Columns (problem indices) of a partial solution reaching `state` with weight `value` at `cut`."""
+        tr = self.tr
+        used = []
+        s, v = int(state), int(value)
+        if self.direction > 0:
+            c = cut
+            while c > 0:
+                lo = max(0, (c - 1) // self.every * self.every)
+                tabs = self.segment(lo, c - 1)
+                for p in range(c - 1, lo - 1, -1):            # step p: cut p -> p + 1
+                    s, v = self._undo(tabs[p], s, v, s | tr.fsel_bits[p], p, used)
+                c = lo
+        else:
+            c = cut
+            while c < tr.N:
+                hi = min(tr.N, (c // self.every + 1) * self.every)
+                tabs = self.segment(c + 1, hi)
+                for p in range(c, hi):                          # backward step p: cut p + 1 -> p
+                    s, v = self._undo(tabs[p + 1], s, v, s | tr.bsel_bits[p], p, used)
+                c = hi
+        assert s == 0 and v == 0, (s, v)
+        return used
+
+    def _undo(self, tab, s, v, s_mid, p, used):
+        tr = self.tr
+        if self.be.lookup(tab, s_mid) == v:
+            return s_mid, v
+        prev, w = s_mid ^ tr.col[p], tr.cw[p]
+        assert tr.col[p] and self.be.lookup(tab, prev) == v - w, "traceback lost the path"
+        used.append(tr.order[p])
+        return prev, v - w
+
+
+def _as_changed(be, tab):
+    """The start table as a `changed` object of the backend (joined in full at the first cut)."""
+    if isinstance(be, GpuTables):
+        return _Changed(tab.arr, tab.n)
+    return tab
+
+
+# ---------------------------------------------------------------------- choice of the split
+def weight_profile(tr, direction, cap, backend="gpu"):
+    """States of each weight <= cap summed over all cuts of a sweep keeping weights <= cap."""
+    sw = Sweep(tr, direction, cap, cap, use_h=False, backend=backend)
+    c0, tab = sw.first()
+    tot = np.zeros(cap + 1)
+    tot[0] = 1
+    for c, tab, _, _ in sw._walk(c0, tab, tr.N if direction > 0 else 0):
+        tot += _hist(sw.be, tab)[:cap + 1]
+    return tot
+
+
+def _hist(be, tab):
+    if hasattr(be, "hist"):
+        return np.asarray(be.hist(tab), dtype=np.float64)
+    return np.bincount(be.arrays(tab)[1], minlength=256).astype(np.float64)
+
+
+def choose_split(tr, K, backend="gpu", probe=3, budget=2e9):
+    """Split a minimising sum_{w <= a-1} F(w) + F(a-1) + 2 sum_{w <= K-a} B(w) from measured and
+    extrapolated weight profiles (cdist/sparse_dp.py:839-867).  Returns (a, info)."""
+    t0 = time.time()
+    prof = {}
+    for direction in (+1, -1):
+        p = weight_profile(tr, direction, min(2, probe), backend)
+        if probe > 2 and len(p) > 2 and p[1] > 0 and p[2] * p[2] / p[1] < budget:
+            p = weight_profile(tr, direction, probe, backend)
+        prof[direction] = p
+
+    def extend(p, upto):
+        p = list(p)
+        r = p[-1] / p[-2] if len(p) > 1 and p[-2] > 0 else 1.0
+        while len(p) <= upto:
+            p.append(p[-1] * max(r, 1.0))
+        return p
+
+    F, B = extend(prof[+1], K), extend(prof[-1], K)
+    costs = {a: sum(F[:a]) + F[a - 1] + 2 * sum(B[:K - a + 1]) for a in range(1, K + 1)}
+    a = min(costs, key=costs.get)
+    return a, {"forward_profile": [float(x) for x in prof[+1]], "backward_profile": [float(x) for x in prof[-1]],
+               "predicted_work": {int(k): float(v) for k, v in costs.items()}, "probe_seconds": time.time() - t0}
+
+
+def cut_profiles(tr, direction, cap, backend="gpu"):
+    """States of each weight <= cap at every cut (array (N + 1, cap + 1))."""
+    sw = Sweep(tr, direction, cap, cap, use_h=False, backend=backend)
+    c0, tab = sw.first()
+    out = np.zeros((tr.N + 1, cap + 1))
+    out[c0, 0] = 1
+    for c, tab, _, _ in sw._walk(c0, tab, tr.N if direction > 0 else 0):
+        out[c] = _hist(sw.be, tab)[:cap + 1]
+    return out
+
+
+def probe_profiles(tr, backend="gpu", probe=3, budget=2e9):
+    """Per-cut state counts of each weight in both directions, up to weight `probe` (or 2 where the
+    weight-3 states, estimated from weights 1 and 2, exceed budget): ({+1: arr, -1: arr}, seconds)."""
+    t0 = time.time()
+
+    def measured(direction, cap):
+        key = ("profile", direction, cap)
+        if key not in tr._bd:
+            tr._bd[key] = cut_profiles(tr, direction, cap, backend)
+        return tr._bd[key]
+
+    prof = {}
+    for direction in (+1, -1):
+        b = budget[direction] if isinstance(budget, dict) else budget
+        p = measured(direction, min(2, probe))
+        tot = p.sum(axis=0)
+        if probe > 2 and tot[1] > 0 and tot[2] * tot[2] / tot[1] < b:
+            p = measured(direction, probe)
+        prof[direction] = p
+    return prof, time.time() - t0
+
+
+def choose_schedule(tr, K, backend="gpu", probe=3, budget=2e9, window=100):
+    """A non-increasing split a(c) per cut minimising sum_c F_c(<= a-1) + F_c(a-1) + 2 B_c(<= K-a),
+    F, B measured up to weight `probe` and extrapolated with the growth of the last two weights over
+    a window of cuts; a DP over cuts and values of a (cdist/sparse_dp.py:906-981)."""
+    prof, probe_seconds = probe_profiles(tr, backend, probe, budget)
+
+    def wsum(x):
+        cs = np.concatenate([[0.0], np.cumsum(x)])
+        idx = np.arange(x.size)
+        return cs[np.minimum(x.size, idx + window + 1)] - cs[np.maximum(0, idx - window)]
+
+    def extend(p):
+        top = p.shape[1] - 1
+        if top >= K:
+            return p[:, :K + 1]
+        hi = wsum(p[:, top])
+        lo = wsum(p[:, top - 1]) if top >= 1 else hi
+        r = np.maximum(np.where(lo > 0, hi / np.maximum(lo, 1e-300), 1.0), 1.0)
+        cols = [p[:, w] for w in range(top + 1)]
+        while len(cols) <= K:
+            cols.append(cols[-1] * r)
+        return np.stack(cols, axis=1)
+
+    F, B = extend(prof[+1]), extend(prof[-1])
+    cF, cB = np.cumsum(F, axis=1), np.cumsum(B, axis=1)
+    n = tr.N + 1
+    cost = np.zeros((n, K + 1))
+    for a in range(1, K + 1):
+        cost[:, a] = cF[:, a - 1] + F[:, a - 1] + 2 * cB[:, K - a]
+    cost[:, 0] = np.inf
+    best = np.empty((n, K + 1))
+    arg = np.zeros((n, K + 1), dtype=np.int64)
+    best[0] = cost[0]
+    for c in range(1, n):
+        prev = best[c - 1]
+        suf = np.minimum.accumulate(prev[::-1])[::-1]
+        sarg = np.empty(K + 1, dtype=np.int64)
+        m, ai = np.inf, K
+        for a in range(K, -1, -1):
+            if prev[a] < m:
+                m, ai = prev[a], a
+            sarg[a] = ai
+        best[c] = cost[c] + suf
+        arg[c] = sarg
+    a = int(np.argmin(best[n - 1]))
+    sched = [0] * n
+    for c in range(n - 1, -1, -1):
+        sched[c] = a
+        if c:
+            a = int(arg[c, a])
+    idx = np.arange(n)
+    av = np.array(sched)
+    fwd = cF[idx, av - 1] + F[idx, av - 1]
+    bwd = cB[idx, K - av]
+    every = max(1, int(math.isqrt(tr.N)))
+    ck = (idx % every == 0) | (idx == 0) | (idx == n - 1)
+    seg = np.add.reduceat(bwd, np.arange(0, n, every)).max()
+    states = bwd[ck].sum() + seg + cF[idx, av - 1][ck].sum() + 4 * max(fwd.max(), bwd.max())
+    uniform = {a: float(cost[:, a].sum()) for a in range(1, K + 1)}
+    return sched, {"predicted_work": float(best[n - 1].min()), "uniform_predicted_work": uniform,
+                   "predicted_peak_states": float(max(fwd.max(), bwd.max())),
+                   "predicted_mean_states": float((fwd.sum() + bwd.sum()) / (2 * n)),
+                   "predicted_bytes": float(8 * states), "schedule": _runs(sched),
+                   "forward_profile": prof[+1].sum(axis=0).tolist(),
+                   "backward_profile": prof[-1].sum(axis=0).tolist(), "probe_seconds": probe_seconds}
+
+
+# ---------------------------------------------------------------------- one query at one threshold
+def query(tr, K, mode="mitm", split=None, use_h=True, witness=True, lower=0, every=None, backend="gpu",
+          dense=None, dense_max=1 << 30, log=None, max_states=None, deadline=None):
+    """Least weight of a solution of the trellis' query if it is <= K (else None), with per-cut
+    statistics and a witness (cdist/sparse_dp.py:985-1095).  mode "forward": one sweep keeping
+    weights <= K.  mode "mitm": a backward sweep keeping weights <= K - a(c), then a forward sweep
+    keeping weights <= a(c) - 1 whose new or improved states are joined with the backward table at
+    every cut (and the whole table where a drops).  split: int, "auto", "schedule" or a list of
+    N + 1 non-increasing values (default K // 2 + 1)."""
+    t0 = time.time()
+    bname = backend if isinstance(backend, str) else backend.name
+    rec = {"K": K, "mode": mode, "use_h": bool(use_h), "value": None, "witness": None, "width": max(tr.width),
+           "backend": bname}
+
+    def new_be():
+        return BACKENDS[backend](tr) if isinstance(backend, str) else backend.__class__(tr)
+
+    be = new_be()
+    if mode == "forward":
+        fw = Sweep(tr, +1, K, K, use_h, every, backend=be, max_states=max_states, deadline=deadline)
+        fw.run()
+        tab = fw.ckpt[tr.N]
+        rec.update(forward_counts=fw.counts, peak_states=fw.peak, peak_table_bytes=fw.peak_bytes,
+                   sweep_seconds=time.time() - t0, steps=fw.steps_done, dense_cuts=fw.dense_cuts)
+        v = be.lookup(tab, 0)
+        if v != INF:
+            rec["value"] = v
+            if witness:
+                t1 = time.time()
+                rec["witness"] = sorted(fw.traceback(tr.N, 0, v))
+                rec["traceback_seconds"] = time.time() - t1
+        rec["seconds"] = time.time() - t0
+        return rec
+    predicted = None
+    if split == "auto":
+        split, rec["split_choice"] = choose_split(tr, K, backend=new_be() if isinstance(backend, str) else backend)
+        predicted = rec["split_choice"]["predicted_work"][split]
+    elif split == "schedule":
+        split, rec["split_choice"] = choose_schedule(tr, K, backend=new_be() if isinstance(backend, str) else backend)
+        predicted = rec["split_choice"]["predicted_work"]
+    if split is None:
+        split = K // 2 + 1
+    sched = [max(1, min(int(x), K)) for x in split] if isinstance(split, (list, tuple)) else \
+        [max(1, min(int(split), K))] * (tr.N + 1)
+    assert len(sched) == tr.N + 1 and all(x >= y for x, y in zip(sched, sched[1:])), "split must not increase"
+    bw = Sweep(tr, -1, K, use_h=use_h, every=every, backend=be, max_states=max_states, deadline=deadline,
+               caps=[K - x for x in sched])
+    fw = Sweep(tr, +1, K, use_h=use_h, every=bw.every, frontier=True, backend=new_be(), max_states=max_states,
+               deadline=deadline, caps=sched)
+    if log:
+        log("K=%d split a=%s: backward sweep (weights <= %s)%s" % (
+            K, _runs(sched), _runs([K - x for x in sched]), "" if predicted is None else
+            ", predicted work %.3g" % predicted))
+    bw.run()
+    t1 = time.time()
+    best = [None]
+    cache = {}
+    joins = [0]
+
+    def join(c, tab, ch, extra):
+        for part in (ch, extra):
+            if part is None:
+                continue
+            if not isinstance(part, _Changed) and isinstance(fw.be, GpuTables):
+                part = _Changed(part.arr, part.n)
+            if not fw.be.changed_size(part):
+                continue
+            joins[0] += fw.be.changed_size(part)
+            r = fw.be.join(part, bw.table(c, cache), tr.tmask[c])
+            if r is not None and (best[0] is None or r[0] < best[0][0]):
+                best[0] = (r[0], c) + tuple(r[1:])
+        return best[0] is not None and best[0][0] <= max(lower, 0)
+
+    fw.run(on_cut=join)
+    cache.clear()
+    rec.update(forward_counts=fw.counts, backward_counts=bw.counts, changed_counts=fw.changed_counts,
+               peak_states=max(fw.peak, bw.peak), peak_table_bytes=fw.peak_bytes + bw.peak_bytes,
+               backward_seconds=t1 - t0, forward_seconds=time.time() - t1,
+               split=sched[0] if len(set(sched)) == 1 else _runs(sched), split_values=sched, joined=joins[0],
+               steps=fw.steps_done + bw.steps_done, dense_cuts=bw.dense_cuts)
+    if best[0] is not None and best[0][0] <= K:
+        value, c, sl, fl, sr = best[0]
+        rec["value"], rec["join_cut"] = value, c
+        if witness:
+            t2 = time.time()
+            cols = fw.traceback(c, sl, fl) + bw.traceback(c, sr, value - fl)
+            rec["witness"] = sorted(cols)
+            rec["traceback_seconds"] = time.time() - t2
+    rec["seconds"] = time.time() - t0
+    return rec
+
+
+def _runs(x):
+    """A per-cut list as 'value' or 'value@cut,value@cut,...' where it changes."""
+    out = [(v, c) for c, v in enumerate(x) if c == 0 or v != x[c - 1]]
+    return str(out[0][0]) if len(out) == 1 else ",".join("%d@%d" % vc for vc in out)
+
+
+# ---------------------------------------------------------------------- distance
+def default_order(p):
+    from . import auto
+    return auto.best_order(p)[0]
+
+
+def distance(p, order=None, start=1, kmax=64, mode="mitm", use_h=True, witness=True, log=None, every=None,
+             backend="gpu", dense=None, split=None):
+    """Exact distance by iterative deepening of K from `start` (a lower bound): a dict with the
+    distance (None if none <= kmax), a checked witness and one record per (threshold, observable)
+    (cdist/sparse_dp.py:1110-1151)."""
+    t0 = time.time()
+    order = default_order(p) if order is None else order
+    trs = [Trellis.for_query(p, i, order) for i in range(p.nobs)]
+    out = {"distance": None, "witness": None, "runs": [], "lower_bound": start,
+           "order_cut_rank": max((max(t.width) for t in trs if t.feasible), default=0)}
+    for K in range(start, kmax + 1):
+        best = None
+        for i, tr in enumerate(trs):
+            if not tr.feasible:
+                continue
+            r = query(tr, K, mode=mode, use_h=use_h, witness=witness, lower=K, every=every, backend=backend,
+                      dense=dense, split=split(K) if callable(split) else split)
+            r["obs"] = i
+            out["runs"].append(summary(r))
+            if log:
+                log("  K=%d obs %d: value %s peak %d states %.2fs" % (K, i, r["value"], r["peak_states"], r["seconds"]))
+            if r["value"] is not None and (best is None or r["value"] < best["value"]):
+                best = r
+                if r["value"] <= K:
+                    break
+        if best is not None:
+            out["distance"] = best["value"]
+            if witness:
+                cols = best["witness"]
+                s = lg = 0
+                for j in cols:
+                    s ^= p.h[j]
+                    lg ^= p.l[j]
+                wt = len(cols) if getattr(p, "weights", None) is None else sum(p.weights[j] for j in cols)
+                assert s == 0 and lg != 0 and wt == best["value"] and len(cols) == len(set(cols)), \
+                    "witness check failed"
+                out["witness"] = cols
+            break
+        out["lower_bound"] = K + 1
+    out["seconds"] = time.time() - t0
+    return out
+
+
+def summary(r):
+    """A query record without the per-cut arrays (their totals instead)."""
+    out = {k: v for k, v in r.items() if not k.endswith("_counts") and k not in ("witness", "split_values")}
+    for k in ("forward_counts", "backward_counts", "changed_counts"):
+        if k in r:
+            out[k.replace("_counts", "_states_total")] = int(sum(r[k]))
+    return out
