@@ -106,6 +106,19 @@ int tg_sp_lookup(const void *H, int lg, const void *keys, uint64_t n, void *vals
 /* replaces sp_hist (cdist/sparse_dp.c:239-242): hist is a device uint64[256] */
 int tg_sp_hist(const void *A, uint64_t n, void *hist, void *stream);
 
+/* ---------------------------------------------------------------- completion tables (search)
+ * Same entry points as the reference's ctypes binding (cdist/search.py:58-67): */
+void *tg_tab_create(int log2slots, int wide, int *status);   /* cdist/gmitm.c:61 tab_create (NULL, *status -3: no memory) */
+void tg_tab_free(void *t);                                    /* cdist/gmitm.c:78 tab_free */
+int64_t tg_tab_count(void *t);                                /* cdist/gmitm.c:84 tab_count */
+int64_t tg_tab_slots_log2(void *t);
+/* cdist/gmitm.c:176 tab_build: zh, zl, lg are HOST uint64[n] */
+int tg_tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, int k);
+/* batched form of cdist/gmitm.c:138 tab_lookup (static there): DEVICE arrays zh, zl, lg (uint64[m]),
+ * R (int32[m]) -> out (int32[m]): least cost <= R[q] with the same fingerprint and another label, or -1 */
+int tg_tab_lookup_dev(void *t, uint64_t m, const void *zh, const void *zl, const void *lg, const void *R,
+                      void *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

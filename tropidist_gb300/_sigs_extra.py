@@ -11,4 +11,10 @@ SIGNATURES = {
     "tg_sp_join": (ci, [vp, u64, vp, ci, u64, vp, vp]),
     "tg_sp_lookup": (ci, [vp, ci, vp, u64, vp, vp]),
     "tg_sp_hist": (ci, [vp, u64, vp, vp]),
+    "tg_tab_create": (vp, [ci, ci, c.POINTER(ci)]),
+    "tg_tab_free": (None, [vp]),
+    "tg_tab_count": (i64, [vp]),
+    "tg_tab_slots_log2": (i64, [vp]),
+    "tg_tab_build": (ci, [vp, ci, vp, vp, vp, ci]),
+    "tg_tab_lookup_dev": (ci, [vp, u64, vp, vp, vp, vp, vp, vp]),
 }

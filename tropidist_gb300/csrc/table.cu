@@ -1,0 +1,265 @@
+// Completion tables of the weight-bounded search on the GPU (cdist/gmitm.c:36-186).
+//
+// A table maps the syndrome hash of every column subset of size <= k to its least size.  Slot
+// index = zh & (slots - 1); keys as the reference: compact tables store key = (zl & 0x7FFF...0000)
+// | (label & 0xFFFF) | 1 << 63 in one 64-bit word (cdist/gmitm.c:46-48), wide tables (more than 16
+// observables) store the 63-bit fingerprint zl | 1 << 63 and the full label in a 16-byte slot
+// claimed with one 128-bit compare-and-swap.  Costs are one byte per slot (255 = empty).
+//
+// Build: one thread per subset, the subsets of size s unranked in the combinatorial number system
+// from a binomial table, one launch per size s = 0..k in increasing order; the thread that creates a
+// key writes its cost, and since every later launch has a larger size, the first cost of a key is
+// its minimum: no atomic min on the cost byte is needed.
+// Lookup (cdist/gmitm.c:138-163): least cost <= R among the entries with the probe's fingerprint and
+// a label different from the probe's, scanning from the slot until an empty slot.
+#include "tg_common.cuh"
+#include "tg_capi.h"
+
+#include <cstring>
+#include <vector>
+
+namespace tg {
+
+#define TB_FPMASK 0x7FFFFFFFFFFF0000ull
+#define TB_MAXK 8
+
+struct TableHandle {
+    int log2slots;
+    int wide;
+    uint64_t slots;
+    unsigned long long *keys;      // compact: keys[slots]; wide: pairs (key, label) [2 * slots]
+    uint8_t *cost;                 // [slots]
+    unsigned long long *count;     // device counter of entries
+    int64_t entries;
+    int k;
+};
+
+__device__ __forceinline__ uint64_t tb_compact_key(uint64_t zl, uint64_t lg) {
+    return (zl & TB_FPMASK) | (lg & 0xFFFFull) | (1ull << 63);
+}
+
+// subset of size s with colex rank r: c_s > ... > c_1, C(c_j, j) <= remaining rank
+__device__ __forceinline__ void tb_unrank(uint64_t r, int s, int n, const unsigned long long *binom, int *cols) {
+    int hi = n;   // exclusive bound for c_s
+    for (int j = s; j >= 1; j--) {
+        // largest c in [j-1, hi) with C(c, j) <= r
+        int lo = j - 1, top = hi - 1;
+        while (lo < top) {
+            int mid = (lo + top + 1) >> 1;
+            if (binom[(uint64_t)mid * (TB_MAXK + 1) + j] <= r) lo = mid;
+            else top = mid - 1;
+        }
+        cols[j - 1] = lo;
+        r -= binom[(uint64_t)lo * (TB_MAXK + 1) + j];
+        hi = lo;
+    }
+}
+
+__global__ void k_tb_clear(unsigned long long *keys, uint64_t nwords, uint8_t *cost, uint64_t slots) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += stride) keys[i] = 0ull;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < slots; i += stride) cost[i] = 255;
+}
+
+__global__ void k_tb_build(TableHandle T, int s, uint64_t nsub, int n, const unsigned long long *binom,
+                           const unsigned long long *zh, const unsigned long long *zl, const unsigned long long *lg,
+                           unsigned long long *errflag) {
+    const uint64_t mask = T.slots - 1;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nsub; r += (uint64_t)gridDim.x * blockDim.x) {
+        int cols[TB_MAXK];
+        tb_unrank(r, s, n, binom, cols);
+        uint64_t h = 0, l = 0, g = 0;
+        for (int j = 0; j < s; j++) { h ^= zh[cols[j]]; l ^= zl[cols[j]]; g ^= lg[cols[j]]; }
+        uint64_t i = h & mask;
+        bool done = false;
+        if (!T.wide) {
+            const uint64_t key = tb_compact_key(l, g);
+            for (uint64_t probe = 0; probe <= mask && !done; probe++) {
+                unsigned long long cur = T.keys[i];
+                if (cur == 0ull) {
+                    unsigned long long prev = atomicCAS(T.keys + i, 0ull, (unsigned long long)key);
+                    if (prev == 0ull) {
+                        T.cost[i] = (uint8_t)s;
+                        atomicAdd(T.count, 1ull);
+                        done = true;
+                        break;
+                    }
+                    cur = prev;
+                }
+                if (cur == key) { done = true; break; }
+                i = (i + 1) & mask;
+            }
+        } else {
+            const uint64_t key = l | (1ull << 63);
+            for (uint64_t probe = 0; probe <= mask && !done; probe++) {
+                unsigned __int128 *slot = reinterpret_cast<unsigned __int128 *>(T.keys) + i;
+                unsigned __int128 cur = *slot;
+                const unsigned __int128 want = ((unsigned __int128)g << 64) | key;
+                if (cur == 0) {
+                    unsigned __int128 prev = atomicCAS(slot, (unsigned __int128)0, want);
+                    if (prev == 0) {
+                        T.cost[i] = (uint8_t)s;
+                        atomicAdd(T.count, 1ull);
+                        done = true;
+                        break;
+                    }
+                    cur = prev;
+                }
+                if (cur == want) { done = true; break; }
+                i = (i + 1) & mask;
+            }
+        }
+        if (!done) atomicOr(errflag, 1ull);
+    }
+}
+
+__global__ void k_tb_lookup(TableHandle T, uint64_t m, const unsigned long long *zh, const unsigned long long *zl,
+                            const unsigned long long *lg, const int *R, int *out) {
+    const uint64_t mask = T.slots - 1;
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < m; q += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = zh[q] & mask;
+        int best = -1;
+        const int rq = R[q];
+        if (!T.wide) {
+            const uint64_t fp = zl[q] & TB_FPMASK, lab = lg[q] & 0xFFFFull;
+            for (uint64_t probe = 0; probe <= mask; probe++) {
+                const unsigned long long cur = T.keys[i];
+                if (cur == 0ull) break;
+                if ((cur & TB_FPMASK) == fp && (cur & 0xFFFFull) != lab) {
+                    const int c = T.cost[i];
+                    if (c <= rq && (best < 0 || c < best)) best = c;
+                }
+                i = (i + 1) & mask;
+            }
+        } else {
+            const uint64_t key = zl[q] | (1ull << 63);
+            for (uint64_t probe = 0; probe <= mask; probe++) {
+                const unsigned long long ck = T.keys[2 * i], cl = T.keys[2 * i + 1];
+                if (ck == 0ull && cl == 0ull) break;
+                if (ck == key && cl != lg[q]) {
+                    const int c = T.cost[i];
+                    if (c <= rq && (best < 0 || c < best)) best = c;
+                }
+                i = (i + 1) & mask;
+            }
+        }
+        out[q] = best;
+    }
+}
+
+static unsigned tb_grid(uint64_t items) {
+    uint64_t g = (items + 255) / 256;
+    uint64_t cap = (uint64_t)sm_count() * 16;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" {
+
+// cdist/gmitm.c:61-76 tab_create: a table of 2^log2slots slots (wide: full labels).  NULL (and
+// *status = -3) when the device memory cannot be allocated.
+void *tg_tab_create(int log2slots, int wide, int *status) {
+    int st = TG_OK;
+    TableHandle *T = nullptr;
+    if (log2slots < 1 || log2slots > 40) st = set_error(TG_ERR_ARG, "log2slots out of range");
+    else {
+        T = new TableHandle();
+        memset(T, 0, sizeof(*T));
+        T->log2slots = log2slots;
+        T->wide = wide ? 1 : 0;
+        T->slots = 1ull << log2slots;
+        const uint64_t nwords = T->slots * (wide ? 2 : 1);
+        if (cudaMalloc(&T->keys, nwords * 8) != cudaSuccess || cudaMalloc(&T->cost, T->slots) != cudaSuccess ||
+            cudaMalloc(&T->count, 8) != cudaSuccess) {
+            cudaGetLastError();
+            if (T->keys) cudaFree(T->keys);
+            if (T->cost) cudaFree(T->cost);
+            if (T->count) cudaFree(T->count);
+            delete T;
+            T = nullptr;
+            st = set_error(TG_ERR_NOMEM, "device table allocation failed");
+        } else {
+            k_tb_clear<<<tb_grid(nwords), 256>>>(T->keys, nwords, T->cost, T->slots);
+            cudaMemset(T->count, 0, 8);
+            st = cuda_check(cudaDeviceSynchronize(), "table clear");
+        }
+    }
+    if (status) *status = st;
+    return T;
+}
+
+void tg_tab_free(void *p) {
+    TableHandle *T = static_cast<TableHandle *>(p);
+    if (!T) return;
+    cudaFree(T->keys);
+    cudaFree(T->cost);
+    cudaFree(T->count);
+    delete T;
+}
+
+int64_t tg_tab_count(void *p) { return p ? static_cast<TableHandle *>(p)->entries : -1; }
+
+int64_t tg_tab_slots_log2(void *p) { return p ? static_cast<TableHandle *>(p)->log2slots : -1; }
+
+// cdist/gmitm.c:176-186 tab_build: every subset of size 0..k of the n columns (hashes zh, zl and
+// labels lg are HOST arrays of n uint64).
+int tg_tab_build(void *p, int n, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, int k) {
+    TableHandle *T = static_cast<TableHandle *>(p);
+    if (!T || n < 0 || k < 0 || (n > 0 && (!zh || !zl || !lg))) return set_error(TG_ERR_ARG, "bad table build");
+    if (k > TB_MAXK) return set_error(TG_ERR_TOO_BIG, "table depth beyond 8");
+    k = std::min(k, n);
+    T->k = k;
+    // binomials C(c, j) for c <= n, j <= k
+    std::vector<unsigned long long> binom((uint64_t)(n + 1) * (TB_MAXK + 1), 0ull);
+    for (int c = 0; c <= n; c++) {
+        binom[(uint64_t)c * (TB_MAXK + 1)] = 1;
+        for (int j = 1; j <= TB_MAXK && j <= c; j++)
+            binom[(uint64_t)c * (TB_MAXK + 1) + j] = binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j - 1] +
+                                                     (j <= c - 1 ? binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j] : 0ull);
+    }
+    unsigned long long *d = nullptr;
+    const size_t nb = binom.size() * 8, nh = (size_t)std::max(n, 1) * 8;
+    if (cudaMalloc(&d, nb + 3 * nh + 8) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(TG_ERR_NOMEM, "device buffers for the build");
+    }
+    unsigned long long *dbin = d, *dzh = d + binom.size(), *dzl = dzh + std::max(n, 1), *dlg = dzl + std::max(n, 1);
+    unsigned long long *derr = dlg + std::max(n, 1);
+    int e = cuda_check(cudaMemcpy(dbin, binom.data(), nb, cudaMemcpyHostToDevice), "binomials");
+    if (!e && n) e = cuda_check(cudaMemcpy(dzh, zh, (size_t)n * 8, cudaMemcpyHostToDevice), "hashes");
+    if (!e && n) e = cuda_check(cudaMemcpy(dzl, zl, (size_t)n * 8, cudaMemcpyHostToDevice), "hashes");
+    if (!e && n) e = cuda_check(cudaMemcpy(dlg, lg, (size_t)n * 8, cudaMemcpyHostToDevice), "labels");
+    if (!e) e = cuda_check(cudaMemset(derr, 0, 8), "flag");
+    for (int s = 0; s <= k && !e; s++) {
+        const uint64_t nsub = binom[(uint64_t)n * (TB_MAXK + 1) + s];
+        k_tb_build<<<tb_grid(nsub), 256>>>(*T, s, nsub, n, dbin, dzh, dzl, dlg, derr);
+        e = cuda_check(cudaGetLastError(), "table build");
+    }
+    unsigned long long err = 0, cnt = 0;
+    if (!e) e = cuda_check(cudaMemcpy(&err, derr, 8, cudaMemcpyDeviceToHost), "flag read");
+    if (!e) e = cuda_check(cudaMemcpy(&cnt, T->count, 8, cudaMemcpyDeviceToHost), "count read");
+    cudaFree(d);
+    if (e) return e;
+    if (err) return set_error(TG_ERR_TOO_BIG, "completion table full");
+    T->entries = (int64_t)cnt;
+    return TG_OK;
+}
+
+// Batched probes (DEVICE arrays of m entries): out[q] = least cost <= R[q] among the entries with
+// the fingerprint of (zh[q], zl[q]) and a label other than lg[q], or -1.
+int tg_tab_lookup_dev(void *p, uint64_t m, const void *zh, const void *zl, const void *lg, const void *R, void *out,
+                      void *stream) {
+    TableHandle *T = static_cast<TableHandle *>(p);
+    if (!T || (m && (!zh || !zl || !lg || !R || !out))) return set_error(TG_ERR_ARG, "bad lookup");
+    if (m) k_tb_lookup<<<tb_grid(m), 256, 0, (cudaStream_t)stream>>>(*T, m, (const unsigned long long *)zh,
+                                                                      (const unsigned long long *)zl,
+                                                                      (const unsigned long long *)lg, (const int *)R,
+                                                                      (int *)out);
+    return cuda_check(cudaGetLastError(), "table lookup");
+}
+
+}  // extern "C"
