@@ -119,6 +119,16 @@ int tg_tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const u
 int tg_tab_lookup_dev(void *t, uint64_t m, const void *zh, const void *zl, const void *lg, const void *R,
                       void *out, void *stream);
 
+/* ---------------------------------------------------------------- batched dense Rank DP
+ * Many plans (op streams ops[offsets[i]..offsets[i+1]), uint8) in one persistent launch fed from a
+ * device work queue.  No counterpart in the reference, which runs one plan at a time
+ * (cdist/auto.py:111-122).  info: arena bytes, jobs, units, plans.  values: HOST uint32[nplans]. */
+void *tg_batch_create(int nplans, const int64_t *ops, const int64_t *offsets, int *status);
+int tg_batch_info(void *batch, int64_t *info, int ninfo);
+/* window: plans in progress at once (0: all), admitted widest first */
+int tg_batch_run(void *batch, void *arena, int blocks, int window, uint32_t *values, void *stream);
+void tg_batch_free(void *batch);
+
 #ifdef __cplusplus
 }
 #endif

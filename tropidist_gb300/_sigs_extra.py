@@ -17,4 +17,8 @@ SIGNATURES = {
     "tg_tab_slots_log2": (i64, [vp]),
     "tg_tab_build": (ci, [vp, ci, vp, vp, vp, ci]),
     "tg_tab_lookup_dev": (ci, [vp, u64, vp, vp, vp, vp, vp, vp]),
+    "tg_batch_create": (vp, [ci, vp, vp, c.POINTER(ci)]),
+    "tg_batch_info": (ci, [vp, vp, ci]),
+    "tg_batch_run": (ci, [vp, vp, ci, ci, vp, vp]),
+    "tg_batch_free": (None, [vp]),
 }

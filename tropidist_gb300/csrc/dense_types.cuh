@@ -1,0 +1,364 @@
+// Types and device bodies shared by the dense kernels (dense.cu) and the batched persistent kernel
+// (batch.cu): the shared-memory update, the narrow-table sweep, the fused-pass parameters and the
+// host-side schedule of a plan.
+#pragma once
+#include "tg_common.cuh"
+#include "fused_u8.cuh"
+
+#include <cstring>
+#include <vector>
+
+namespace tg {
+
+// ------------------------------------------------------------------ shared-memory tile helpers
+// one update over a shared-memory table of 2^bits entries (all threads of the block)
+template <typename E>
+__device__ __forceinline__ void smem_update(E *T, int bits, uint32_t m, uint32_t w) {
+    constexpr int CB = Entry<E>::CB;
+    if (bits >= CB && (bits > CB || (m >> CB) == 0)) {
+        Chunk *C = reinterpret_cast<Chunk *>(T);
+        const uint32_t mhi = m >> CB, mlo = m & ((1u << CB) - 1);
+        const uint32_t nch = 1u << (bits - CB);
+        if (mhi == 0) {
+            for (uint32_t c = threadIdx.x; c < nch; c += blockDim.x) {
+                Chunk a = C[c];
+                C[c] = chunk_minplus<E>(a, chunk_xor<E>(a, mlo), w);
+            }
+        } else {
+            const int hb = 31 - __clz(mhi);
+            // perm(b') = min(perm(b), a + w): both directions from one unpacking of a and perm(b)
+            for (uint32_t p = threadIdx.x; p < nch / 2; p += blockDim.x) {
+                uint32_t c = insert_zero(p, hb), c2 = c ^ mhi;
+                Chunk a = C[c], pb = chunk_xor<E>(C[c2], mlo);
+                chunk_minplus_pair<E>(a, pb, w);
+                C[c] = a;
+                C[c2] = chunk_xor<E>(pb, mlo);
+            }
+        }
+    } else {
+        const int hb = 31 - __clz(m);
+        const uint32_t n = 1u << bits;
+        for (uint32_t p = threadIdx.x; p < n / 2; p += blockDim.x) {
+            uint32_t s = insert_zero(p, hb), t = s ^ m;
+            E a = T[s], b = T[t];
+            T[s] = minplus1<E>(a, b, w);
+            T[t] = minplus1<E>(b, a, w);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ single-CTA sweep (narrow tables)
+// Op words: bits 30-31 code (0 expand, 1 update, 2 select); update: mask in bits 0-19, weight in
+// bits 20-27; select: pos in bits 0-5, target in bit 6.
+#define SW_MAXOPS 900
+struct SweepParams {
+    int nops;
+    int w_in;             // width of the input table (0: start from {0: 0})
+    int max_bits;         // shared-memory capacity per buffer (entries = 2^max_bits)
+    int has_in;
+    uint32_t ops[SW_MAXOPS];
+};
+
+// a whole run of ops on a table held in shared memory (smem_raw: 2 x 2^max_bits entries), all
+// threads of the block; has_in: the input table is read from `in`, else the table starts as {0: 0}
+template <typename E>
+__device__ __forceinline__ void sweep_body(const SweepParams &P, const E *__restrict__ in, E *__restrict__ out,
+                                           uint4 *smem_raw) {
+    constexpr int CB = Entry<E>::CB;
+    E *T = reinterpret_cast<E *>(smem_raw);
+    E *S = T + (1u << P.max_bits);
+    int bits = P.w_in;
+    uint32_t n = 1u << bits;
+    if (P.has_in) {
+        for (uint32_t s = threadIdx.x; s < n; s += blockDim.x) T[s] = __ldcg(in + s);
+    } else if (threadIdx.x == 0) {
+        T[0] = 0;
+    }
+    __syncthreads();
+    for (int i = 0; i < P.nops; i++) {
+        const uint32_t op = P.ops[i];
+        const uint32_t code = op >> 30;
+        if (code == 0) {
+            for (uint32_t s = threadIdx.x; s < n; s += blockDim.x) T[n + s] = (E)Entry<E>::INF;
+            bits++;
+            n <<= 1;
+        } else if (code == 1) {
+            smem_update<E>(T, bits, op & 0xFFFFFu, (op >> 20) & 0xFFu);
+        } else {
+            const int pos = op & 63;
+            const uint32_t tgt = (op >> 6) & 1u;
+            const uint32_t half = n >> 1;
+            if (pos >= CB && half >= (1u << CB)) {
+                const Chunk *C = reinterpret_cast<const Chunk *>(T);
+                Chunk *D = reinterpret_cast<Chunk *>(S);
+                const int cp = pos - CB;
+                for (uint32_t q = threadIdx.x; q < (half >> CB); q += blockDim.x)
+                    D[q] = C[insert_zero(q, cp) | (tgt << cp)];
+            } else {
+                for (uint32_t k = threadIdx.x; k < half; k += blockDim.x) S[k] = T[insert_zero(k, pos) | (tgt << pos)];
+            }
+            E *tmp = T; T = S; S = tmp;
+            bits--;
+            n >>= 1;
+        }
+        __syncthreads();
+    }
+    for (uint32_t s = threadIdx.x; s < n; s += blockDim.x) out[s] = T[s];
+}
+
+// ------------------------------------------------------------------ fused tile pass (wide tables)
+#define FP_MAXD 20
+#define FP_MAXU 48
+#define FP_MAXOUTER 64
+struct PassParams {
+    uint64_t ntiles;
+    int d, d_in, d_out, n_outer;
+    int nupd, fast_out;
+    uint32_t sel_bits;                 // target bits of the selected local bits (smem index)
+    uint64_t loc_in[FP_MAXD];          // input entry weight of local bit j (j < d_in)
+    uint64_t cmp_out[FP_MAXD];         // output entry weight of compacted local bit j (j < d_out)
+    uint32_t cmp_smem[FP_MAXD];        // smem entry weight of compacted local bit j
+    uint64_t outer_in[FP_MAXOUTER], outer_out[FP_MAXOUTER];
+    uint32_t upd_mask[FP_MAXU];
+    uint8_t upd_w[FP_MAXU];
+    uint16_t pat[16];                  // smem index of the low compacted entries (generic store)
+    // uint8 register-group form of the same updates (k_fused_pass_u8)
+    int use_groups, ngroups;
+    int store_mode;                    // output chunk from: 0 one smem chunk, 1 two chunks without local
+                                       // bit sel_low (< 4), 2 byte gathers through pat
+    int sel_low;
+    int nslow;                         // updates with in-chunk bits, applied in shared memory
+    uint8_t slow_idx[FP_MAXU];
+    GroupDesc groups[FP_MAXG];
+    uint8_t ucode[FP_MAXU];
+    uint8_t uw[FP_MAXU];
+};
+
+__device__ __forceinline__ uint64_t pdep_w64(uint32_t x, const uint64_t *wt, int nb) {
+    uint64_t r = 0;
+    for (int j = 0; j < nb; j++)
+        if ((x >> j) & 1u) r += wt[j];
+    return r;
+}
+__device__ __forceinline__ uint32_t pdep_w32(uint32_t x, const uint32_t *wt, int nb) {
+    uint32_t r = 0;
+    for (int j = 0; j < nb; j++)
+        if ((x >> j) & 1u) r += wt[j];
+    return r;
+}
+
+#define FP_THREADS 512
+#define FP_TBITS 9
+
+struct HostOp { int code; uint64_t a; int64_t b; };
+
+struct Seg {
+    int kind;               // 0 sweep in shared memory, 1 fused pass, 2 one op out of place
+    int op_code = 0;
+    uint64_t op_a = 0;
+    uint32_t op_b = 0;
+    int w_in, w_out;
+    int64_t op_end;         // ops done after this segment
+    SweepParams sp;
+    PassParams pp;
+    int ckpt = -1;          // index of a checkpoint written after this segment
+};
+
+struct DensePlan {
+    int eb;                 // entry bytes
+    int peak_bits;
+    int64_t nops;
+    std::vector<Seg> segs;
+    std::vector<int64_t> ckpt_ops;
+    int final_buf;          // buffer holding the final table (0: a, 1: b)
+    int64_t n_updates;
+    double pass_bytes;      // algorithmic bytes moved by the fused passes
+    std::vector<float> seg_ms;  // per-segment launch time of the last timed execution
+    double sweep_bytes;     // bytes read + written by the shared-memory sweeps
+};
+
+
+// One tile of a fused uint8 pass by one block of NT threads, without pipelining (the batched
+// kernel's unit of work): load the tile's input chunks (cp.async, through L2), INF over the rows
+// expanded in the pass, the register groups and the shared-memory updates, and the store of the
+// selected halves in the output order.  TC: 2^d entries of shared memory.
+template <int NT>
+static __device__ void u8_tile(const PassParams &P, uint64_t tile, const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                        uint4 *TC) {
+    constexpr int CB = 4;
+    const uint32_t tid = threadIdx.x;
+    const int nb_in = P.d_in - CB, nb_out = P.d_out - CB;
+    const uint32_t nch_in = 1u << nb_in, nch_all = 1u << (P.d - CB), nch_out = 1u << nb_out;
+    uint64_t ib = 0, ob = 0;
+    for (int k = 0; k < P.n_outer; k++)
+        if ((tile >> k) & 1ull) { ib += P.outer_in[k]; ob += P.outer_out[k]; }
+    for (uint32_t c = tid; c < nch_in; c += NT) cp_async16(TC + c, in + ib + pdep_w64(c, P.loc_in + CB, nb_in));
+    for (uint32_t c = nch_in + tid; c < nch_all; c += NT) TC[c] = make_uint4(~0u, ~0u, ~0u, ~0u);
+    cp_async_wait_all();
+    __syncthreads();
+    uint8_t *T = reinterpret_cast<uint8_t *>(TC);
+    if (P.use_groups) {
+        for (int g = 0; g < P.ngroups; g++) {
+            run_group<NT>(TC, P.d, P.groups[g], P.ucode, P.uw);
+            __syncthreads();
+        }
+        for (int u = 0; u < P.nslow; u++) {
+            const int k = P.slow_idx[u];
+            smem_update<uint8_t>(T, P.d, P.upd_mask[k], P.upd_w[k]);
+            __syncthreads();
+        }
+    } else {
+        for (int u = 0; u < P.nupd; u++) {
+            smem_update<uint8_t>(T, P.d, P.upd_mask[u], P.upd_w[u]);
+            __syncthreads();
+        }
+    }
+    const int mode = P.use_groups ? P.store_mode : (P.fast_out ? 0 : 2);
+    for (uint32_t q = tid; q < nch_out; q += NT) {
+        const uint64_t off = ob + pdep_w64(q, P.cmp_out + CB, nb_out);
+        const uint32_t sidx = pdep_w32(q, P.cmp_smem + CB, nb_out) + P.sel_bits;
+        uint4 v;
+        if (mode == 0) {
+            v = TC[sidx >> CB];
+        } else if (mode == 1) {
+            const uint32_t base = (sidx >> 5) << 1;
+            v = gather_one_select(TC[base], TC[base + 1], P.sel_low, (sidx >> P.sel_low) & 1u);
+        } else {
+            uint32_t wd[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                uint32_t word = 0;
+#pragma unroll
+                for (int e = 0; e < 4; e++) word |= (uint32_t)T[sidx + P.pat[4 * k + e]] << (8 * e);
+                wd[k] = word;
+            }
+            v = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+        }
+        *reinterpret_cast<uint4 *>(out + off) = v;
+    }
+}
+
+// The tiles [t0, t1) of a fused uint8 pass by one block of FP_THREADS threads: the tile loads go
+// through a three-buffer cp.async ring (tiles t + 1 and t + 2 load while tile t is computed), the
+// updates run in register-resident groups, the selected halves are stored in the output order.
+// Chunk c of a tile is handled by thread c % 256 in iteration c / 256: its offsets are the
+// thread's own part (computed once) plus an iteration part that is the same for every thread
+// (tables in shared memory), and the tile bases advance by a carry table (tile t+1 differs from
+// tile t in the bits up to the lowest zero bit of t).
+#define FP_MAXIT 8
+static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t t0, uint64_t t1,
+                                           const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                           uint4 *smem_raw) {
+    constexpr int CB = 4;
+    __shared__ uint64_t s_in_hi[FP_MAXIT], s_out_hi[FP_MAXIT];
+    __shared__ uint32_t s_sm_hi[FP_MAXIT];
+    __shared__ int64_t s_cin[FP_MAXOUTER], s_cout[FP_MAXOUTER];
+    const uint32_t tid = threadIdx.x;
+    const int nb_in = P.d_in - CB, nb_out = P.d_out - CB;
+    const int tb_in = min(nb_in, FP_TBITS), tb_out = min(nb_out, FP_TBITS);
+    const uint32_t nch_in = 1u << nb_in, nch_all = 1u << (P.d - CB), nch_out = 1u << nb_out;
+    const uint32_t it_in = (nch_in + FP_THREADS - 1) / FP_THREADS, it_out = (nch_out + FP_THREADS - 1) / FP_THREADS;
+    if (tid < it_in) s_in_hi[tid] = pdep_w64(tid, P.loc_in + CB + FP_TBITS, nb_in - tb_in);
+    if (tid < it_out) {
+        s_out_hi[tid] = pdep_w64(tid, P.cmp_out + CB + FP_TBITS, nb_out - tb_out);
+        s_sm_hi[tid] = pdep_w32(tid, P.cmp_smem + CB + FP_TBITS, nb_out - tb_out);
+    }
+    if (tid < (uint32_t)P.n_outer) {
+        // carry table: base(t + 1) - base(t) when bit tid is the lowest zero bit of t
+        int64_t ci = (int64_t)P.outer_in[tid], co = (int64_t)P.outer_out[tid];
+        for (uint32_t k = 0; k < tid; k++) { ci -= (int64_t)P.outer_in[k]; co -= (int64_t)P.outer_out[k]; }
+        s_cin[tid] = ci;
+        s_cout[tid] = co;
+    }
+    const uint64_t tid_in = pdep_w64(tid, P.loc_in + CB, tb_in);
+    const uint64_t tid_out = pdep_w64(tid, P.cmp_out + CB, tb_out);
+    const uint32_t tid_sm = pdep_w32(tid, P.cmp_smem + CB, tb_out) + P.sel_bits;
+    const bool in_full = nch_in >= FP_THREADS, out_full = nch_out >= FP_THREADS;
+
+    uint64_t ib0 = 0, ob0 = 0;
+    for (int k = 0; k < P.n_outer; k++)
+        if ((t0 >> k) & 1ull) { ib0 += P.outer_in[k]; ob0 += P.outer_out[k]; }
+    __syncthreads();
+
+    const uint8_t *inb = in + tid_in;
+    auto issue_load = [&](uint64_t ib, uint4 *TC) {
+        const uint8_t *src = inb + ib;
+        if (in_full) {
+            for (uint32_t it = 0; it < it_in; it++) cp_async16(TC + it * FP_THREADS + tid, src + s_in_hi[it]);
+        } else if (tid < nch_in) {
+            cp_async16(TC + tid, src);
+        }
+        for (uint32_t c = nch_in + tid; c < nch_all; c += FP_THREADS) TC[c] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        cp_async_commit();
+    };
+    auto advance = [&](uint64_t t, uint64_t &ib, uint64_t &ob) {   // bases of tile t + 1 from tile t
+        const int k = __ffsll((long long)~t) - 1;
+        ib += s_cin[k];
+        ob += s_cout[k];
+    };
+
+    // three tile buffers: tiles t + 1 and t + 2 load while tile t is computed and stored
+    uint4 *const buf0 = smem_raw, *const buf1 = smem_raw + nch_all, *const buf2 = smem_raw + 2 * nch_all;
+    int cur = 0;
+    uint64_t ob = ob0, ibn = ib0, dummy = 0;
+    uint64_t tl = t0;          // next tile to load (ibn: its input base)
+    if (tl < t1) { issue_load(ibn, buf0); tl++; }
+    if (tl < t1) { advance(tl - 1, ibn, dummy); issue_load(ibn, buf1); tl++; }
+    for (uint64_t tile = t0; tile < t1; tile++) {
+        if (tl < t1) {
+            advance(tl - 1, ibn, dummy);
+            const int slot = (cur + 2) % 3;
+            issue_load(ibn, slot == 0 ? buf0 : slot == 1 ? buf1 : buf2);
+            tl++;
+        }
+        const uint64_t ahead = tl - 1 - tile;        // loads still allowed in flight
+        if (ahead >= 2) cp_async_wait_group<2>();
+        else if (ahead == 1) cp_async_wait_group<1>();
+        else cp_async_wait_group<0>();
+        __syncthreads();
+        uint4 *TC = cur == 0 ? buf0 : cur == 1 ? buf1 : buf2;
+        const uint8_t *T = reinterpret_cast<const uint8_t *>(TC);
+        for (int g = 0; g < P.ngroups; g++) {
+            run_group<FP_THREADS>(TC, P.d, P.groups[g], P.ucode, P.uw);
+            __syncthreads();
+        }
+        for (int u = 0; u < P.nslow; u++) {
+            const int k = P.slow_idx[u];
+            smem_update<uint8_t>(reinterpret_cast<uint8_t *>(TC), P.d, P.upd_mask[k], P.upd_w[k]);
+            __syncthreads();
+        }
+        uint8_t *dstb = out + ob + tid_out;
+        for (uint32_t it = 0; it < it_out; it++) {
+            const uint32_t q = it * FP_THREADS + tid;
+            if (!out_full && q >= nch_out) break;
+            const uint32_t sidx = tid_sm + s_sm_hi[it];
+            uint4 v;
+            if (P.store_mode == 0) {
+                v = TC[sidx >> CB];
+            } else if (P.store_mode == 1) {
+                const uint32_t base = (sidx >> 5) << 1;
+                v = gather_one_select(TC[base], TC[base + 1], P.sel_low, (sidx >> P.sel_low) & 1u);
+            } else {
+                uint32_t wd[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) word |= (uint32_t)T[sidx + P.pat[4 * k + e]] << (8 * e);
+                    wd[k] = word;
+                }
+                v = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+            }
+            __stcs(reinterpret_cast<uint4 *>(dstb + s_out_hi[it]), v);
+        }
+        __syncthreads();
+        cur = cur == 2 ? 0 : cur + 1;
+        if (tile + 1 < t1) advance(tile, dummy, ob);
+    }
+}
+
+
+int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P);
+int set_dense_attrs();
+
+}  // namespace tg

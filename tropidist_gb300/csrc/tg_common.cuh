@@ -77,6 +77,10 @@ __device__ __forceinline__ Chunk ld_chunk(const void *p) {
 __device__ __forceinline__ void st_chunk(void *p, const Chunk &c) {
     *reinterpret_cast<uint4 *>(p) = make_uint4(c.w[0], c.w[1], c.w[2], c.w[3]);
 }
+__device__ __forceinline__ Chunk ld_chunk_cg(const void *p) {   // through L2 (written by other SMs)
+    uint4 v = __ldcg(reinterpret_cast<const uint4 *>(p));
+    Chunk c; c.w[0] = v.x; c.w[1] = v.y; c.w[2] = v.z; c.w[3] = v.w; return c;
+}
 __device__ __forceinline__ Chunk ldg_chunk(const void *p) {
     uint4 v = __ldcs(reinterpret_cast<const uint4 *>(p));   // streamed once: evict-first
     Chunk c; c.w[0] = v.x; c.w[1] = v.y; c.w[2] = v.z; c.w[3] = v.w; return c;

@@ -99,7 +99,7 @@ class Table:
         if m == 0:
             return np.zeros(0, dtype=np.int32)
         dev = [torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).cuda() for a in (zh, zl, lg)]
-        r = torch.from_numpy(np.ascontiguousarray(R)).cuda()
+        r = torch.from_numpy(np.array(R, dtype=np.int32)).cuda()
         out = torch.empty(m, dtype=torch.int32, device="cuda")
         _lib.check(_lib.lib().tg_tab_lookup_dev(self.handle, m, dev[0].data_ptr(), dev[1].data_ptr(),
                                                 dev[2].data_ptr(), r.data_ptr(), out.data_ptr(), device.stream_ptr()))
