@@ -55,10 +55,9 @@ class DenseBatch:
         return out
 
     def default_window(self):
-        """Plans in progress at once: as many of the widest plans' table pairs as fit in ~96 MB of
-        L2, at least 4."""
-        peak = max((pl.peak_bits for pl in self.plans if pl.feasible), default=0)
-        return max(4, int((96 << 20) // max(1, 2 << peak)))
+        """Plans in progress at once: all of them (measured best on the uneven-width batches; a
+        small window serialises the wide plans, whose passes then run on few blocks)."""
+        return 0
 
     def free(self):
         if self.handle:

@@ -252,7 +252,8 @@ void *tg_batch_create(int nplans, const int64_t *ops, const int64_t *offsets, in
                 } else if (S.kind == 1) {
                     J.kind = 1;
                     const uint64_t nt = S.pp.ntiles;
-                    J.grain = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(16, nt / (uint64_t)sm_count()));
+                    // large units amortise the per-unit overhead; concurrency comes from the other plans
+                    J.grain = (uint32_t)std::min<uint64_t>(nt, std::max<uint64_t>(16, (nt + sm_count() - 1) / sm_count()));
                     J.nunits = (uint32_t)((nt + J.grain - 1) / J.grain);
                     J.params_off = align_up(B->params.size(), 16);
                     B->params.resize(J.params_off + sizeof(PassParams));

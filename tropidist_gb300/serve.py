@@ -1,0 +1,215 @@
+"""Serving exact distances: a request loop with continuous batching on one GPU.
+
+Server             accepts distance requests (dense Rank DP problems, as their scheduled plans) at
+                   any time; a scheduler thread admits a waiting request as soon as a stream slot
+                   is free and its tables fit the device-memory budget (80 % of the free HBM by
+                   default), launches all of its passes on its own CUDA stream, and retires it when
+                   its completion event fires.  Requests admitted while others run overlap on the
+                   device (narrow plans' sweeps and small passes share the SMs); finished requests
+                   return their slot and memory at once, so the batch is continuous.
+serve_plain        the same requests one at a time on one stream (the plain GPU path).
+poisson_arrivals   seeded exponential inter-arrival times.
+Latency = completion time - arrival time; p50 / p99 and solves/s are computed by `summarize`.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+
+import numpy as np
+
+from . import device, kernel
+
+
+class Request:
+    __slots__ = ("rid", "plans", "cps", "arrival", "admitted", "done", "values", "distance", "footprint",
+                 "bufs", "event", "host", "stream")
+
+    def __init__(self, rid, plans, cps=None):
+        self.rid = rid
+        self.plans = list(plans)
+        self.cps = cps
+        self.arrival = self.admitted = self.done = None
+        self.values = None
+        self.distance = None
+        peak = max((pl.peak_bits for pl in self.plans if pl.feasible), default=0)
+        self.footprint = 2 << peak
+        self.bufs = self.event = self.host = self.stream = None
+
+
+def compile_request(rid, plans):
+    """A request whose plans are scheduled ahead of time (scheduling is host work, outside the GPU
+    timing of both serving modes)."""
+    return Request(rid, plans, [kernel.CompiledPlan(pl) if pl.feasible else None for pl in plans])
+
+
+def _launch(req, stream):
+    import torch
+    peak = max((pl.peak_bits for pl in req.plans if pl.feasible), default=0)
+    n = 1 << peak
+    with torch.cuda.stream(stream):
+        a = torch.empty(n, dtype=torch.uint8, device="cuda")
+        b = torch.empty(n, dtype=torch.uint8, device="cuda")
+        res = torch.empty(max(1, len(req.plans)), dtype=torch.uint8, device="cuda")
+    req.host = torch.empty(max(1, len(req.plans)), dtype=torch.uint8).pin_memory()
+    sp = stream.cuda_stream
+    for k, (pl, cp) in enumerate(zip(req.plans, req.cps)):
+        if cp is None:
+            continue
+        cp.execute(a, b, stream=sp)
+        src = b if cp.final_buf else a
+        with torch.cuda.stream(stream):
+            res[k:k + 1].copy_(src[:1])
+    with torch.cuda.stream(stream):
+        req.host.copy_(res, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record(stream)
+    req.bufs = (a, b, res)
+    req.event = ev
+
+
+def _finish(req):
+    vals = req.host.tolist()
+    req.values = []
+    best = None
+    for k, pl in enumerate(req.plans):
+        if not pl.feasible:
+            req.values.append(None)
+            continue
+        v = kernel.final_value(vals[k])
+        req.values.append(v)
+        best = v if best is None else min(best, v)
+    req.distance = best
+    req.bufs = None
+
+
+class Server:
+    """Continuous-batching request loop (see the module docstring)."""
+
+    def __init__(self, slots=16, budget_bytes=None, budget_frac=0.8):
+        import torch
+        device.require_gpu()
+        self.torch = torch
+        self.streams = [torch.cuda.Stream() for _ in range(slots)]
+        self.free_slots = list(range(slots))
+        self.budget = int(budget_frac * device.free_bytes()) if budget_bytes is None else int(budget_bytes)
+        self.in_use = 0
+        self.pending = collections.deque()
+        self.running = {}
+        self.finished = []
+        self.lock = threading.Lock()
+        self.wake = threading.Event()
+        self.stop_flag = False
+        self.peak_running = 0
+        self.submitted = 0
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.thread.start()
+
+    def submit(self, req, arrival=None):
+        if req.footprint > self.budget:
+            raise MemoryError("request %s needs %d bytes of tables, beyond the budget" % (req.rid, req.footprint))
+        req.arrival = time.perf_counter() if arrival is None else arrival
+        with self.lock:
+            self.pending.append(req)
+            self.submitted += 1
+        self.wake.set()
+        return req
+
+    def _loop(self):
+        while not self.stop_flag:
+            progressed = False
+            # retire finished requests (their slot and memory return at once)
+            for slot, req in list(self.running.items()):
+                if req.event.query():
+                    req.done = time.perf_counter()
+                    _finish(req)
+                    del self.running[slot]
+                    self.free_slots.append(slot)
+                    self.in_use -= req.footprint
+                    self.finished.append(req)
+                    progressed = True
+            # admit waiting requests in arrival order while slots and memory allow
+            while self.free_slots:
+                with self.lock:
+                    if not self.pending or self.in_use + self.pending[0].footprint > self.budget:
+                        break
+                    req = self.pending.popleft()
+                slot = self.free_slots.pop()
+                req.admitted = time.perf_counter()
+                req.stream = self.streams[slot]
+                _launch(req, req.stream)
+                self.running[slot] = req
+                self.in_use += req.footprint
+                self.peak_running = max(self.peak_running, len(self.running))
+                progressed = True
+            if not progressed:
+                if self.running:
+                    time.sleep(20e-6)
+                else:
+                    self.wake.wait(0.001)
+                    self.wake.clear()
+
+    def drain(self, timeout=600.0):
+        """Wait until every submitted request has finished."""
+        t0 = time.perf_counter()
+        while True:
+            with self.lock:
+                todo = self.submitted
+            if len(self.finished) >= todo:
+                return
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError("requests still running after %.0f s" % timeout)
+            time.sleep(0.0005)
+
+    def close(self):
+        self.stop_flag = True
+        self.wake.set()
+        self.thread.join(timeout=10)
+
+
+def poisson_arrivals(n, rate, seed=0):
+    """n arrival offsets (seconds) of a Poisson process of the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
+
+
+def serve_continuous(reqs, arrivals, slots=16, budget_bytes=None):
+    """Submit the requests at their arrival offsets to a Server; returns (requests, wall seconds, peak in flight)."""
+    srv = Server(slots=slots, budget_bytes=budget_bytes)
+    t0 = time.perf_counter()
+    for req, at in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        srv.submit(req, arrival=t0 + at)
+    srv.drain()
+    wall = time.perf_counter() - t0
+    peak = srv.peak_running
+    srv.close()
+    return reqs, wall, peak
+
+
+def serve_plain(reqs, arrivals):
+    """The plain path: one request at a time, in arrival order, each waited for before the next."""
+    import torch
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    for req, at in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        req.arrival = t0 + at
+        req.admitted = time.perf_counter()
+        _launch(req, stream)
+        req.event.synchronize()
+        req.done = time.perf_counter()
+        _finish(req)
+    return reqs, time.perf_counter() - t0
+
+
+def summarize(reqs, wall):
+    lat = np.array([r.done - r.arrival for r in reqs])
+    return {"requests": len(reqs), "seconds": wall, "solves_per_s": len(reqs) / wall,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3)}
