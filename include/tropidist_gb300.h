@@ -129,6 +129,18 @@ int tg_batch_info(void *batch, int64_t *info, int ninfo);
 int tg_batch_run(void *batch, void *arena, int blocks, int window, uint32_t *values, void *stream);
 void tg_batch_free(void *batch);
 
+/* ---------------------------------------------------------------- continuous serving
+ * A long-lived persistent launch that takes new plans while it runs (no counterpart in the
+ * reference, which solves one problem per process, cdist/__main__.py:64-108).  submit returns the
+ * plan's slot or a negative status (-3: no room now; collect finished plans and retry); poll
+ * returns finished (slot, final entry) pairs. */
+void *tg_server_create(void *arena, uint64_t arena_bytes, int jcap, int64_t prm_bytes, int plan_cap, int blocks,
+                       int *status);
+int tg_server_submit(void *server, const int64_t *ops, int64_t nops);
+int tg_server_poll(void *server, int *slots, uint32_t *values, int max);
+int tg_server_stop(void *server);
+void tg_server_free(void *server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,3 +51,27 @@ def test_budget_admission():
         assert all(r.distance is not None for r in fits)
     finally:
         srv.close()
+
+
+def test_persistent_server_results_match():
+    from tropidist_gb300 import auto
+    from tropidist_gb300.serve import poisson_arrivals, serve_persistent
+    ps, reqs = _requests(9, 20)
+    alone = [auto.dp_distance(p, list(range(p.ncols)))[0] for p in ps]
+    arr = poisson_arrivals(len(reqs), rate=1000.0, seed=2)
+    done, wall, peak = serve_persistent(reqs, arr, arena_bytes=1 << 30, jobs=1 << 16, param_bytes=1 << 26, plans=256)
+    assert [r.distance for r in done] == alone
+    assert peak > 1
+
+
+def test_persistent_server_reuses_slots_under_a_small_arena():
+    """An arena that holds only a few plans at once: plans wait for room, slots and job ranges are
+    reused, every result is still exact."""
+    from tropidist_gb300 import auto
+    from tropidist_gb300.serve import poisson_arrivals, serve_persistent
+    ps, reqs = _requests(4, 16)
+    alone = [auto.dp_distance(p, list(range(p.ncols)))[0] for p in ps]
+    biggest = max(r.footprint for r in reqs)
+    done, wall, peak = serve_persistent(reqs, poisson_arrivals(len(reqs), 5000.0, seed=3), arena_bytes=3 * biggest,
+                                        jobs=1 << 14, param_bytes=1 << 25, plans=8)
+    assert [r.distance for r in done] == alone

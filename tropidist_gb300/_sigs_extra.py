@@ -21,4 +21,9 @@ SIGNATURES = {
     "tg_batch_info": (ci, [vp, vp, ci]),
     "tg_batch_run": (ci, [vp, vp, ci, ci, vp, vp]),
     "tg_batch_free": (None, [vp]),
+    "tg_server_create": (vp, [vp, u64, ci, i64, ci, ci, c.POINTER(ci)]),
+    "tg_server_submit": (ci, [vp, vp, i64]),
+    "tg_server_poll": (ci, [vp, vp, vp, ci]),
+    "tg_server_stop": (ci, [vp]),
+    "tg_server_free": (None, [vp]),
 }

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 namespace tg {
@@ -106,6 +107,43 @@ __device__ void batch_single_op(const BJob &J, unsigned unit, const uint8_t *src
     }
 }
 
+// one unit of a job by the whole block: TC = three 64 KB tile buffers, PRM = parameter copy
+__device__ void run_unit(const BJob &J, unsigned unit, uint8_t *arena, const uint8_t *params, uint4 *TC, uint4 *PRM) {
+    const uint8_t *src = arena + J.src_off;
+    uint8_t *dst = arena + J.dst_off;
+    if (J.kind == 0 || J.kind == 1) {
+        const size_t psize = J.kind == 0 ? sizeof(SweepParams) : sizeof(PassParams);
+        const uint4 *g = reinterpret_cast<const uint4 *>(params + J.params_off);
+        for (uint32_t i = threadIdx.x; i < (psize + 15) / 16; i += blockDim.x) PRM[i] = __ldcg(g + i);
+        __syncthreads();
+        if (J.kind == 0) {
+            sweep_body<uint8_t>(*reinterpret_cast<const SweepParams *>(PRM), src, dst, TC);
+        } else {
+            const PassParams &P = *reinterpret_cast<const PassParams *>(PRM);
+            const uint64_t t0 = (uint64_t)unit * J.grain;
+            const uint64_t t1 = t0 + J.grain < P.ntiles ? t0 + J.grain : P.ntiles;
+            if (P.use_groups) u8_pass_range(P, t0, t1, src, dst, TC);
+            else
+                for (uint64_t t = t0; t < t1; t++) {
+                    u8_tile<BT_THREADS>(P, t, src, dst, TC);
+                    __syncthreads();
+                }
+        }
+    } else {
+        batch_single_op(J, unit, src, dst);
+    }
+}
+
+// a job descriptor read through L2 (the host may have rewritten the slot since an earlier read)
+__device__ __forceinline__ BJob load_job(const BJob *p) {
+    BJob J;
+    const uint4 *s = reinterpret_cast<const uint4 *>(p);
+    uint4 *d = reinterpret_cast<uint4 *>(&J);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(BJob) / 16); i++) d[i] = __ldcg(s + i);
+    return J;
+}
+
 #define BT_TILE_SMEM (3 * 65536)
 __global__ void __launch_bounds__(BT_THREADS, 1) k_batch(const __grid_constant__ BatchArgs A) {
     extern __shared__ uint4 smem_raw[];
@@ -126,30 +164,7 @@ __global__ void __launch_bounds__(BT_THREADS, 1) k_batch(const __grid_constant__
         __syncthreads();
         if (s_state != 0) break;
         const BJob J = A.jobs[s_job];
-        const unsigned unit = s_unit;
-        const uint8_t *src = A.arena + J.src_off;
-        uint8_t *dst = A.arena + J.dst_off;
-        if (J.kind == 0 || J.kind == 1) {
-            const size_t psize = J.kind == 0 ? sizeof(SweepParams) : sizeof(PassParams);
-            const uint4 *g = reinterpret_cast<const uint4 *>(A.params + J.params_off);
-            for (uint32_t i = threadIdx.x; i < (psize + 15) / 16; i += blockDim.x) PRM[i] = g[i];
-            __syncthreads();
-            if (J.kind == 0) {
-                sweep_body<uint8_t>(*reinterpret_cast<const SweepParams *>(PRM), src, dst, TC);
-            } else {
-                const PassParams &P = *reinterpret_cast<const PassParams *>(PRM);
-                const uint64_t t0 = (uint64_t)unit * J.grain;
-                const uint64_t t1 = t0 + J.grain < P.ntiles ? t0 + J.grain : P.ntiles;
-                if (P.use_groups) u8_pass_range(P, t0, t1, src, dst, TC);
-                else
-                    for (uint64_t t = t0; t < t1; t++) {
-                        u8_tile<BT_THREADS>(P, t, src, dst, TC);
-                        __syncthreads();
-                    }
-            }
-        } else {
-            batch_single_op(J, unit, src, dst);
-        }
+        run_unit(J, s_unit, A.arena, A.params, TC, PRM);
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -196,8 +211,201 @@ struct BatchPlan {
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 static_assert(sizeof(SweepParams) <= 4096 && sizeof(PassParams) <= 4096, "job parameters exceed their 4 KB copy");
+static_assert(sizeof(BJob) % 16 == 0, "job descriptors are read as 16-byte words");
 
 static bool g_batch_attr = false;
+
+
+// ------------------------------------------------------------------ continuous serving
+// The same units in a long-lived launch whose work arrives while it runs.  Device memory holds a
+// pool of job descriptors, parameters and counters (slots reused by the host), the job queue
+// (circular over the job pool), and a mailbox of admitted plans' first jobs that the host fills by
+// DMA on a copy stream (entry first, then the mailbox tail).  A block that looks for work first
+// moves mailbox entries into the queue, then takes a unit; a plan's last unit sets its done flag.
+// A block that finds nothing for `idle_limit` polls leaves; the host relaunches the kernel when
+// new work arrives, and all state persists across launches.
+struct ServerArgs {
+    const BJob *jobs;
+    const uint8_t *params;
+    uint8_t *arena;
+    unsigned *taken, *done, *queue, *ready;
+    unsigned *ctl;           // 0 queue head, 1 queue tail, 3 error, 4 mailbox head, 5 stop, 6 mailbox tail
+    const unsigned *mbox;
+    unsigned *plan_done;     // per plan slot: 0 running, 0x100 | final entry when done
+    unsigned jcap, mcap;
+    unsigned long long idle_limit;
+};
+
+__device__ void server_push(const ServerArgs &A, unsigned j) {
+    const unsigned slot = atomicAdd(A.ctl + 1, 1u);
+    A.queue[slot % A.jcap] = j;
+    __threadfence();
+    atomicExch(A.ready + slot % A.jcap, slot + 1u);    // the position, so a slot needs no clearing
+}
+
+// thread 0: state 0 job, 1 leave (stop flag or idle)
+__device__ void server_grab(const ServerArgs &A, int &state, unsigned &job, unsigned &unit, BJob &J) {
+    unsigned long long idle = 0;
+    while (idle < A.idle_limit) {
+        if (ld_volatile(A.ctl + 5)) break;
+        const unsigned mt = ld_volatile(A.ctl + 6), mh = ld_volatile(A.ctl + 4);
+        if (mh < mt) {
+            if (atomicCAS(A.ctl + 4, mh, mh + 1) == mh) {
+                __threadfence();
+                server_push(A, ld_volatile(A.mbox + mh % A.mcap));
+            }
+            continue;
+        }
+        const unsigned h = ld_volatile(A.ctl + 0), t = ld_volatile(A.ctl + 1);
+        if (h < t) {
+            if (ld_volatile(A.ready + h % A.jcap) != h + 1u) { __nanosleep(64); idle++; continue; }
+            __threadfence();
+            const unsigned j = ld_volatile(A.queue + h % A.jcap);
+            J = load_job(A.jobs + j);
+            const unsigned u = atomicAdd(A.taken + j, 1u);
+            if (u < J.nunits) { state = 0; job = j; unit = u; __threadfence(); return; }
+            atomicCAS(A.ctl + 0, h, h + 1);
+            continue;
+        }
+        __nanosleep(256);
+        idle++;
+    }
+    state = 1;
+}
+
+__global__ void __launch_bounds__(BT_THREADS, 1) k_server(const __grid_constant__ ServerArgs A) {
+    extern __shared__ uint4 smem_raw[];
+    uint4 *TC = smem_raw;
+    uint4 *PRM = smem_raw + (BT_TILE_SMEM / 16);
+    __shared__ int s_state;
+    __shared__ unsigned s_job, s_unit;
+    __shared__ BJob s_J;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int st = 1;
+            unsigned j = 0, u = 0;
+            BJob J;
+            server_grab(A, st, j, u, J);
+            s_state = st;
+            s_job = j;
+            s_unit = u;
+            if (st == 0) s_J = J;
+        }
+        __syncthreads();
+        if (s_state != 0) break;
+        const BJob J = s_J;
+        run_unit(J, s_unit, A.arena, A.params, TC, PRM);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned prev = atomicAdd(A.done + s_job, 1u);
+            if (prev + 1 == J.nunits) {
+                if (J.next != BJ_NONE) {
+                    server_push(A, J.next);
+                } else {
+                    // the plan's result: entry 0 of the last job's output, written (and fenced) by
+                    // the block that ran unit 0 before its completion count
+                    __threadfence();
+                    const unsigned v = *reinterpret_cast<volatile const uint8_t *>(A.arena + J.dst_off);
+                    atomicExch(A.plan_done + J.plan, 0x100u | v);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// first-fit allocator over [0, cap) in units of `align`
+struct RangeAlloc {
+    uint64_t cap = 0, align = 1;
+    std::vector<std::pair<uint64_t, uint64_t>> free;   // (offset, size), sorted by offset
+    void init(uint64_t c, uint64_t a) { cap = c; align = a; free.assign(1, {0, c}); }
+    bool take(uint64_t n, uint64_t &off) {
+        n = (n + align - 1) / align * align;
+        for (size_t i = 0; i < free.size(); i++) {
+            if (free[i].second >= n) {
+                off = free[i].first;
+                free[i].first += n;
+                free[i].second -= n;
+                if (!free[i].second) free.erase(free.begin() + i);
+                return true;
+            }
+        }
+        return false;
+    }
+    void give(uint64_t off, uint64_t n) {
+        n = (n + align - 1) / align * align;
+        auto it = std::lower_bound(free.begin(), free.end(), std::make_pair(off, (uint64_t)0));
+        it = free.insert(it, {off, n});
+        size_t i = it - free.begin();
+        if (i + 1 < free.size() && free[i].first + free[i].second == free[i + 1].first) {
+            free[i].second += free[i + 1].second;
+            free.erase(free.begin() + i + 1);
+        }
+        if (i > 0 && free[i - 1].first + free[i - 1].second == free[i].first) {
+            free[i - 1].second += free[i].second;
+            free.erase(free.begin() + i);
+        }
+    }
+};
+
+struct ServedPlan {
+    bool live = false, done = false, reported = false, tail_seen = false;
+    uint64_t arena_off = 0, arena_bytes = 0, job0 = 0, njobs = 0, prm_off = 0, prm_bytes = 0;
+    unsigned value = 0;
+    unsigned tail_at_done = 0;     // queue tail read after the plan finished
+};
+
+struct Server {
+    uint8_t *arena = nullptr;
+    void *dev = nullptr;
+    unsigned jcap = 0, mcap = 0, pcap = 0;
+    uint64_t prm_cap = 0;
+    BJob *d_jobs = nullptr;
+    uint8_t *d_params = nullptr;
+    unsigned *d_taken = nullptr, *d_done = nullptr, *d_queue = nullptr, *d_ready = nullptr, *d_ctl = nullptr;
+    unsigned *d_mbox = nullptr, *d_plan_done = nullptr;
+    cudaStream_t ks = nullptr, cs = nullptr;
+    RangeAlloc arena_a, job_a, prm_a;
+    std::vector<ServedPlan> plans;
+    std::vector<unsigned> free_slots;    // kept sorted, highest first: low slots are reused first
+    unsigned mbox_tail = 0;
+    int blocks = 0;
+    bool launched = false;
+    unsigned *h_buf = nullptr;           // pinned: plan_done flags, then the control words
+};
+
+static int server_launch(Server &S) {
+    if (S.launched && cudaStreamQuery(S.ks) == cudaErrorNotReady) return TG_OK;
+    cudaGetLastError();
+    ServerArgs A;
+    A.jobs = S.d_jobs;
+    A.params = S.d_params;
+    A.arena = S.arena;
+    A.taken = S.d_taken;
+    A.done = S.d_done;
+    A.queue = S.d_queue;
+    A.ready = S.d_ready;
+    A.ctl = S.d_ctl;
+    A.mbox = S.d_mbox;
+    A.plan_done = S.d_plan_done;
+    A.jcap = S.jcap;
+    A.mcap = S.mcap;
+    A.idle_limit = 20000ull;        // about 5-10 ms of polling without work, then the blocks leave
+    static bool attr = false;
+    if (!attr) {
+        const int e = cuda_check(cudaFuncSetAttribute(k_server, cudaFuncAttributeMaxDynamicSharedMemorySize, BT_TILE_SMEM + 4096), "attr");
+        if (e) return e;
+        attr = true;
+    }
+    k_server<<<S.blocks, BT_THREADS, BT_TILE_SMEM + 4096, S.ks>>>(A);
+    S.launched = true;
+    return cuda_check(cudaGetLastError(), "server launch");
+}
+
+static uint32_t pass_grain(uint64_t nt) {
+    return (uint32_t)std::min<uint64_t>(nt, std::max<uint64_t>(16, (nt + sm_count() - 1) / sm_count()));
+}
 
 }  // namespace tg
 
@@ -416,6 +624,263 @@ void tg_batch_free(void *p) {
     if (!B) return;
     if (B->dev) cudaFree(B->dev);
     delete B;
+}
+
+// ---------------------------------------------------------------- continuous serving
+// Pools: jobs (jcap descriptors), parameters (prm_bytes), plan slots (plan_cap).  arena: device
+// tables of the plans in progress (caller-owned, arena_bytes).
+void *tg_server_create(void *arena, uint64_t arena_bytes, int jcap, int64_t prm_bytes, int plan_cap, int blocks,
+                       int *status) {
+    int st = TG_OK;
+    Server *S = nullptr;
+    if (!arena || !arena_bytes || jcap <= 0 || prm_bytes <= 0 || plan_cap <= 0)
+        st = set_error(TG_ERR_ARG, "bad server arguments");
+    if (!st) {
+        S = new Server();
+        S->arena = static_cast<uint8_t *>(arena);
+        S->jcap = (unsigned)jcap;
+        S->mcap = S->pcap = (unsigned)plan_cap;
+        S->prm_cap = (uint64_t)prm_bytes;
+        S->blocks = blocks > 0 ? blocks : sm_count();
+        const size_t o_prm = align_up((size_t)jcap * sizeof(BJob), 256);
+        const size_t o_cnt = align_up(o_prm + (size_t)prm_bytes, 256);
+        const size_t ncnt = 4 * (size_t)jcap + 8 + 2 * (size_t)plan_cap;
+        if (cudaMalloc(&S->dev, o_cnt + ncnt * 4) != cudaSuccess) {
+            cudaGetLastError();
+            S->dev = nullptr;
+            st = set_error(TG_ERR_NOMEM, "server pools");
+        }
+        if (!st) {
+            uint8_t *d = static_cast<uint8_t *>(S->dev);
+            S->d_jobs = reinterpret_cast<BJob *>(d);
+            S->d_params = d + o_prm;
+            unsigned *c = reinterpret_cast<unsigned *>(d + o_cnt);
+            S->d_taken = c;
+            S->d_done = c + jcap;
+            S->d_queue = c + 2 * (size_t)jcap;
+            S->d_ready = c + 3 * (size_t)jcap;
+            S->d_ctl = c + 4 * (size_t)jcap;
+            S->d_mbox = S->d_ctl + 8;
+            S->d_plan_done = S->d_mbox + plan_cap;
+            st = cuda_check(cudaMemset(c, 0, ncnt * 4), "server counters");
+        }
+        if (!st) st = cuda_check(cudaStreamCreateWithFlags(&S->ks, cudaStreamNonBlocking), "server stream");
+        if (!st) st = cuda_check(cudaStreamCreateWithFlags(&S->cs, cudaStreamNonBlocking), "copy stream");
+        if (!st) st = cuda_check(cudaMallocHost(&S->h_buf, ((size_t)plan_cap + 8) * 4), "server host buffer");
+        if (!st) {
+            S->arena_a.init(arena_bytes, 256);
+            S->job_a.init((uint64_t)jcap, 1);
+            S->prm_a.init((uint64_t)prm_bytes, 16);
+            S->plans.assign(plan_cap, ServedPlan());
+            for (int k = plan_cap - 1; k >= 0; k--) S->free_slots.push_back((unsigned)k);
+        }
+        if (st) {
+            if (S->ks) cudaStreamDestroy(S->ks);
+            if (S->cs) cudaStreamDestroy(S->cs);
+            if (S->h_buf) cudaFreeHost(S->h_buf);
+            if (S->dev) cudaFree(S->dev);
+            delete S;
+            S = nullptr;
+        }
+    }
+    if (status) *status = st;
+    return S;
+}
+
+// Admits one plan (op stream of nops rows (code, a, b), uint8 tables).  Returns its slot, or
+// TG_ERR_NOMEM when the arena, the pools or the plan slots have no room now (collect finished
+// plans with tg_server_poll and retry), or another negative status.
+int tg_server_submit(void *p, const int64_t *ops, int64_t nops) {
+    if (!p || (!ops && nops)) return set_error(TG_ERR_ARG, "null argument");
+    Server &S = *static_cast<Server *>(p);
+    if (S.free_slots.empty()) return TG_ERR_NOMEM;
+    DensePlan P;
+    int st = build_dense_plan(ops, nops, 1, nullptr, 0, P);
+    if (st) return st;
+    for (const Seg &G : P.segs)
+        if ((G.kind == 0 && G.sp.max_bits > 15) || (G.kind == 1 && G.pp.d > 16))
+            return set_error(TG_ERR_TOO_BIG, "served plans need sweeps of <= 15 bits and tiles of <= 16 bits");
+    const unsigned slot = S.free_slots.back();
+    ServedPlan &R = S.plans[slot];
+    R = ServedPlan();
+    if (P.segs.empty()) {              // nothing to run: the start table {0: 0} is the result
+        S.free_slots.pop_back();
+        R.live = R.done = true;
+        R.tail_seen = true;
+        R.value = 0;
+        return (int)slot;
+    }
+    // parameter blob and jobs
+    std::vector<uint8_t> prm;
+    std::vector<BJob> jobs(P.segs.size());
+    const uint64_t tb = align_up((size_t)1 << P.peak_bits, 256);
+    R.arena_bytes = 2 * tb;
+    if (!S.arena_a.take(R.arena_bytes, R.arena_off)) return TG_ERR_NOMEM;
+    for (const Seg &G : P.segs) {
+        const size_t n = G.kind == 0 ? sizeof(SweepParams) : G.kind == 1 ? sizeof(PassParams) : 0;
+        if (n) prm.resize(align_up(prm.size(), 16) + n);
+    }
+    R.prm_bytes = std::max<size_t>(16, prm.size());
+    R.njobs = jobs.size();
+    if (!S.job_a.take(R.njobs, R.job0)) {
+        S.arena_a.give(R.arena_off, R.arena_bytes);
+        return TG_ERR_NOMEM;
+    }
+    if (!S.prm_a.take(R.prm_bytes, R.prm_off)) {
+        S.arena_a.give(R.arena_off, R.arena_bytes);
+        S.job_a.give(R.job0, R.njobs);
+        return TG_ERR_NOMEM;
+    }
+    S.free_slots.pop_back();
+    R.live = true;
+    const uint64_t a = R.arena_off, b = a + tb;
+    size_t poff = 0;
+    int cur = 0;
+    for (size_t k = 0; k < P.segs.size(); k++) {
+        const Seg &G = P.segs[k];
+        BJob &J = jobs[k];
+        memset(&J, 0, sizeof(J));
+        J.plan = (int)slot;
+        J.next = k + 1 < P.segs.size() ? (unsigned)(R.job0 + k + 1) : BJ_NONE;
+        J.src_off = cur ? b : a;
+        J.dst_off = cur ? a : b;
+        if (G.kind == 0) {
+            J.kind = 0;
+            J.nunits = 1;
+            poff = align_up(poff, 16);
+            memcpy(prm.data() + poff, &G.sp, sizeof(SweepParams));
+            J.params_off = R.prm_off + poff;
+            poff += sizeof(SweepParams);
+        } else if (G.kind == 1) {
+            J.kind = 1;
+            J.grain = pass_grain(G.pp.ntiles);
+            J.nunits = (uint32_t)((G.pp.ntiles + J.grain - 1) / J.grain);
+            poff = align_up(poff, 16);
+            memcpy(prm.data() + poff, &G.pp, sizeof(PassParams));
+            J.params_off = R.prm_off + poff;
+            poff += sizeof(PassParams);
+        } else {
+            J.kind = 2;
+            J.bits = G.w_in;
+            J.op_code = G.op_code;
+            J.op_a = G.op_a;
+            J.op_b = G.op_b;
+            const uint64_t chunks = std::max<uint64_t>(1, ((uint64_t)1 << G.w_in) >> 4);
+            J.nunits = (uint32_t)((chunks + BJ_UNIT_CHUNKS - 1) / BJ_UNIT_CHUNKS);
+        }
+        cur ^= 1;
+    }
+    if ((P.final_buf ? b : a) != jobs.back().dst_off) return set_error(TG_ERR_STATE, "plan result buffer mismatch");
+    // descriptors, counters, start table, then the mailbox entry and tail (stream order on the copy
+    // stream makes everything before the tail visible before the kernel can see the entry)
+    unsigned *hb = S.h_buf;
+    const unsigned first = (unsigned)R.job0;
+    cudaStream_t cs = S.cs;
+    st = cuda_check(cudaMemcpyAsync(S.d_jobs + R.job0, jobs.data(), jobs.size() * sizeof(BJob), cudaMemcpyHostToDevice, cs), "server jobs");
+    if (!st && !prm.empty())
+        st = cuda_check(cudaMemcpyAsync(S.d_params + R.prm_off, prm.data(), prm.size(), cudaMemcpyHostToDevice, cs), "server params");
+    if (!st) st = cuda_check(cudaMemsetAsync(S.d_taken + R.job0, 0, R.njobs * 4, cs), "taken");
+    if (!st) st = cuda_check(cudaMemsetAsync(S.d_done + R.job0, 0, R.njobs * 4, cs), "done");
+    if (!st) st = cuda_check(cudaMemsetAsync(S.d_plan_done + slot, 0, 4, cs), "plan flag");
+    if (!st) st = cuda_check(cudaMemsetAsync(S.arena + a, 0, 1, cs), "start table");
+    if (!st) {
+        hb[0] = first;
+        hb[1] = S.mbox_tail + 1;
+        st = cuda_check(cudaMemcpyAsync(S.d_mbox + S.mbox_tail % S.mcap, hb, 4, cudaMemcpyHostToDevice, cs), "mailbox");
+    }
+    if (!st) st = cuda_check(cudaMemcpyAsync(S.d_ctl + 6, hb + 1, 4, cudaMemcpyHostToDevice, cs), "mailbox tail");
+    if (!st) st = cuda_check(cudaStreamSynchronize(cs), "submit sync");
+    if (st) return st;
+    S.mbox_tail++;
+    st = server_launch(S);
+    return st ? st : (int)slot;
+}
+
+// Finished plans since the last call: up to `max` (slot, final entry) pairs into slots/values
+// (host arrays).  Returns how many, or a negative status.  Frees a finished plan's tables at once
+// and its descriptors once the queue head has passed every position the plan used.
+int tg_server_poll(void *p, int *slots, uint32_t *values, int max) {
+    if (!p || (max > 0 && (!slots || !values))) return set_error(TG_ERR_ARG, "null argument");
+    Server &S = *static_cast<Server *>(p);
+    unsigned hi = 0;
+    bool running = false;
+    for (unsigned k = 0; k < S.pcap; k++)
+        if (S.plans[k].live) {
+            hi = k + 1;
+            running |= !S.plans[k].done;
+        }
+    unsigned *flags = S.h_buf, *ctl = S.h_buf + S.pcap;
+    int st = TG_OK;
+    if (hi) st = cuda_check(cudaMemcpyAsync(flags, S.d_plan_done, (size_t)hi * 4, cudaMemcpyDeviceToHost, S.cs), "plan flags");
+    // after the flags: a tail read here is at or past the last push of every plan seen finished
+    if (!st) st = cuda_check(cudaMemcpyAsync(ctl, S.d_ctl, 8 * 4, cudaMemcpyDeviceToHost, S.cs), "control words");
+    if (!st) st = cuda_check(cudaStreamSynchronize(S.cs), "poll sync");
+    if (st) return st;
+    if (ctl[3]) return set_error(TG_ERR_TIMEOUT, "a server block waited beyond its bound");
+    const cudaError_t q = cudaStreamQuery(S.ks);
+    if (q != cudaSuccess && q != cudaErrorNotReady) return cuda_check(q, "server kernel");
+    int n = 0;
+    for (unsigned k = 0; k < hi; k++) {
+        ServedPlan &R = S.plans[k];
+        if (!R.live) continue;
+        if (!R.done && (flags[k] & 0x100u)) {
+            R.done = true;
+            R.value = flags[k] & 0xFFu;
+            R.tail_at_done = ctl[1];
+            S.arena_a.give(R.arena_off, R.arena_bytes);
+        } else if (R.done && !R.tail_seen && R.njobs && (int)(ctl[0] - R.tail_at_done) >= 0) {
+            // a later poll: no block can still be reading these descriptors
+            R.tail_seen = true;
+            S.job_a.give(R.job0, R.njobs);
+            S.prm_a.give(R.prm_off, R.prm_bytes);
+        }
+        if (R.done && !R.reported && n < max) {
+            slots[n] = (int)k;
+            values[n] = R.value;
+            n++;
+            R.reported = true;
+        }
+        if (R.done && R.reported && R.tail_seen) {
+            R.live = false;
+            S.free_slots.insert(std::upper_bound(S.free_slots.begin(), S.free_slots.end(), k, std::greater<unsigned>()), k);
+        }
+    }
+    if (running) {
+        bool undone = false;
+        for (unsigned k = 0; k < hi; k++) undone |= S.plans[k].live && !S.plans[k].done;
+        if (undone) {
+            st = server_launch(S);      // blocks that idled out leave; new work brings them back
+            if (st) return st;
+        }
+    }
+    return n;
+}
+
+// Makes the kernel's blocks leave and waits for them.
+int tg_server_stop(void *p) {
+    if (!p) return set_error(TG_ERR_ARG, "null server");
+    Server &S = *static_cast<Server *>(p);
+    S.h_buf[S.pcap] = 1;
+    int st = cuda_check(cudaMemcpyAsync(S.d_ctl + 5, S.h_buf + S.pcap, 4, cudaMemcpyHostToDevice, S.cs), "stop flag");
+    if (!st) st = cuda_check(cudaStreamSynchronize(S.cs), "stop sync");
+    if (!st) st = cuda_check(cudaStreamSynchronize(S.ks), "server drain");
+    if (!st) {
+        S.h_buf[S.pcap] = 0;
+        st = cuda_check(cudaMemcpyAsync(S.d_ctl + 5, S.h_buf + S.pcap, 4, cudaMemcpyHostToDevice, S.cs), "stop flag");
+        if (!st) st = cuda_check(cudaStreamSynchronize(S.cs), "stop sync");
+    }
+    return st;
+}
+
+void tg_server_free(void *p) {
+    Server *S = static_cast<Server *>(p);
+    if (!S) return;
+    tg_server_stop(S);
+    cudaStreamDestroy(S->ks);
+    cudaStreamDestroy(S->cs);
+    cudaFreeHost(S->h_buf);
+    cudaFree(S->dev);
+    delete S;
 }
 
 }  // extern "C"

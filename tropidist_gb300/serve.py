@@ -7,6 +7,10 @@ Server             accepts distance requests (dense Rank DP problems, as their s
                    its completion event fires.  Requests admitted while others run overlap on the
                    device (narrow plans' sweeps and small passes share the SMs); finished requests
                    return their slot and memory at once, so the batch is continuous.
+PersistentServer   the same interface on one long-lived persistent kernel (csrc/batch.cu k_server):
+                   admitted plans are handed to the running kernel through a device mailbox and
+                   their passes are interleaved with the plans already in flight at tile-range
+                   granularity, with no kernel launches per pass.
 serve_plain        the same requests one at a time on one stream (the plain GPU path).
 poisson_arrivals   seeded exponential inter-arrival times.
 Latency = completion time - arrival time; p50 / p99 and solves/s are computed by `summarize`.
@@ -213,3 +217,146 @@ def summarize(reqs, wall):
     return {"requests": len(reqs), "seconds": wall, "solves_per_s": len(reqs) / wall,
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_ms": float(lat.mean() * 1e3)}
+
+
+class PersistentServer:
+    """Continuous batching inside one persistent kernel.  A request's plans are submitted as soon as
+    the arena (device tables) and the descriptor pools have room; finished plans are collected by
+    polling, and a request completes when all of its plans have."""
+
+    def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192):
+        import ctypes
+        import torch
+        from . import _lib
+        device.require_gpu()
+        self.torch, self.ctypes, self.L = torch, ctypes, _lib.lib()
+        if arena_bytes is None:
+            arena_bytes = int(budget_frac * device.free_bytes()) - param_bytes - 64 * jobs
+        self.arena = device.empty(arena_bytes)
+        st = ctypes.c_int(0)
+        self.handle = self.L.tg_server_create(self.arena.data_ptr(), arena_bytes, jobs, param_bytes, plans, 0,
+                                              ctypes.byref(st))
+        if not self.handle:
+            _lib.check(st.value)
+        self.plan_cap = plans
+        self.pending = collections.deque()
+        self.owner = {}                # slot -> (request, plan index)
+        self.left = {}                 # request id -> plans still running
+        self.finished = []
+        self.submitted = 0
+        self.peak_running = 0
+        self.lock = threading.Lock()
+        self.stop_flag = False
+        self.slots = np.zeros(plans, dtype=np.int32)
+        self.vals = np.zeros(plans, dtype=np.uint32)
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.thread.start()
+
+    def submit(self, req, arrival=None):
+        req.arrival = time.perf_counter() if arrival is None else arrival
+        with self.lock:
+            self.pending.append(req)
+            self.submitted += 1
+        return req
+
+    def _admit(self, req):
+        """Submit every feasible plan of the request; False (nothing submitted) if there is no room."""
+        from . import _lib
+        encs = [(k, pl.encode()) for k, pl in enumerate(req.plans) if pl.feasible]
+        slots = []
+        for k, enc in encs:
+            enc = np.ascontiguousarray(enc)
+            r = self.L.tg_server_submit(self.handle, enc.ctypes.data, len(enc))
+            if r == -3 and not slots and not self.owner:
+                _lib.check(r)               # does not fit even in an empty server
+            if r == -3:
+                return slots, False
+            if r < 0:
+                _lib.check(r)
+            slots.append((r, k))
+        return slots, True
+
+    def _loop(self):
+        partial = None
+        while not self.stop_flag:
+            progressed = False
+            n = self.L.tg_server_poll(self.handle, self.slots.ctypes.data, self.vals.ctypes.data, self.plan_cap)
+            if n < 0:
+                from . import _lib
+                _lib.check(n)
+            for i in range(n):
+                req, k = self.owner.pop(int(self.slots[i]))
+                req.values[k] = kernel.final_value(int(self.vals[i]))
+                self.left[req.rid] -= 1
+                if self.left[req.rid] == 0:
+                    req.done = time.perf_counter()
+                    feas = [v for v in req.values if v is not None]
+                    req.distance = min(feas) if feas else None
+                    self.finished.append(req)
+                progressed = True
+            # admit waiting requests (a request whose plans did not all fit keeps its place)
+            while True:
+                if partial is None:
+                    with self.lock:
+                        if not self.pending:
+                            break
+                        req = self.pending.popleft()
+                    req.admitted = time.perf_counter()
+                    req.values = [None] * len(req.plans)
+                    feasible = [k for k, pl in enumerate(req.plans) if pl.feasible]
+                    self.left[req.rid] = len(feasible)
+                    partial = (req, feasible)
+                    if not feasible:
+                        req.done = time.perf_counter()
+                        self.finished.append(req)
+                        partial = None
+                        continue
+                req, todo = partial
+                sub = _Sub(req, todo)
+                got, ok = self._admit(sub)
+                for slot, kk in got:
+                    self.owner[slot] = (req, todo[kk])
+                partial = None if ok else (req, todo[len(got):])
+                progressed = progressed or bool(got)
+                self.peak_running = max(self.peak_running, len(self.owner))
+                if not ok:
+                    break
+            if not progressed:
+                time.sleep(50e-6)
+
+    def drain(self, timeout=600.0):
+        t0 = time.perf_counter()
+        while len(self.finished) < self.submitted:
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError("requests still running after %.0f s" % timeout)
+            time.sleep(0.0005)
+
+    def close(self):
+        self.stop_flag = True
+        self.thread.join(timeout=10)
+        if self.handle:
+            self.L.tg_server_free(self.handle)
+            self.handle = None
+
+
+class _Sub:
+    """The not yet submitted plans of a request."""
+
+    def __init__(self, req, todo):
+        self.plans = [req.plans[k] for k in todo]
+
+
+def serve_persistent(reqs, arrivals, **kw):
+    """Submit the requests at their arrival offsets to a PersistentServer; (requests, seconds, peak plans)."""
+    srv = PersistentServer(**kw)
+    t0 = time.perf_counter()
+    for req, at in zip(reqs, arrivals):
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        srv.submit(req, arrival=t0 + at)
+    srv.drain()
+    wall = time.perf_counter() - t0
+    peak = srv.peak_running
+    srv.close()
+    return reqs, wall, peak
