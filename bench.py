@@ -196,15 +196,18 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch():
-    """DRAM bytes per fused-pass launch from the committed ncu summary, scaled to the bench's
-    table size (traffic grows with the table), or None."""
-    path = os.path.join(ROOT, "profiles", "fused_pass_traffic.json")
-    try:
-        with open(path) as f:
-            return json.load(f)
-    except (OSError, ValueError):
-        return None
+def traffic_per_launch(kernel):
+    """DRAM bytes / algorithmic bytes of `kernel` from the committed ncu summaries
+    (profiles/<kernel>_traffic.json, or the older fused_pass_traffic.json), or None."""
+    for name in ("%s_traffic.json" % kernel, "fused_pass_traffic.json"):
+        try:
+            with open(os.path.join(ROOT, "profiles", name)) as f:
+                tr = json.load(f)
+        except (OSError, ValueError):
+            continue
+        if tr.get("kernel") == kernel:
+            return tr
+    return None
 
 
 # ---------------------------------------------------------------------- GPU arm
@@ -238,9 +241,9 @@ def main():
             if timed is None:
                 cp.execute(a, b)
             else:
-                out = (ctypes.c_double * 9)()
-                _lib.check(L.tg_dense_execute_timed(cp.handle, a.data_ptr(), b.data_ptr(), st.cuda_stream, out, 9))
-                for k in range(9):
+                out = (ctypes.c_double * 12)()
+                _lib.check(L.tg_dense_execute_timed(cp.handle, a.data_ptr(), b.data_ptr(), st.cuda_stream, out, 12))
+                for k in range(12):
                     timed[k] += out[k]
             vals.append(cp)
         return vals
@@ -256,7 +259,7 @@ def main():
         os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else str(local)
     clocks = Clocks(gpu_index)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    acc = [0.0] * 9
+    acc = [0.0] * 12
     e0.record(st)
     for _ in range(args.steps):
         step(acc)
@@ -297,10 +300,14 @@ def main():
         e2e_value = None
 
     peak_gbs, peak_kind = measured_peak()
-    n_fp, ms_fp, bytes_fp = acc[3], acc[4], acc[5]
+    # the dominant kernel by GPU time: coset-streaming passes or fused tile passes
+    kinds = {"k_fused_pass_u8": 1, "k_stream_pass_u8": 3}
+    kname = max(kinds, key=lambda k: acc[3 * kinds[k] + 1])
+    ki = kinds[kname]
+    n_fp, ms_fp, bytes_fp = acc[3 * ki], acc[3 * ki + 1], acc[3 * ki + 2]
     achieved = (bytes_fp / n_fp) / (ms_fp / n_fp / 1e3) / 1e9 if n_fp else None
-    tr = traffic_per_launch()
-    roofline = {"bound": "hbm", "kernel": "k_fused_pass<uint8>", "achieved": achieved, "peak": peak_gbs,
+    tr = traffic_per_launch(kname)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak_gbs,
                 "unit": "GB/s", "frac": achieved / peak_gbs if achieved else None,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_launch": bytes_fp / n_fp if n_fp else None,
@@ -313,7 +320,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded banded problem)",
             "config": config(args, plans, {"parallelism": "replicas (one instance per rank)" if world > 1 else "1 GPU",
-                                           "distances": dists, "fused_passes_per_step": int(n_fp / args.steps),
+                                           "distances": dists,
+                                           "fused_passes_per_step": int((acc[3] + acc[9]) / args.steps),
+                                           "streaming_passes_per_step": int(acc[9] / args.steps),
                                            "segments_per_step": sum(cp.nsegs for cp in cps)}),
             "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -51,14 +51,15 @@ void *tg_dense_plan(const int64_t *ops, int64_t nops, int entry_bytes, const int
 int tg_dense_plan_info(void *plan, int64_t *info, int ninfo);
 /* info: peak_bits, segments, fused passes, shared-memory sweeps, final buffer (0 a / 1 b),
  *       update ops, pass bytes, sweep bytes */
-/* per segment 8 int64: kind (0 sweep, 1 fused pass, 2 one-op pass), width in, width out, ops done,
- * tile bits, updates, register groups, store mode */
+/* per segment 8 int64: kind (0 sweep, 1 fused tile pass, 2 one-op pass, 3 coset-streaming pass),
+ * width in, width out, ops done, tile bits, updates, register groups, store mode */
 int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg);
 void tg_dense_plan_free(void *plan);
 int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, void *stream);
 int tg_dense_result(void *plan, void *buf_a, void *buf_b, uint32_t *value, void *stream);
-/* execute with a CUDA event pair around every launch (on `stream`), waits for the end; out[9]:
- * for shared-memory sweeps, fused passes and one-op passes: launches, total ms, table bytes */
+/* execute with a CUDA event pair around every launch (on `stream`), waits for the end; out[12]:
+ * for shared-memory sweeps, fused tile passes, one-op passes and coset-streaming passes:
+ * launches, total ms, table bytes (nout < 12 truncates) */
 int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, double *out, int nout);
 /* per-segment launch times (ms) of the plan's last timed execution; returns the count */
 int tg_dense_segment_ms(void *plan, float *out, int64_t maxseg);

@@ -20,6 +20,7 @@
 #include "dense_types.cuh"
 
 #include <algorithm>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -258,6 +259,19 @@ __global__ void __launch_bounds__(FP_THREADS, 1) k_fused_pass_u8(const __grid_co
     u8_pass_range(P, t0, t1, in, out, smem_raw);
 }
 
+// uint8 one-group passes in the coset-streaming form: one persistent CTA per SM over a contiguous
+// range of steps (u8_stream_range).
+__global__ void __launch_bounds__(FP_THREADS, 1) k_stream_pass_u8(const __grid_constant__ PassParams P,
+                                                                 const uint8_t *__restrict__ in,
+                                                                 uint8_t *__restrict__ out) {
+    extern __shared__ uint4 smem_raw[];
+    const uint64_t nsteps = (P.ntiles + (1ull << (9 - P.nk)) - 1) >> (9 - P.nk);
+    const uint64_t per = nsteps / gridDim.x, rem = nsteps % gridDim.x;
+    const uint64_t s0 = blockIdx.x * per + ((uint64_t)blockIdx.x < rem ? (uint64_t)blockIdx.x : rem);
+    const uint64_t s1 = s0 + per + (blockIdx.x < rem ? 1 : 0);
+    u8_stream_range(P, s0, s1, in, out, smem_raw);
+}
+
 // ------------------------------------------------------------------ one op, out of place (wide masks)
 // dst = op(src) for an op whose rows do not fit a fused tile: update (code 1), expand (code 0,
 // dst holds 2n entries, the upper half INF), select (code 2).
@@ -327,14 +341,21 @@ struct Layout {
 static int g_dmax8 = 16, g_dmax16 = 15;          // fused tile bits
 static int g_sweep_bits8 = 15, g_sweep_bits16 = 14; // shared-memory sweep capacity (bits)
 static bool g_relayout = true;                       // uint8 layout planning between passes
+static bool g_cosets = true;                         // coset-streaming form of one-group uint8 passes
 
-// Groups of the pass's chunk-level updates (no bit below 4) whose chunk masks span <= 3
-// dimensions (see fused_u8.cuh); updates with in-chunk bits are listed for the shared-memory
-// path.  Also the store mode.  use_groups = 0 when the register form does not apply.
+// Groups of the pass's updates whose chunk masks (mask >> 4) span <= 3 dimensions, every update
+// in a group (the in-chunk part of a mask is free in the register form; see fused_u8.cuh).  Also
+// the thread -> coset maps and the store mode.  use_groups = 0 when the register form does not
+// apply (tiles of fewer than 7 bits).
+static inline bool has_row(const std::vector<int> &v, int r) { return std::find(v.begin(), v.end(), r) != v.end(); }
+static inline int index_of(const std::vector<int> &v, int r) { return (int)(std::find(v.begin(), v.end(), r) - v.begin()); }
+static inline bool has_bit(const std::vector<int> &v, int b) { return std::find(v.begin(), v.end(), b) != v.end(); }
+
 static void build_groups(PassParams &pp, uint32_t selmask) {
     const int CB = 4;
     (void)selmask;
     pp.use_groups = 0;
+    pp.nslow = 0;
     const int nb = pp.d - CB;
     if (nb < 3) return;
     struct G { std::vector<uint32_t> basis; std::vector<int> ups; };
@@ -354,58 +375,29 @@ static void build_groups(PassParams &pp, uint32_t selmask) {
             if ((b >> pv) & 1u) b ^= v;
         basis.push_back(v);
     };
-    pp.nslow = 0;
-    for (int u = 0; u < pp.nupd; u++) {
-        const uint32_t m = pp.upd_mask[u];
-        if (m & 15u) {
-            pp.slow_idx[pp.nslow++] = (uint8_t)u;
-            continue;
-        }
-        const uint32_t c = m >> CB;
-        bool placed = false;
-        for (G &g : gs) {
-            if (!reduce(c, g.basis) || g.basis.size() < 3) {
+    // chunk-level updates first (they shape the bases), then the in-chunk ones into the first group
+    for (int pass = 0; pass < 2; pass++) {
+        for (int u = 0; u < pp.nupd; u++) {
+            const uint32_t c = pp.upd_mask[u] >> CB;
+            if ((c == 0) != (pass == 1)) continue;
+            bool placed = false;
+            for (G &g : gs) {
+                if (!reduce(c, g.basis) || g.basis.size() < 3) {
+                    add_vec(g.basis, c);
+                    g.ups.push_back(u);
+                    placed = true;
+                    break;
+                }
+            }
+            if (!placed) {
+                G g;
                 add_vec(g.basis, c);
                 g.ups.push_back(u);
-                placed = true;
-                break;
+                gs.push_back(g);
             }
-        }
-        if (!placed) {
-            G g;
-            add_vec(g.basis, c);
-            g.ups.push_back(u);
-            gs.push_back(g);
         }
     }
     if ((int)gs.size() > FP_MAXG) return;
-    int code_i = 0;
-    for (size_t gi = 0; gi < gs.size(); gi++) {
-        G &g = gs[gi];
-        for (int b = nb - 1; b >= 0 && g.basis.size() < 3; b--) add_vec(g.basis, 1u << b);
-        std::sort(g.basis.begin(), g.basis.end(), [](uint32_t a, uint32_t b) { return __builtin_clz(a) > __builtin_clz(b); });
-        GroupDesc &D = pp.groups[gi];
-        memset(&D, 0, sizeof(D));
-        for (int j = 0; j < 3; j++) D.piv[j] = (uint8_t)(31 - __builtin_clz(g.basis[j]));
-        for (int x = 0; x < 8; x++) {
-            uint32_t o = 0;
-            for (int j = 0; j < 3; j++)
-                if ((x >> j) & 1) o ^= g.basis[j];
-            D.xoff[x] = o;
-        }
-        D.first = (uint8_t)code_i;
-        D.count = (uint8_t)g.ups.size();
-        for (int u : g.ups) {
-            const uint32_t mhi = pp.upd_mask[u] >> CB;
-            uint32_t y = 0;
-            for (int j = 0; j < 3; j++)
-                if ((mhi >> D.piv[j]) & 1u) y |= 1u << j;
-            pp.ucode[code_i] = (uint8_t)y;
-            pp.uw[code_i] = pp.upd_w[u];
-            code_i++;
-        }
-    }
-    pp.ngroups = (int)gs.size();
     // store mode from the smem weights of the four lowest output positions
     bool ident = true;
     for (int b = 0; b < CB; b++) ident = ident && pp.cmp_smem[b] == (1u << b);
@@ -423,7 +415,146 @@ static void build_groups(PassParams &pp, uint32_t selmask) {
             if (ok) { pp.store_mode = 1; pp.sel_low = sb; break; }
         }
     }
+    int code_i = 0;
+    for (size_t gi = 0; gi < gs.size(); gi++) {
+        G &g = gs[gi];
+        // output chunks from chunk pairs (store mode 1) want chunk bit 0 in the coset
+        if (pp.store_mode == 1 && g.basis.size() < 3) add_vec(g.basis, 1u);
+        for (int b = nb - 1; b >= 0 && g.basis.size() < 3; b--) add_vec(g.basis, 1u << b);
+        std::sort(g.basis.begin(), g.basis.end(), [](uint32_t a, uint32_t b) { return __builtin_clz(a) > __builtin_clz(b); });
+        GroupDesc &D = pp.groups[gi];
+        memset(&D, 0, sizeof(D));
+        uint32_t piv = 0;
+        int pv[3];
+        for (int j = 0; j < 3; j++) {
+            pv[j] = 31 - __builtin_clz(g.basis[j]);
+            piv |= 1u << pv[j];
+        }
+        // coset number -> chunk bits: the three lowest non-pivot bits of distinct residues mod 3
+        // first (the lanes of a quarter warp: distinct bank quads under the slot swizzle), then
+        // the other non-pivot bits ascending
+        std::vector<int> free_bits, order;
+        for (int b = 0; b < nb; b++) if (!((piv >> b) & 1u)) free_bits.push_back(b);
+        for (int r = 0; r < 3 && (int)order.size() < 3; r++) {
+            (void)r;
+            for (int b : free_bits) {
+                bool clash = false;
+                for (int o : order) clash |= (o % 3) == (b % 3);
+                if (!clash && !has_bit(order, b)) { order.push_back(b); break; }
+            }
+        }
+        for (int b : free_bits) if (!has_bit(order, b)) order.push_back(b);
+        for (size_t j = 0; j < order.size(); j++) D.tpos[j] = (uint8_t)order[j];
+        for (int x = 0; x < 8; x++) {
+            uint32_t o = 0;
+            for (int j = 0; j < 3; j++)
+                if ((x >> j) & 1) o ^= g.basis[j];
+            D.xoff[x] = o;
+        }
+        D.first = (uint8_t)code_i;
+        D.count = (uint8_t)g.ups.size();
+        for (int u : g.ups) {
+            const uint32_t m = pp.upd_mask[u], mhi = m >> CB, mlo = m & 15u;
+            uint32_t y = 0;
+            for (int j = 0; j < 3; j++)
+                if ((mhi >> pv[j]) & 1u) y |= 1u << j;
+            const uint32_t X = 8 * y + 2 * (mlo >> 2) + (mlo & 1u);
+            pp.ucode[code_i] = (uint8_t)(X | (((mlo >> 1) & 1u) << 6));
+            pp.uw[code_i] = pp.upd_w[u];
+            code_i++;
+        }
+    }
+    pp.ngroups = (int)gs.size();
     pp.use_groups = 1;
+}
+
+// The coset-streaming form of a one-group uint8 pass (u8_stream_range): the thread -> coset map,
+// the input / output offsets of the coset members and of the coset-number bits, and the store
+// form.  local: tile rows (local bit -> row), out: output order, d_in: local bits read from the input.
+static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in, const std::vector<int> &out,
+                         const std::vector<int> &sel_rows, const std::vector<int> &sel_tg, int w_in, int w_out) {
+    const int CB = 4, nb = pp.d - CB;
+    pp.stream = 0;
+    if (!pp.use_groups || pp.ngroups != 1 || nb < 3 || w_in > 32 || w_out > 32) return;
+    const GroupDesc &G = pp.groups[0];
+    const uint32_t bas[3] = {G.xoff[1], G.xoff[2], G.xoff[4]};
+    uint32_t piv = 0, supp = 0;
+    for (int q = 0; q < 3; q++) {
+        piv |= 1u << (31 - __builtin_clz(bas[q]));
+        supp |= bas[q];
+    }
+    if (pp.store_mode == 0) pp.s_mode = 0;
+    else if (pp.store_mode == 1 && bas[0] == 1u) pp.s_mode = 1;
+    else return;
+    std::vector<int> opos(pp.d, -1);
+    for (int lb = 0; lb < pp.d; lb++) {
+        const int q = index_of(out, local[lb]);
+        if (q < (int)out.size()) opos[lb] = q;
+    }
+    auto inw = [&](int b) -> uint64_t { return CB + b < d_in ? pp.loc_in[CB + b] : 0; };
+    auto outw = [&](int b) -> uint64_t { return opos[CB + b] >= CB ? (1ull << opos[CB + b]) : 0; };
+    uint32_t fixed = 0;
+    pp.cfix = pp.selm = pp.selb = pp.expm = 0;
+    for (size_t q = 0; q < sel_rows.size(); q++) {
+        const int lb = index_of(local, sel_rows[q]);
+        const uint32_t t = sel_tg[q] ? 1u : 0u;
+        if (lb < CB) {
+            if (pp.s_mode != 1 || lb != pp.sel_low) return;
+            continue;
+        }
+        const int b = lb - CB;
+        if (!((supp >> b) & 1u)) {
+            fixed |= 1u << b;
+            pp.cfix |= t << b;
+        } else {
+            pp.selm |= 1u << b;
+            pp.selb |= t << b;
+        }
+    }
+    for (int lb = std::max(d_in, CB); lb < pp.d; lb++) pp.expm |= 1u << (lb - CB);
+    // coset-number bits: the free chunk bits, inputs by ascending address (coalesced lanes), then
+    // the expanded ones
+    std::vector<int> kp;
+    for (int b = 0; b < nb; b++)
+        if (!((piv >> b) & 1u) && !((fixed >> b) & 1u)) kp.push_back(b);
+    std::stable_sort(kp.begin(), kp.end(), [&](int a, int b) {
+        const uint64_t wa = inw(a) ? inw(a) : ~0ull, wb = inw(b) ? inw(b) : ~0ull;
+        return wa < wb;
+    });
+    if (kp.size() > 9) return;
+    pp.nk = (int)kp.size();
+    for (int q = 0; q < pp.nk; q++) {
+        pp.kpos[q] = (uint8_t)kp[q];
+        pp.kin[q] = (uint32_t)inw(kp[q]);
+        pp.kout[q] = (uint32_t)outw(kp[q]);
+    }
+    for (int x = 0; x < 8; x++) {
+        uint64_t a = 0, o = 0;
+        for (int b = 0; b < nb; b++)
+            if ((G.xoff[x] >> b) & 1u) { a ^= inw(b); o ^= outw(b); }
+        pp.xin[x] = (uint32_t)a;
+        pp.xout[x] = (uint32_t)o;
+    }
+    uint64_t fa = 0, fo = 0;
+    for (int b = 0; b < nb; b++)
+        if ((pp.cfix >> b) & 1u) { fa ^= inw(b); fo ^= outw(b); }
+    pp.fin = (uint32_t)fa;
+    pp.fout = (uint32_t)fo;
+    if (pp.s_mode == 1) {
+        const int sb = pp.sel_low;
+        const int r = local[sb];
+        pp.s_bit = sb;
+        pp.s_both = has_row(sel_rows, r) ? 0 : 1;
+        pp.s_tgt = 0;
+        pp.s_w = 0;
+        if (pp.s_both) {
+            if (opos[sb] < CB) return;
+            pp.s_w = (uint32_t)(1ull << opos[sb]);
+        } else {
+            pp.s_tgt = sel_tg[index_of(sel_rows, r)] ? 1u : 0u;
+        }
+    }
+    pp.stream = 1;
 }
 
 // Row bookkeeping of an op stream: which rows each op touches (rows are numbered in order of
@@ -463,8 +594,6 @@ static void row_info(const std::vector<HostOp> &hops, RowInfo &R) {
     }
 }
 
-static inline bool has_row(const std::vector<int> &v, int r) { return std::find(v.begin(), v.end(), r) != v.end(); }
-static inline int index_of(const std::vector<int> &v, int r) { return (int)(std::find(v.begin(), v.end(), r) - v.begin()); }
 
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt,
                      DensePlan &P) {
@@ -531,7 +660,8 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             int evict = -1, cand = -1;
             std::vector<int> sel_in;
             for (int r : inchunk) if (has_row(sel_rows, r)) sel_in.push_back(r);
-            if (!force && relayout && sel_in.size() <= 1) {
+            const bool srule = eb == 1 && g_cosets;
+            if (!force && relayout && sel_in.size() <= 1 && (!srule || sel_in.size() == 1)) {
                 if (sel_in.size() == 1) {
                     evict = sel_in[0];
                 } else {
@@ -547,7 +677,9 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                     int64_t far = -1;
                     auto consider = [&](int r) {
                         if (has_row(inchunk, r) || has_row(sel_rows, r) || !has_row(lin, r)) return;
-                        int64_t nu = RI.next_use(r, j0);
+                        // streaming form: the row that stays longest (in-chunk rows are free in the
+                        // register form); else the row with the furthest next use
+                        int64_t nu = srule ? RI.uses[r].empty() ? INT64_MAX : RI.uses[r].back() : RI.next_use(r, j0);
                         if (nu > far) { far = nu; cand = r; }
                     };
                     for (int r : trows) consider(r);
@@ -647,7 +779,10 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                 pp.upd_mask[u] = m;
                 pp.upd_w[u] = (uint8_t)upd[u].second;
             }
-            if (eb == 1) build_groups(pp, selmask);
+            if (eb == 1) {
+                build_groups(pp, selmask);
+                if (g_cosets) build_stream(pp, local, d_in, out, sel_rows, sel_tg, w_in, (int)cout_.size());
+            }
             phys = out;
             canon = cout_;
             S.kind = 1;
@@ -705,6 +840,13 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             std::vector<int> cur = canon, touched;
             int nupd = 0;
             int64_t j = i;
+            // coset-streaming passes (uint8): the updates' masks outside the in-chunk rows span at most
+            // 3 dimensions (one register group), at most one in-chunk row closes, and then at most 2
+            // (the row entering the in-chunk positions joins the coset)
+            const bool srule = eb == 1 && g_cosets && relayout;
+            std::vector<int> srows;                     // row -> bit of the span vectors
+            std::vector<uint64_t> sbasis;
+            int nsel_in = 0;
             while (j < limit && nupd < FP_MAXU) {
                 const HostOp &o = hops[j];
                 std::vector<int> t2 = touched, cur2 = cur;
@@ -722,6 +864,35 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                     need.push_back(-1);       // room for a row entering the in-chunk positions
                 }
                 if ((int)need.size() > DMAX) break;
+                if (srule) {
+                    std::vector<uint64_t> b2 = sbasis;
+                    int ns2 = nsel_in;
+                    if (o.code == 1) {
+                        uint64_t v = 0;
+                        bool fits = true;
+                        for (int r : RI.upd_rows[j]) {
+                            if (has_row(inchunk, r)) continue;
+                            int q = index_of(srows, r);
+                            if (q == (int)srows.size()) {
+                                if (q >= 64) { fits = false; break; }
+                                srows.push_back(r);
+                            }
+                            v |= 1ull << q;
+                        }
+                        if (!fits) break;
+                        for (uint64_t b : b2)
+                            if ((v ^ b) < v) v ^= b;
+                        if (v) {
+                            b2.push_back(v);
+                            std::sort(b2.begin(), b2.end(), std::greater<uint64_t>());
+                        }
+                    } else if (o.code == 2 && has_row(inchunk, RI.sel_row[j])) {
+                        ns2++;
+                    }
+                    if (ns2 > 1 || (int)b2.size() > (ns2 ? 2 : 3)) break;
+                    sbasis.swap(b2);
+                    nsel_in = ns2;
+                }
                 touched.swap(t2);
                 cur.swap(cur2);
                 if (o.code == 1) nupd++;
@@ -792,6 +963,8 @@ int set_dense_attrs() {
     if (e) return e;
     e = cuda_check(cudaFuncSetAttribute(k_fused_pass_u8, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 << 16), "attr");
     if (e) return e;
+    e = cuda_check(cudaFuncSetAttribute(k_stream_pass_u8, cudaFuncAttributeMaxDynamicSharedMemorySize, 16 * FS_WARP_BYTES), "attr");
+    if (e) return e;
     g_attr_done = true;
     return TG_OK;
 }
@@ -838,7 +1011,12 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
             k_sweep_smem<E><<<1, 512, sm, st>>>(S.sp, src, dst);
         } else {
             size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
-            if (sizeof(E) == 1 && S.pp.use_groups) {
+            if (sizeof(E) == 1 && S.pp.stream) {
+                const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nk)) - 1) >> (9 - S.pp.nk);
+                const uint64_t grid = std::min<uint64_t>(nsteps, (uint64_t)sm_count());
+                k_stream_pass_u8<<<(unsigned)grid, FP_THREADS, 16 * FS_WARP_BYTES, st>>>(S.pp, (const uint8_t *)src,
+                                                                                    (uint8_t *)dst);
+            } else if (sizeof(E) == 1 && S.pp.use_groups) {
                 // persistent: one CTA per SM, three tile buffers
                 uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());
                 k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 3 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
@@ -868,54 +1046,105 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
 // arithmetic (entry-level arithmetic instead of packed chunks).  Used by the CPU test-suite to
 // check the scheduler; the evaluators never call it.
 // the register-group update of k_fused_pass_u8 on host memory: same cosets, register model,
-// codes and lane arithmetic as run_group / grp_update
+// codes and lane arithmetic as run_group / reg_dispatch
+// one update of the register form (reg_dispatch) on an emulated register file
+static void emu_reg_update(uint32_t (&R)[64], uint32_t code, uint32_t w) {
+    auto sw = [](uint32_t v) { return (v >> 16) | (v << 16); };
+    auto addmin = [](uint32_t b, uint32_t w_, uint32_t a) {
+        uint32_t lo = std::min((b & 0xFFFFu) + w_, a & 0xFFFFu);
+        uint32_t hi = std::min((b >> 16) + w_, a >> 16);
+        return lo | (hi << 16);
+    };
+    const uint32_t X = code & 63u, HS = code >> 6;
+    for (uint32_t i = 0; i < 64; i++) {
+        const uint32_t j = i ^ X;
+        if (X == 0) {
+            if (HS) R[i] = addmin(sw(R[i]), w, R[i]);
+        } else if (i < j) {
+            const uint32_t a = R[i], b = R[j];
+            R[i] = addmin(HS ? sw(b) : b, w, a);
+            R[j] = addmin(HS ? sw(a) : a, w, b);
+        }
+    }
+}
+static void emu_unpack(const uint8_t *ch, uint32_t *R8) {      // one chunk -> R[8x .. 8x + 7]
+    for (int wd = 0; wd < 4; wd++) {
+        R8[2 * wd] = ch[4 * wd] | ((uint32_t)ch[4 * wd + 2] << 16);
+        R8[2 * wd + 1] = ch[4 * wd + 1] | ((uint32_t)ch[4 * wd + 3] << 16);
+    }
+}
+static void emu_pack(const uint32_t *R8, uint8_t *ch) {
+    for (int wd = 0; wd < 4; wd++) {
+        const uint32_t e = R8[2 * wd], o = R8[2 * wd + 1];
+        ch[4 * wd] = (uint8_t)(e & 0xFF);
+        ch[4 * wd + 2] = (uint8_t)(e >> 16);
+        ch[4 * wd + 1] = (uint8_t)(o & 0xFF);
+        ch[4 * wd + 3] = (uint8_t)(o >> 16);
+    }
+}
+
 static void emulate_groups(const PassParams &pp, uint8_t *T) {
-    const uint32_t ncos = 1u << (pp.d - 4 - 3);
+    const int nt = pp.d - 4 - 3;
+    const uint32_t ncos = 1u << nt;
     for (int g = 0; g < pp.ngroups; g++) {
         const GroupDesc &G = pp.groups[g];
         for (uint32_t k = 0; k < ncos; k++) {
-            uint32_t c0 = k;
-            for (int j = 0; j < 3; j++) {
-                uint32_t lo = c0 & ((1u << G.piv[j]) - 1);
-                c0 = ((c0 ^ lo) << 1) | lo;
-            }
+            uint32_t c0 = 0;
+            for (int j = 0; j < nt; j++) c0 |= ((k >> j) & 1u) << G.tpos[j];
             uint32_t R[64];
+            for (int x = 0; x < 8; x++) emu_unpack(T + 16 * (size_t)(c0 ^ G.xoff[x]), R + 8 * x);
+            for (int u = 0; u < G.count; u++) emu_reg_update(R, pp.ucode[G.first + u], pp.uw[G.first + u]);
+            for (int x = 0; x < 8; x++) emu_pack(R + 8 * x, T + 16 * (size_t)(c0 ^ G.xoff[x]));
+        }
+    }
+}
+
+// the coset-streaming pass (u8_stream_range) on host memory: the same steps, coset map, offsets
+// and store forms, thread by thread
+static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *dst) {
+    const int g = 9 - pp.nk;
+    const int ng = std::min(g, pp.n_outer);
+    const uint64_t nsteps = (pp.ntiles + (1ull << g) - 1) >> g;
+    const GroupDesc &G = pp.groups[0];
+    for (uint64_t s = 0; s < nsteps; s++) {
+        for (uint32_t tid = 0; tid < FP_THREADS; tid++) {
+            const uint32_t k = tid & ((1u << pp.nk) - 1u), j = tid >> pp.nk;
+            if (((s << g) | j) >= pp.ntiles) continue;
+            uint32_t c0 = pp.cfix, inc = pp.fin, outc = pp.fout;
+            for (int q = 0; q < pp.nk; q++)
+                if ((k >> q) & 1u) { c0 |= 1u << pp.kpos[q]; inc ^= pp.kin[q]; outc ^= pp.kout[q]; }
+            uint64_t ib = 0, ob = 0;
+            for (int q = 0; q < ng; q++)
+                if ((j >> q) & 1u) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
+            for (int q = ng; q < pp.n_outer; q++)
+                if ((s >> (q - ng)) & 1ull) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
+            uint32_t R[64];
+            uint8_t ch[16];
             for (int x = 0; x < 8; x++) {
-                const uint8_t *ch = T + 16 * (size_t)(c0 ^ G.xoff[x]);
-                for (int wd = 0; wd < 4; wd++) {
-                    R[8 * x + 2 * wd] = ch[4 * wd] | ((uint32_t)ch[4 * wd + 2] << 16);
-                    R[8 * x + 2 * wd + 1] = ch[4 * wd + 1] | ((uint32_t)ch[4 * wd + 3] << 16);
-                }
+                const uint32_t c = c0 ^ G.xoff[x];
+                if (c & pp.expm) memset(ch, 0xFF, 16);
+                else memcpy(ch, src + ib + (inc ^ pp.xin[x]), 16);
+                emu_unpack(ch, R + 8 * x);
             }
-            auto sw = [](uint32_t v) { return (v >> 16) | (v << 16); };
-            auto addmin = [](uint32_t b, uint32_t w, uint32_t a) {
-                uint32_t lo = std::min((b & 0xFFFFu) + w, a & 0xFFFFu);
-                uint32_t hi = std::min((b >> 16) + w, a >> 16);
-                return lo | (hi << 16);
-            };
-            for (int u = 0; u < G.count; u++) {
-                uint32_t w = pp.uw[G.first + u];
-                uint32_t Y = (uint32_t)pp.ucode[G.first + u] << 3, HS = 0;
-                for (uint32_t i = 0; i < 64; i++) {
-                    uint32_t j = i ^ Y;
-                    if (Y == 0) {
-                        R[i] = addmin(sw(R[i]), w, R[i]);
-                    } else if (i < j) {
-                        uint32_t a = R[i], q = HS ? sw(R[j]) : R[j];
-                        uint32_t na = addmin(q, w, a), nq = addmin(a, w, q);
-                        R[i] = na;
-                        R[j] = HS ? sw(nq) : nq;
+            for (int u = 0; u < G.count; u++) emu_reg_update(R, pp.ucode[u], pp.uw[u]);
+            uint8_t W[8][16];
+            for (int x = 0; x < 8; x++) emu_pack(R + 8 * x, W[x]);
+            for (int x = 0; x < 8; x++) {
+                const uint32_t c = c0 ^ G.xoff[x];
+                if ((c & pp.selm) != pp.selb) continue;
+                if (pp.s_mode == 0) {
+                    memcpy(dst + ob + (outc ^ pp.xout[x]), W[x], 16);
+                } else if ((x & 1) == 0) {
+                    const int sb = pp.s_bit;
+                    for (uint32_t t = 0; t < 2; t++) {
+                        if (!pp.s_both && t != pp.s_tgt) continue;
+                        uint8_t *o = dst + ob + (outc ^ pp.xout[x]) + (pp.s_both ? t * pp.s_w : 0);
+                        for (uint32_t e = 0; e < 16; e++) {
+                            const uint32_t lo = e & ((1u << sb) - 1);
+                            const uint32_t se = ((e ^ lo) << 1) | lo | (t << sb);
+                            o[e] = se < 16 ? W[x][se] : W[x + 1][se - 16];
+                        }
                     }
-                }
-            }
-            for (int x = 0; x < 8; x++) {
-                uint8_t *ch = T + 16 * (size_t)(c0 ^ G.xoff[x]);
-                for (int wd = 0; wd < 4; wd++) {
-                    uint32_t e = R[8 * x + 2 * wd], o = R[8 * x + 2 * wd + 1];
-                    ch[4 * wd] = (uint8_t)(e & 0xFF);
-                    ch[4 * wd + 2] = (uint8_t)(e >> 16);
-                    ch[4 * wd + 1] = (uint8_t)(o & 0xFF);
-                    ch[4 * wd + 3] = (uint8_t)(o >> 16);
                 }
             }
         }
@@ -979,7 +1208,9 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
         } else {
             const PassParams &pp = S.pp;
             std::vector<E> T((size_t)1 << pp.d);
-            for (uint64_t tile = 0; tile < pp.ntiles; tile++) {
+            if (sizeof(E) == 1 && pp.stream)
+                emulate_stream(pp, reinterpret_cast<const uint8_t *>(src), reinterpret_cast<uint8_t *>(dst));
+            else for (uint64_t tile = 0; tile < pp.ntiles; tile++) {
                 uint64_t ib = 0, ob = 0;
                 for (int k = 0; k < pp.n_outer; k++)
                     if ((tile >> k) & 1ull) { ib += pp.outer_in[k]; ob += pp.outer_out[k]; }
@@ -1172,7 +1403,7 @@ int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg) {
     for (const Seg &S : P.segs) {
         if (k >= maxseg) break;
         int64_t *o = out + 8 * k;
-        o[0] = S.kind;
+        o[0] = S.kind == 1 && S.pp.stream ? 3 : S.kind;
         o[1] = S.w_in;
         o[2] = S.w_out;
         o[3] = S.op_end;
@@ -1210,7 +1441,8 @@ int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, voi
 }
 
 int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, double *out, int nout) {
-    // out: per segment kind (0 sweep, 1 fused pass, 2 one-op pass): launches, total ms, bytes
+    // out: per segment kind (0 sweep, 1 fused tile pass, 2 one-op pass, 3 coset-streaming pass):
+    // launches, total ms, bytes
     if (!plan || !buf_a || !buf_b || !out) return set_error(TG_ERR_ARG, "null argument");
     const DensePlan &P = *static_cast<DensePlan *>(plan);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1222,7 +1454,7 @@ int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, d
     if (P.segs.empty()) return TG_OK;
     e = cuda_check(cudaEventSynchronize(g_events[2 * P.segs.size() - 1]), "event sync");
     if (e) return e;
-    double acc[9] = {0};
+    double acc[12] = {0};
     DensePlan &PM = *static_cast<DensePlan *>(plan);
     PM.seg_ms.assign(P.segs.size(), 0.f);
     for (size_t k = 0; k < P.segs.size(); k++) {
@@ -1230,14 +1462,14 @@ int tg_dense_execute_timed(void *plan, void *buf_a, void *buf_b, void *stream, d
         float ms = 0.f;
         cudaEventElapsedTime(&ms, g_events[2 * k], g_events[2 * k + 1]);
         PM.seg_ms[k] = ms;
-        int kk = S.kind;
+        const int kk = S.kind == 1 && S.pp.stream ? 3 : S.kind;
         acc[3 * kk] += 1;
         acc[3 * kk + 1] += ms;
         double bytes = S.kind == 0 ? (double)P.eb * ((S.sp.has_in ? (1ull << S.w_in) : 0) + (1ull << S.w_out))
                                    : (double)P.eb * ((1ull << S.w_in) + (1ull << S.w_out));
         acc[3 * kk + 2] += bytes;
     }
-    for (int k = 0; k < nout && k < 9; k++) out[k] = acc[k];
+    for (int k = 0; k < nout && k < 12; k++) out[k] = acc[k];
     return TG_OK;
 }
 

@@ -132,6 +132,21 @@ struct PassParams {
     GroupDesc groups[FP_MAXG];
     uint8_t ucode[FP_MAXU];
     uint8_t uw[FP_MAXU];
+    // coset-streaming form of a one-group uint8 pass (k_stream_pass_u8): thread k of a tile takes
+    // the coset of chunk c0 = deposit(k, kpos) | cfix and goes global -> registers -> global
+    int stream;                        // 1: the streaming form applies
+    int s_mode;                        // 0 one output chunk per tile chunk; 1 output chunks from the
+                                       // chunk pairs (x, x + 1) without in-chunk bit s_bit
+    int s_bit, s_both;                 // mode 1: both halves of s_bit stored (evicted row) or only s_tgt
+    uint32_t s_tgt, s_w;               // mode 1: target (selected row) / output offset of the evicted row
+    int nk;                            // coset-number bits: a tile has 2^nk cosets, a block 512 >> nk tiles
+    uint8_t kpos[16];                  // local chunk bit receiving coset-number bit j
+    uint32_t cfix;                     // chunk bits fixed in every coset (selected rows outside the span)
+    uint32_t expm;                     // chunk bits of the rows expanded in the pass (their 1-half is INF)
+    uint32_t selm, selb;               // chunk bits of the selected rows in the span, and their targets
+    uint32_t kin[16], kout[16];        // input / output offsets of coset-number bit j
+    uint32_t xin[8], xout[8];          // input / output offsets of the coset members xoff[x]
+    uint32_t fin, fout;                // input / output offsets of cfix
 };
 
 __device__ __forceinline__ uint64_t pdep_w64(uint32_t x, const uint64_t *wt, int nb) {
@@ -178,6 +193,32 @@ struct DensePlan {
 };
 
 
+// Output chunk of a uint8 tile whose compacted entry 0 is tile entry sidx (the selected bits
+// already in place): mode 0 one slot, 1 two slots without local bit sel_low (< 4), 2 byte gathers
+// through pat; sm is the slot swizzle of the tile (tslot).
+static __device__ __forceinline__ uint4 u8_out_chunk(const uint4 *TC, int mode, uint32_t sidx, const PassParams &P,
+                                                    uint32_t sm) {
+    constexpr int CB = 4;
+    if (mode == 0) return TC[tslot(sidx >> CB, sm)];
+    if (mode == 1) {
+        const uint32_t s0 = tslot((sidx >> 5) << 1, sm);
+        return gather_one_select(TC[s0], TC[s0 ^ 1u], P.sel_low, (sidx >> P.sel_low) & 1u);
+    }
+    const uint8_t *T = reinterpret_cast<const uint8_t *>(TC);
+    uint32_t wd[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const uint32_t b = sidx + P.pat[4 * k + e];
+            word |= (uint32_t)T[(tslot(b >> CB, sm) << CB) | (b & 15u)] << (8 * e);
+        }
+        wd[k] = word;
+    }
+    return make_uint4(wd[0], wd[1], wd[2], wd[3]);
+}
+
 // One tile of a fused uint8 pass by one block of NT threads, without pipelining (the batched
 // kernel's unit of work): load the tile's input chunks (cp.async, through L2), INF over the rows
 // expanded in the pass, the register groups and the shared-memory updates, and the store of the
@@ -192,19 +233,15 @@ static __device__ void u8_tile(const PassParams &P, uint64_t tile, const uint8_t
     uint64_t ib = 0, ob = 0;
     for (int k = 0; k < P.n_outer; k++)
         if ((tile >> k) & 1ull) { ib += P.outer_in[k]; ob += P.outer_out[k]; }
-    for (uint32_t c = tid; c < nch_in; c += NT) cp_async16(TC + c, in + ib + pdep_w64(c, P.loc_in + CB, nb_in));
-    for (uint32_t c = nch_in + tid; c < nch_all; c += NT) TC[c] = make_uint4(~0u, ~0u, ~0u, ~0u);
+    const uint32_t sm = P.use_groups ? 7u : 0u;        // slot swizzle of the register-group form
+    for (uint32_t c = tid; c < nch_in; c += NT) cp_async16(TC + tslot(c, sm), in + ib + pdep_w64(c, P.loc_in + CB, nb_in));
+    for (uint32_t c = nch_in + tid; c < nch_all; c += NT) TC[tslot(c, sm)] = make_uint4(~0u, ~0u, ~0u, ~0u);
     cp_async_wait_all();
     __syncthreads();
     uint8_t *T = reinterpret_cast<uint8_t *>(TC);
     if (P.use_groups) {
         for (int g = 0; g < P.ngroups; g++) {
             run_group<NT>(TC, P.d, P.groups[g], P.ucode, P.uw);
-            __syncthreads();
-        }
-        for (int u = 0; u < P.nslow; u++) {
-            const int k = P.slow_idx[u];
-            smem_update<uint8_t>(T, P.d, P.upd_mask[k], P.upd_w[k]);
             __syncthreads();
         }
     } else {
@@ -217,24 +254,7 @@ static __device__ void u8_tile(const PassParams &P, uint64_t tile, const uint8_t
     for (uint32_t q = tid; q < nch_out; q += NT) {
         const uint64_t off = ob + pdep_w64(q, P.cmp_out + CB, nb_out);
         const uint32_t sidx = pdep_w32(q, P.cmp_smem + CB, nb_out) + P.sel_bits;
-        uint4 v;
-        if (mode == 0) {
-            v = TC[sidx >> CB];
-        } else if (mode == 1) {
-            const uint32_t base = (sidx >> 5) << 1;
-            v = gather_one_select(TC[base], TC[base + 1], P.sel_low, (sidx >> P.sel_low) & 1u);
-        } else {
-            uint32_t wd[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                uint32_t word = 0;
-#pragma unroll
-                for (int e = 0; e < 4; e++) word |= (uint32_t)T[sidx + P.pat[4 * k + e]] << (8 * e);
-                wd[k] = word;
-            }
-            v = make_uint4(wd[0], wd[1], wd[2], wd[3]);
-        }
-        *reinterpret_cast<uint4 *>(out + off) = v;
+        *reinterpret_cast<uint4 *>(out + off) = u8_out_chunk(TC, mode, sidx, P, sm);
     }
 }
 
@@ -284,11 +304,11 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
     auto issue_load = [&](uint64_t ib, uint4 *TC) {
         const uint8_t *src = inb + ib;
         if (in_full) {
-            for (uint32_t it = 0; it < it_in; it++) cp_async16(TC + it * FP_THREADS + tid, src + s_in_hi[it]);
+            for (uint32_t it = 0; it < it_in; it++) cp_async16(TC + tslot(it * FP_THREADS + tid, 7u), src + s_in_hi[it]);
         } else if (tid < nch_in) {
-            cp_async16(TC + tid, src);
+            cp_async16(TC + tslot(tid, 7u), src);
         }
-        for (uint32_t c = nch_in + tid; c < nch_all; c += FP_THREADS) TC[c] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        for (uint32_t c = nch_in + tid; c < nch_all; c += FP_THREADS) TC[tslot(c, 7u)] = make_uint4(~0u, ~0u, ~0u, ~0u);
         cp_async_commit();
     };
     auto advance = [&](uint64_t t, uint64_t &ib, uint64_t &ob) {   // bases of tile t + 1 from tile t
@@ -317,14 +337,8 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
         else cp_async_wait_group<0>();
         __syncthreads();
         uint4 *TC = cur == 0 ? buf0 : cur == 1 ? buf1 : buf2;
-        const uint8_t *T = reinterpret_cast<const uint8_t *>(TC);
         for (int g = 0; g < P.ngroups; g++) {
             run_group<FP_THREADS>(TC, P.d, P.groups[g], P.ucode, P.uw);
-            __syncthreads();
-        }
-        for (int u = 0; u < P.nslow; u++) {
-            const int k = P.slow_idx[u];
-            smem_update<uint8_t>(reinterpret_cast<uint8_t *>(TC), P.d, P.upd_mask[k], P.upd_w[k]);
             __syncthreads();
         }
         uint8_t *dstb = out + ob + tid_out;
@@ -332,24 +346,7 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
             const uint32_t q = it * FP_THREADS + tid;
             if (!out_full && q >= nch_out) break;
             const uint32_t sidx = tid_sm + s_sm_hi[it];
-            uint4 v;
-            if (P.store_mode == 0) {
-                v = TC[sidx >> CB];
-            } else if (P.store_mode == 1) {
-                const uint32_t base = (sidx >> 5) << 1;
-                v = gather_one_select(TC[base], TC[base + 1], P.sel_low, (sidx >> P.sel_low) & 1u);
-            } else {
-                uint32_t wd[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    uint32_t word = 0;
-#pragma unroll
-                    for (int e = 0; e < 4; e++) word |= (uint32_t)T[sidx + P.pat[4 * k + e]] << (8 * e);
-                    wd[k] = word;
-                }
-                v = make_uint4(wd[0], wd[1], wd[2], wd[3]);
-            }
-            __stcs(reinterpret_cast<uint4 *>(dstb + s_out_hi[it]), v);
+            __stcs(reinterpret_cast<uint4 *>(dstb + s_out_hi[it]), u8_out_chunk(TC, P.store_mode, sidx, P, 7u));
         }
         __syncthreads();
         cur = cur == 2 ? 0 : cur + 1;
@@ -357,6 +354,131 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
     }
 }
 
+
+// ------------------------------------------------------------------ coset-streaming pass (uint8)
+// A one-group pass without a shared-memory tile: thread k of tile t owns the coset {c0 ^ X[x]} of
+// the tile's chunks (c0 fixed per thread for the whole launch), stages its 8 input chunks in its
+// own shared-memory slots with cp.async three tiles ahead (no barriers: a thread reads back only
+// its own copies), applies the group's updates in registers and stores the output chunks straight
+// to global memory.  A block covers 512 >> nk tiles per step; steps [s0, s1) in order.
+#define FS_STAGES 3
+#define FS_WARP_BYTES (FS_STAGES * 8 * 512)      // staging bytes of one warp
+
+static __device__ __noinline__ void u8_stream_range(const PassParams &P, uint64_t s0, uint64_t s1,
+                                                   const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                   uint4 *smem_raw) {
+    __shared__ int64_t s_cin[FP_MAXOUTER], s_cout[FP_MAXOUTER];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const int g = 9 - P.nk;                            // log2 of the tiles per step
+    const uint32_t k = tid & ((1u << P.nk) - 1u), j = tid >> P.nk;
+    const int ng = min(g, P.n_outer);
+    if (tid < (uint32_t)P.n_outer && (int)tid >= ng) {
+        // carry table of the step index: base(s + 1) - base(s) when bit tid - ng is the lowest zero bit of s
+        int64_t ci = (int64_t)P.outer_in[tid], co = (int64_t)P.outer_out[tid];
+        for (int q = ng; q < (int)tid; q++) { ci -= (int64_t)P.outer_in[q]; co -= (int64_t)P.outer_out[q]; }
+        s_cin[tid] = ci;
+        s_cout[tid] = co;
+    }
+    // the thread's coset (constant for the launch): its chunk offsets, kept and INF members
+    uint32_t c0 = P.cfix, inc = P.fin, outc = P.fout;
+    for (int q = 0; q < P.nk; q++)
+        if ((k >> q) & 1u) { c0 |= 1u << P.kpos[q]; inc ^= P.kin[q]; outc ^= P.kout[q]; }
+    uint32_t keep = 0, inf = 0;
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+        const uint32_t c = c0 ^ P.groups[0].xoff[x];
+        if ((c & P.selm) == P.selb) keep |= 1u << x;
+        if (c & P.expm) inf |= 1u << x;
+    }
+    uint64_t jin = 0, jout = 0;                        // the thread's tile within a step
+    for (int q = 0; q < ng; q++)
+        if ((j >> q) & 1u) { jin += P.outer_in[q]; jout += P.outer_out[q]; }
+    uint64_t ib = jin, ob = jout;                      // bases of step s0
+    for (int q = ng; q < P.n_outer; q++)
+        if ((s0 >> (q - ng)) & 1ull) { ib += P.outer_in[q]; ob += P.outer_out[q]; }
+    const uint64_t ntiles = P.ntiles;
+    __syncthreads();
+
+    uint8_t *const stage0 = reinterpret_cast<uint8_t *>(smem_raw) + (size_t)warp * FS_WARP_BYTES + lane * 16u;
+    auto issue = [&](uint64_t s, uint64_t b, int st) {
+        if ((((s << g) | j) < ntiles)) {
+            uint8_t *dst = stage0 + st * 4096;
+#pragma unroll
+            for (int x = 0; x < 8; x++)
+                if (!((inf >> x) & 1u)) cp_async16(dst + x * 512, in + b + (inc ^ P.xin[x]));
+        }
+        cp_async_commit();
+    };
+    auto advance = [&](uint64_t s, uint64_t &bi, uint64_t &bo) {   // bases of step s + 1 from step s
+        const int q = __ffsll((long long)~s) - 1 + ng;
+        if (q < P.n_outer) { bi += s_cin[q]; bo += s_cout[q]; }
+    };
+    const int nu = P.groups[0].count;
+    uint64_t ibn = ib, dummy = 0;
+    // prologue: steps s0 and s0 + 1 in flight
+    issue(s0, ibn, 0);
+    if (s0 + 1 < s1) {
+        advance(s0, ibn, dummy);
+        issue(s0 + 1, ibn, 1);
+    } else {
+        cp_async_commit();
+    }
+    int st = 0;
+    for (uint64_t s = s0; s < s1; s++) {
+        if (s + 2 < s1) {
+            advance(s + 1, ibn, dummy);
+            issue(s + 2, ibn, st == 0 ? 2 : st - 1);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_group<2>();
+        if (((s << g) | j) < ntiles) {
+            const uint8_t *src = stage0 + st * 4096;
+            uint32_t R[64];
+#pragma unroll
+            for (int x = 0; x < 8; x++) {
+                uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
+                if (!((inf >> x) & 1u)) v = *reinterpret_cast<const uint4 *>(src + x * 512);
+                unpack_eo(v.x, R[8 * x + 0], R[8 * x + 1]);
+                unpack_eo(v.y, R[8 * x + 2], R[8 * x + 3]);
+                unpack_eo(v.z, R[8 * x + 4], R[8 * x + 5]);
+                unpack_eo(v.w, R[8 * x + 6], R[8 * x + 7]);
+            }
+            for (int u = 0; u < nu; u++) {
+                const uint32_t w = P.uw[u];
+                reg_dispatch(P.ucode[u], R, w | (w << 16));
+            }
+            uint32_t W[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++) W[q] = pack_eo(R[2 * q], R[2 * q + 1]);
+            uint8_t *const dst = out + ob;
+            if (P.s_mode == 0) {
+#pragma unroll
+                for (int x = 0; x < 8; x++)
+                    if ((keep >> x) & 1u)
+                        __stcs(reinterpret_cast<uint4 *>(dst + (outc ^ P.xout[x])),
+                               make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]));
+            } else {
+#pragma unroll
+                for (int x = 0; x < 8; x += 2) {
+                    if (!((keep >> x) & 1u)) continue;
+                    const uint4 A = make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]);
+                    const uint4 B = make_uint4(W[4 * x + 4], W[4 * x + 5], W[4 * x + 6], W[4 * x + 7]);
+                    uint8_t *const o = dst + (outc ^ P.xout[x]);
+                    if (P.s_both) {
+                        __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, 0u));
+                        __stcs(reinterpret_cast<uint4 *>(o + P.s_w), gather_one_select(A, B, P.s_bit, 1u));
+                    } else {
+                        __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, P.s_tgt));
+                    }
+                }
+            }
+        }
+        st = st == FS_STAGES - 1 ? 0 : st + 1;
+        if (s + 1 < s1) advance(s, dummy, ob);
+    }
+    cp_async_wait_group<0>();
+}
 
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P);
 int set_dense_attrs();
