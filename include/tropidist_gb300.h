@@ -52,7 +52,8 @@ int tg_dense_plan_info(void *plan, int64_t *info, int ninfo);
 /* info: peak_bits, segments, fused passes, shared-memory sweeps, final buffer (0 a / 1 b),
  *       update ops, pass bytes, sweep bytes */
 /* per segment 8 int64: kind (0 sweep, 1 fused tile pass, 2 one-op pass, 3 coset-streaming pass),
- * width in, width out, ops done, tile bits, updates, register groups, store mode */
+ * width in, width out, ops done, tile bits, updates, register groups (kind 3: residual updates,
+ * + 16 when coset members are word-permuted), store mode */
 int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg);
 void tg_dense_plan_free(void *plan);
 int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, void *stream);

@@ -468,24 +468,114 @@ static void build_groups(PassParams &pp, uint32_t selmask) {
     pp.use_groups = 1;
 }
 
-// The coset-streaming form of a one-group uint8 pass (u8_stream_range): the thread -> coset map,
-// the input / output offsets of the coset members and of the coset-number bits, and the store
-// form.  local: tile rows (local bit -> row), out: output order, d_in: local bits read from the input.
+// The coset-streaming form of a one-group uint8 pass (u8_stream_range): the canonical coset basis
+// (the chunk parts of the first independent updates, then extension vectors), the entry
+// permutations that make those updates plain member pairings, the residual codes of the other
+// updates, the thread -> coset map, the input / output offsets and the store form.  local: tile
+// rows (local bit -> row), out: output order, d_in: local bits read from the input.
 static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in, const std::vector<int> &out,
                          const std::vector<int> &sel_rows, const std::vector<int> &sel_tg, int w_in, int w_out) {
     const int CB = 4, nb = pp.d - CB;
     pp.stream = 0;
     if (!pp.use_groups || pp.ngroups != 1 || nb < 3 || w_in > 32 || w_out > 32) return;
-    const GroupDesc &G = pp.groups[0];
-    const uint32_t bas[3] = {G.xoff[1], G.xoff[2], G.xoff[4]};
-    uint32_t piv = 0, supp = 0;
-    for (int q = 0; q < 3; q++) {
-        piv |= 1u << (31 - __builtin_clz(bas[q]));
-        supp |= bas[q];
-    }
     if (pp.store_mode == 0) pp.s_mode = 0;
-    else if (pp.store_mode == 1 && bas[0] == 1u) pp.s_mode = 1;
+    else if (pp.store_mode == 1) pp.s_mode = 1;
     else return;
+    auto reduce = [](uint32_t v, const std::vector<uint32_t> &bs) {     // bs: echelon (distinct top bits)
+        for (uint32_t b : bs)
+            if ((v ^ b) < v) v ^= b;
+        return v;
+    };
+    auto echelon = [&](const std::vector<uint32_t> &vs) {
+        std::vector<uint32_t> e;
+        for (uint32_t v : vs) {
+            v = reduce(v, e);
+            if (v) { e.push_back(v); std::sort(e.begin(), e.end(), std::greater<uint32_t>()); }
+        }
+        return e;
+    };
+    // canonical vectors: chunk parts of the first independent updates
+    std::vector<uint32_t> B, Bm;
+    std::vector<int> Bu, res;
+    for (int u = 0; u < pp.nupd; u++) {
+        const uint32_t y = pp.upd_mask[u] >> CB;
+        if (y && B.size() < 3 && reduce(y, echelon(B))) {
+            B.push_back(y);
+            Bm.push_back(pp.upd_mask[u] & 15u);
+            Bu.push_back(u);
+        } else {
+            res.push_back(u);
+        }
+    }
+    for (int u : res)
+        if (reduce(pp.upd_mask[u] >> CB, echelon(B))) return;          // more than 3 dimensions
+    int pb = -1;                        // mode 1: x bit of chunk bit 0 (the pairs of the output chunks)
+    std::vector<uint32_t> ext;
+    if (pp.s_mode == 1) {
+        for (size_t q = 0; q < B.size(); q++)
+            if (B[q] == 1u) pb = (int)q;
+        if (pb < 0) {
+            if (reduce(1u, echelon(B))) {
+                if (B.size() == 3) return;
+                ext.push_back(1u);
+            } else {
+                // chunk bit 0 is a sum of canonical vectors: it replaces one of them (whose update
+                // becomes residual)
+                for (size_t q = 0; q < B.size() && pb < 0; q++) {
+                    std::vector<uint32_t> rest;
+                    for (size_t r = 0; r < B.size(); r++) if (r != q) rest.push_back(B[r]);
+                    rest.push_back(1u);
+                    if (echelon(rest).size() == B.size()) {
+                        res.push_back(Bu[q]);
+                        B.erase(B.begin() + q); Bm.erase(Bm.begin() + q); Bu.erase(Bu.begin() + q);
+                        ext.push_back(1u);
+                        pb = 0;
+                    }
+                }
+                if (pb < 0) return;
+            }
+        }
+    }
+    const int nc = (int)B.size();
+    for (uint32_t e : ext) { B.push_back(e); Bm.push_back(0); }
+    for (int b = nb - 1; b >= 0 && B.size() < 3; b--)
+        if (reduce(1u << b, echelon(B))) { B.push_back(1u << b); Bm.push_back(0); }
+    if (B.size() != 3) return;
+    if (pp.s_mode == 1)
+        for (int q = 0; q < 3; q++) if (B[q] == 1u) pb = q;
+    std::vector<uint32_t> E = echelon(B);
+    uint32_t piv = 0, supp = 0;
+    for (uint32_t e : E) { piv |= 1u << (31 - __builtin_clz(e)); supp |= e; }
+    for (int x = 0; x < 8; x++) {
+        uint32_t o = 0, sh = 0;
+        for (int j = 0; j < 3; j++)
+            if ((x >> j) & 1) { o ^= B[j]; sh ^= Bm[j]; }
+        pp.sxoff[x] = o;
+        pp.sshift[x] = (uint8_t)sh;
+        const uint32_t sp = sh & 1u, shh = (sh >> 1) & 1u;
+        auto selu = [&](uint32_t par) { return (par + 2 * shh) | 0x40u | ((par + 2 * (1u - shh)) << 8) | 0x4000u; };
+        pp.s_selu[x][0] = selu(sp);
+        pp.s_selu[x][1] = selu(1u - sp);
+        uint32_t sel = 0;
+        for (uint32_t tb = 0; tb < 4; tb++) sel |= (4 * ((tb & 1u) ^ sp) + 2 * (((tb >> 1) & 1u) ^ shh)) << (4 * tb);
+        pp.s_selp[x] = sel;
+        pp.s_wsw[x] = (uint8_t)(sh >> 2);
+    }
+    pp.s_nc = nc;
+    pp.s_ws = 0;
+    for (int x = 0; x < 8; x++) pp.s_ws |= pp.s_wsw[x] != 0;
+    for (int q = 0; q < nc; q++) pp.s_cw[q] = pp.upd_w[Bu[q]];
+    pp.s_nres = (int)res.size();
+    for (size_t q = 0; q < res.size(); q++) {
+        const int u = res[q];
+        const uint32_t y = pp.upd_mask[u] >> CB, mlo = pp.upd_mask[u] & 15u;
+        int c = -1;
+        for (int x = 0; x < 8; x++) if (pp.sxoff[x] == y) c = x;
+        if (c < 0) return;
+        const uint32_t r = mlo ^ pp.sshift[c];
+        pp.s_rcode[q] = (uint8_t)((8u * c + 2u * (r >> 2) + (r & 1u)) | (((r >> 1) & 1u) << 6));
+        pp.s_rw[q] = pp.upd_w[u];
+    }
     std::vector<int> opos(pp.d, -1);
     for (int lb = 0; lb < pp.d; lb++) {
         const int q = index_of(out, local[lb]);
@@ -531,7 +621,7 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
     for (int x = 0; x < 8; x++) {
         uint64_t a = 0, o = 0;
         for (int b = 0; b < nb; b++)
-            if ((G.xoff[x] >> b) & 1u) { a ^= inw(b); o ^= outw(b); }
+            if ((pp.sxoff[x] >> b) & 1u) { a ^= inw(b); o ^= outw(b); }
         pp.xin[x] = (uint32_t)a;
         pp.xout[x] = (uint32_t)o;
     }
@@ -540,6 +630,7 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
         if ((pp.cfix >> b) & 1u) { fa ^= inw(b); fo ^= outw(b); }
     pp.fin = (uint32_t)fa;
     pp.fout = (uint32_t)fo;
+    pp.s_pb = pb < 0 ? 0 : pb;
     if (pp.s_mode == 1) {
         const int sb = pp.sel_low;
         const int r = local[sb];
@@ -1099,13 +1190,13 @@ static void emulate_groups(const PassParams &pp, uint8_t *T) {
     }
 }
 
-// the coset-streaming pass (u8_stream_range) on host memory: the same steps, coset map, offsets
-// and store forms, thread by thread
+// the coset-streaming pass (u8_stream_range) on host memory: the same steps, coset map, entry
+// permutations, update codes, offsets and store forms, thread by thread
 static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *dst) {
     const int g = 9 - pp.nk;
     const int ng = std::min(g, pp.n_outer);
     const uint64_t nsteps = (pp.ntiles + (1ull << g) - 1) >> g;
-    const GroupDesc &G = pp.groups[0];
+    auto reg = [](int x, uint32_t q) { return 8 * x + 2 * (int)(q >> 2) + (int)(q & 1u); };
     for (uint64_t s = 0; s < nsteps; s++) {
         for (uint32_t tid = 0; tid < FP_THREADS; tid++) {
             const uint32_t k = tid & ((1u << pp.nk) - 1u), j = tid >> pp.nk;
@@ -1118,31 +1209,40 @@ static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *ds
                 if ((j >> q) & 1u) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
             for (int q = ng; q < pp.n_outer; q++)
                 if ((s >> (q - ng)) & 1ull) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
-            uint32_t R[64];
-            uint8_t ch[16];
+            uint32_t R[64] = {0};
             for (int x = 0; x < 8; x++) {
-                const uint32_t c = c0 ^ G.xoff[x];
+                const uint32_t c = c0 ^ pp.sxoff[x];
+                uint8_t ch[16];
                 if (c & pp.expm) memset(ch, 0xFF, 16);
                 else memcpy(ch, src + ib + (inc ^ pp.xin[x]), 16);
-                emu_unpack(ch, R + 8 * x);
+                for (uint32_t q = 0; q < 16; q++)       // storage position q holds entry q ^ shift
+                    R[reg(x, q)] |= (uint32_t)ch[q ^ pp.sshift[x]] << (16 * ((q >> 1) & 1u));
             }
-            for (int u = 0; u < G.count; u++) emu_reg_update(R, pp.ucode[u], pp.uw[u]);
+            for (int u = 0; u < pp.s_nres; u++) emu_reg_update(R, pp.s_rcode[u], pp.s_rw[u]);
+            for (int u = 0; u < pp.s_nc; u++) emu_reg_update(R, 8u << u, pp.s_cw[u]);
             uint8_t W[8][16];
-            for (int x = 0; x < 8; x++) emu_pack(R + 8 * x, W[x]);
+            for (int x = 0; x < 8; x++)
+                for (uint32_t e = 0; e < 16; e++) {
+                    const uint32_t q = e ^ pp.sshift[x];
+                    W[x][e] = (uint8_t)(R[reg(x, q)] >> (16 * ((q >> 1) & 1u)));
+                }
+            const int PB = 1 << pp.s_pb;
             for (int x = 0; x < 8; x++) {
-                const uint32_t c = c0 ^ G.xoff[x];
+                const uint32_t c = c0 ^ pp.sxoff[x];
                 if ((c & pp.selm) != pp.selb) continue;
                 if (pp.s_mode == 0) {
                     memcpy(dst + ob + (outc ^ pp.xout[x]), W[x], 16);
-                } else if ((x & 1) == 0) {
+                } else if (!(x & PB)) {
                     const int sb = pp.s_bit;
+                    const bool sw = pp.sxoff[x] & 1u;
+                    const uint8_t *A = sw ? W[x | PB] : W[x], *B = sw ? W[x] : W[x | PB];
                     for (uint32_t t = 0; t < 2; t++) {
                         if (!pp.s_both && t != pp.s_tgt) continue;
                         uint8_t *o = dst + ob + (outc ^ pp.xout[x]) + (pp.s_both ? t * pp.s_w : 0);
                         for (uint32_t e = 0; e < 16; e++) {
                             const uint32_t lo = e & ((1u << sb) - 1);
                             const uint32_t se = ((e ^ lo) << 1) | lo | (t << sb);
-                            o[e] = se < 16 ? W[x][se] : W[x + 1][se - 16];
+                            o[e] = se < 16 ? A[se] : B[se - 16];
                         }
                     }
                 }
@@ -1409,7 +1509,13 @@ int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg) {
         o[3] = S.op_end;
         o[4] = S.kind == 1 ? S.pp.d : S.kind == 0 ? S.sp.max_bits : -1;
         o[5] = S.kind == 1 ? S.pp.nupd : S.kind == 0 ? S.sp.nops : (S.op_code == 1);
-        o[6] = S.kind == 1 && S.pp.use_groups ? S.pp.ngroups : 0;
+        if (S.kind == 1 && S.pp.stream) {
+            int ws = 0;
+            for (int x = 0; x < 8; x++) ws |= S.pp.s_wsw[x] != 0;
+            o[6] = S.pp.s_nres + 16 * ws;
+        } else {
+            o[6] = S.kind == 1 && S.pp.use_groups ? S.pp.ngroups : 0;
+        }
         o[7] = S.kind == 1 ? S.pp.store_mode : -1;
         k++;
     }

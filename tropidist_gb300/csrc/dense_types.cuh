@@ -145,8 +145,23 @@ struct PassParams {
     uint32_t expm;                     // chunk bits of the rows expanded in the pass (their 1-half is INF)
     uint32_t selm, selb;               // chunk bits of the selected rows in the span, and their targets
     uint32_t kin[16], kout[16];        // input / output offsets of coset-number bit j
-    uint32_t xin[8], xout[8];          // input / output offsets of the coset members xoff[x]
+    uint32_t xin[8], xout[8];          // input / output offsets of the coset members sxoff[x]
     uint32_t fin, fout;                // input / output offsets of cfix
+    // canonical form: coset member x is chunk c0 ^ sxoff[x], sxoff spanned by the chunk parts of
+    // the first (up to 3) independent updates; member x is held with its entries permuted by
+    // XOR with sshift[x] (the XOR of those updates' in-chunk masks selected by x), which turns
+    // each of those updates into a plain pairing of members x and x ^ 2^j (weights s_cw); the
+    // other updates keep a residual code (s_rcode, s_rw)
+    uint32_t sxoff[8];
+    uint32_t s_selu[8][2];             // unpack selectors (even / odd lanes) of member x
+    uint32_t s_selp[8];                // pack selector of member x
+    uint8_t s_wsw[8];                  // word-index XOR of member x (bits 2..3 of sshift[x])
+    uint8_t sshift[8];
+    int s_nc, s_nres;
+    int s_ws;                          // 1: some member is word-permuted (s_wsw)
+    int s_pb;                          // mode 1: x bit of the member pairs (chunk bit 0)
+    uint8_t s_cw[4];
+    uint8_t s_rcode[FP_MAXU], s_rw[FP_MAXU];
 };
 
 __device__ __forceinline__ uint64_t pdep_w64(uint32_t x, const uint64_t *wt, int nb) {
@@ -266,7 +281,7 @@ static __device__ void u8_tile(const PassParams &P, uint64_t tile, const uint8_t
 // (tables in shared memory), and the tile bases advance by a carry table (tile t+1 differs from
 // tile t in the bits up to the lowest zero bit of t).
 #define FP_MAXIT 8
-static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t t0, uint64_t t1,
+static __device__ __forceinline__ void u8_pass_range(const PassParams &P, uint64_t t0, uint64_t t1,
                                            const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
                                            uint4 *smem_raw) {
     constexpr int CB = 4;
@@ -356,6 +371,96 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
 
 
 // ------------------------------------------------------------------ coset-streaming pass (uint8)
+// mode-1 output chunks of a coset: the member pairs (x, x ^ PB) that differ in chunk bit 0, without
+// in-chunk bit s_bit
+template <int PB>
+static __device__ __forceinline__ void u8_stream_pairs(const PassParams &P, const uint32_t (&W)[32], uint32_t keep,
+                                                      uint8_t *dst, uint32_t outc) {
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+        if (x & PB) continue;
+        if (!((keep >> x) & 1u)) continue;
+        const uint4 M0 = make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]);
+        const uint4 M1 = make_uint4(W[4 * (x | PB)], W[4 * (x | PB) + 1], W[4 * (x | PB) + 2], W[4 * (x | PB) + 3]);
+        const bool sw = P.sxoff[x] & 1u;           // member x has chunk bit 0 set: it is the upper one
+        const uint4 A = sw ? M1 : M0, B = sw ? M0 : M1;
+        uint8_t *const o = dst + (outc ^ P.xout[x]);
+        if (P.s_both) {
+            __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, 0u));
+            __stcs(reinterpret_cast<uint4 *>(o + P.s_w), gather_one_select(A, B, P.s_bit, 1u));
+        } else {
+            __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, P.s_tgt));
+        }
+    }
+}
+
+// One coset of a streaming pass: its 8 staged chunks (INF where `inf`) into registers in the
+// canonical permuted form, the residual updates, the NC canonical updates (straight-line code:
+// member x with member x ^ 2^j), back to entry order and out to the output chunks (`keep`).
+template <int NC, bool WS, bool GEN = false>
+static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, const uint8_t *src, uint32_t inf,
+                                                      uint32_t keep, uint8_t *dst, uint32_t outc) {
+    uint32_t R[64];
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+        uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
+        if (!((inf >> x) & 1u)) v = *reinterpret_cast<const uint4 *>(src + x * 512);
+        const uint32_t se = P.s_selu[x][0], so = P.s_selu[x][1];
+        uint32_t w0 = v.x, w1 = v.y, w2 = v.z, w3 = v.w;
+        if (WS) switch (P.s_wsw[x]) {  // storage word k holds entry word k ^ wsw (uniform branch)
+            case 1: w0 = v.y; w1 = v.x; w2 = v.w; w3 = v.z; break;
+            case 2: w0 = v.z; w1 = v.w; w2 = v.x; w3 = v.y; break;
+            case 3: w0 = v.w; w1 = v.z; w2 = v.y; w3 = v.x; break;
+            default: break;
+        }
+        R[8 * x + 0] = __byte_perm(w0, 0u, se); R[8 * x + 1] = __byte_perm(w0, 0u, so);
+        R[8 * x + 2] = __byte_perm(w1, 0u, se); R[8 * x + 3] = __byte_perm(w1, 0u, so);
+        R[8 * x + 4] = __byte_perm(w2, 0u, se); R[8 * x + 5] = __byte_perm(w2, 0u, so);
+        R[8 * x + 6] = __byte_perm(w3, 0u, se); R[8 * x + 7] = __byte_perm(w3, 0u, so);
+    }
+    if constexpr (GEN) {
+        // general form (residual updates present): every update through the code switch
+        for (int u = 0; u < P.s_nc; u++) {
+            const uint32_t w = P.s_cw[u];
+            reg_dispatch(8u << u, R, w | (w << 16));
+        }
+        for (int u = 0; u < P.s_nres; u++) {
+            const uint32_t w = P.s_rw[u];
+            reg_dispatch(P.s_rcode[u], R, w | (w << 16));
+        }
+    }
+    if constexpr (!GEN && NC >= 1) { const uint32_t w = P.s_cw[0]; RegPairs<8, 0, 0>::run(R, w | (w << 16)); }
+    if constexpr (!GEN && NC >= 2) { const uint32_t w = P.s_cw[1]; RegPairs<16, 0, 0>::run(R, w | (w << 16)); }
+    if constexpr (!GEN && NC >= 3) { const uint32_t w = P.s_cw[2]; RegPairs<32, 0, 0>::run(R, w | (w << 16)); }
+    uint32_t W[32];
+#pragma unroll
+    for (int x = 0; x < 8; x++) {
+        const uint32_t sp = P.s_selp[x];
+        const uint32_t q0 = __byte_perm(R[8 * x + 0], R[8 * x + 1], sp), q1 = __byte_perm(R[8 * x + 2], R[8 * x + 3], sp);
+        const uint32_t q2 = __byte_perm(R[8 * x + 4], R[8 * x + 5], sp), q3 = __byte_perm(R[8 * x + 6], R[8 * x + 7], sp);
+        // entry word k is storage word k ^ wsw
+        switch (WS ? P.s_wsw[x] : 0) {
+            case 1: W[4 * x] = q1; W[4 * x + 1] = q0; W[4 * x + 2] = q3; W[4 * x + 3] = q2; break;
+            case 2: W[4 * x] = q2; W[4 * x + 1] = q3; W[4 * x + 2] = q0; W[4 * x + 3] = q1; break;
+            case 3: W[4 * x] = q3; W[4 * x + 1] = q2; W[4 * x + 2] = q1; W[4 * x + 3] = q0; break;
+            default: W[4 * x] = q0; W[4 * x + 1] = q1; W[4 * x + 2] = q2; W[4 * x + 3] = q3; break;
+        }
+    }
+    if (P.s_mode == 0) {
+#pragma unroll
+        for (int x = 0; x < 8; x++)
+            if ((keep >> x) & 1u)
+                __stcs(reinterpret_cast<uint4 *>(dst + (outc ^ P.xout[x])),
+                       make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]));
+    } else if (P.s_pb == 0) {
+        u8_stream_pairs<1>(P, W, keep, dst, outc);
+    } else if (P.s_pb == 1) {
+        u8_stream_pairs<2>(P, W, keep, dst, outc);
+    } else {
+        u8_stream_pairs<4>(P, W, keep, dst, outc);
+    }
+}
+
 // A one-group pass without a shared-memory tile: thread k of tile t owns the coset {c0 ^ X[x]} of
 // the tile's chunks (c0 fixed per thread for the whole launch), stages its 8 input chunks in its
 // own shared-memory slots with cp.async three tiles ahead (no barriers: a thread reads back only
@@ -364,7 +469,7 @@ static __device__ __noinline__ void u8_pass_range(const PassParams &P, uint64_t 
 #define FS_STAGES 3
 #define FS_WARP_BYTES (FS_STAGES * 8 * 512)      // staging bytes of one warp
 
-static __device__ __noinline__ void u8_stream_range(const PassParams &P, uint64_t s0, uint64_t s1,
+static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint64_t s0, uint64_t s1,
                                                    const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
                                                    uint4 *smem_raw) {
     __shared__ int64_t s_cin[FP_MAXOUTER], s_cout[FP_MAXOUTER];
@@ -386,7 +491,7 @@ static __device__ __noinline__ void u8_stream_range(const PassParams &P, uint64_
     uint32_t keep = 0, inf = 0;
 #pragma unroll
     for (int x = 0; x < 8; x++) {
-        const uint32_t c = c0 ^ P.groups[0].xoff[x];
+        const uint32_t c = c0 ^ P.sxoff[x];
         if ((c & P.selm) == P.selb) keep |= 1u << x;
         if (c & P.expm) inf |= 1u << x;
     }
@@ -413,7 +518,6 @@ static __device__ __noinline__ void u8_stream_range(const PassParams &P, uint64_
         const int q = __ffsll((long long)~s) - 1 + ng;
         if (q < P.n_outer) { bi += s_cin[q]; bo += s_cout[q]; }
     };
-    const int nu = P.groups[0].count;
     uint64_t ibn = ib, dummy = 0;
     // prologue: steps s0 and s0 + 1 in flight
     issue(s0, ibn, 0);
@@ -434,44 +538,16 @@ static __device__ __noinline__ void u8_stream_range(const PassParams &P, uint64_
         cp_async_wait_group<2>();
         if (((s << g) | j) < ntiles) {
             const uint8_t *src = stage0 + st * 4096;
-            uint32_t R[64];
-#pragma unroll
-            for (int x = 0; x < 8; x++) {
-                uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
-                if (!((inf >> x) & 1u)) v = *reinterpret_cast<const uint4 *>(src + x * 512);
-                unpack_eo(v.x, R[8 * x + 0], R[8 * x + 1]);
-                unpack_eo(v.y, R[8 * x + 2], R[8 * x + 3]);
-                unpack_eo(v.z, R[8 * x + 4], R[8 * x + 5]);
-                unpack_eo(v.w, R[8 * x + 6], R[8 * x + 7]);
-            }
-            for (int u = 0; u < nu; u++) {
-                const uint32_t w = P.uw[u];
-                reg_dispatch(P.ucode[u], R, w | (w << 16));
-            }
-            uint32_t W[32];
-#pragma unroll
-            for (int q = 0; q < 32; q++) W[q] = pack_eo(R[2 * q], R[2 * q + 1]);
-            uint8_t *const dst = out + ob;
-            if (P.s_mode == 0) {
-#pragma unroll
-                for (int x = 0; x < 8; x++)
-                    if ((keep >> x) & 1u)
-                        __stcs(reinterpret_cast<uint4 *>(dst + (outc ^ P.xout[x])),
-                               make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]));
-            } else {
-#pragma unroll
-                for (int x = 0; x < 8; x += 2) {
-                    if (!((keep >> x) & 1u)) continue;
-                    const uint4 A = make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]);
-                    const uint4 B = make_uint4(W[4 * x + 4], W[4 * x + 5], W[4 * x + 6], W[4 * x + 7]);
-                    uint8_t *const o = dst + (outc ^ P.xout[x]);
-                    if (P.s_both) {
-                        __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, 0u));
-                        __stcs(reinterpret_cast<uint4 *>(o + P.s_w), gather_one_select(A, B, P.s_bit, 1u));
-                    } else {
-                        __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, P.s_tgt));
-                    }
-                }
+            if (P.s_nres) u8_stream_coset<0, true, true>(P, src, inf, keep, out + ob, outc);
+            else switch (P.s_nc + 4 * P.s_ws) {
+                case 0: u8_stream_coset<0, false>(P, src, inf, keep, out + ob, outc); break;
+                case 1: u8_stream_coset<1, false>(P, src, inf, keep, out + ob, outc); break;
+                case 2: u8_stream_coset<2, false>(P, src, inf, keep, out + ob, outc); break;
+                case 3: u8_stream_coset<3, false>(P, src, inf, keep, out + ob, outc); break;
+                case 4: u8_stream_coset<0, true>(P, src, inf, keep, out + ob, outc); break;
+                case 5: u8_stream_coset<1, true>(P, src, inf, keep, out + ob, outc); break;
+                case 6: u8_stream_coset<2, true>(P, src, inf, keep, out + ob, outc); break;
+                default: u8_stream_coset<3, true>(P, src, inf, keep, out + ob, outc); break;
             }
         }
         st = st == FS_STAGES - 1 ? 0 : st + 1;
