@@ -139,6 +139,8 @@ void tg_batch_free(void *batch);
 void *tg_server_create(void *arena, uint64_t arena_bytes, int jcap, int64_t prm_bytes, int plan_cap, int blocks,
                        int *status);
 int tg_server_submit(void *server, const int64_t *ops, int64_t nops);
+/* the same for a plan scheduled ahead of time by tg_dense_plan (uint8); the handle stays the caller's */
+int tg_server_submit_plan(void *server, void *plan);
 int tg_server_poll(void *server, int *slots, uint32_t *values, int max);
 int tg_server_stop(void *server);
 void tg_server_free(void *server);

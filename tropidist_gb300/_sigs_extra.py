@@ -23,6 +23,7 @@ SIGNATURES = {
     "tg_batch_free": (None, [vp]),
     "tg_server_create": (vp, [vp, u64, ci, i64, ci, ci, c.POINTER(ci)]),
     "tg_server_submit": (ci, [vp, vp, i64]),
+    "tg_server_submit_plan": (ci, [vp, vp]),
     "tg_server_poll": (ci, [vp, vp, vp, ci]),
     "tg_server_stop": (ci, [vp]),
     "tg_server_free": (None, [vp]),

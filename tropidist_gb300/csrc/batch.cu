@@ -121,8 +121,10 @@ __device__ void run_unit(const BJob &J, unsigned unit, uint8_t *arena, const uin
         } else {
             const PassParams &P = *reinterpret_cast<const PassParams *>(PRM);
             const uint64_t t0 = (uint64_t)unit * J.grain;
-            const uint64_t t1 = t0 + J.grain < P.ntiles ? t0 + J.grain : P.ntiles;
-            if (P.use_groups) u8_pass_range(P, t0, t1, src, dst, TC);
+            const uint64_t nt = P.stream ? (P.ntiles + (1ull << (9 - P.nk)) - 1) >> (9 - P.nk) : P.ntiles;
+            const uint64_t t1 = t0 + J.grain < nt ? t0 + J.grain : nt;
+            if (P.stream) u8_stream_range(P, t0, t1, src, dst, TC);     // a unit: a range of steps
+            else if (P.use_groups) u8_pass_range(P, t0, t1, src, dst, TC);
             else
                 for (uint64_t t = t0; t < t1; t++) {
                     u8_tile<BT_THREADS>(P, t, src, dst, TC);
@@ -209,6 +211,15 @@ struct BatchPlan {
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// work items of a fused pass: tiles, or steps of 512 >> nk tiles in the streaming form
+static uint64_t pass_units(const PassParams &pp) {
+    return pp.stream ? (pp.ntiles + (1ull << (9 - pp.nk)) - 1) >> (9 - pp.nk) : pp.ntiles;
+}
+// items per unit: at least 16, about one unit per SM for a lone plan
+static uint32_t pass_grain(uint64_t nt) {
+    return (uint32_t)std::min<uint64_t>(nt, std::max<uint64_t>(16, (nt + sm_count() - 1) / sm_count()));
+}
 
 static_assert(sizeof(SweepParams) <= 4096 && sizeof(PassParams) <= 4096, "job parameters exceed their 4 KB copy");
 static_assert(sizeof(BJob) % 16 == 0, "job descriptors are read as 16-byte words");
@@ -403,9 +414,6 @@ static int server_launch(Server &S) {
     return cuda_check(cudaGetLastError(), "server launch");
 }
 
-static uint32_t pass_grain(uint64_t nt) {
-    return (uint32_t)std::min<uint64_t>(nt, std::max<uint64_t>(16, (nt + sm_count() - 1) / sm_count()));
-}
 
 }  // namespace tg
 
@@ -459,9 +467,9 @@ void *tg_batch_create(int nplans, const int64_t *ops, const int64_t *offsets, in
                     memcpy(B->params.data() + J.params_off, &S.sp, sizeof(SweepParams));
                 } else if (S.kind == 1) {
                     J.kind = 1;
-                    const uint64_t nt = S.pp.ntiles;
                     // large units amortise the per-unit overhead; concurrency comes from the other plans
-                    J.grain = (uint32_t)std::min<uint64_t>(nt, std::max<uint64_t>(16, (nt + sm_count() - 1) / sm_count()));
+                    const uint64_t nt = pass_units(S.pp);
+                    J.grain = pass_grain(nt);
                     J.nunits = (uint32_t)((nt + J.grain - 1) / J.grain);
                     J.params_off = align_up(B->params.size(), 16);
                     B->params.resize(J.params_off + sizeof(PassParams));
@@ -690,13 +698,31 @@ void *tg_server_create(void *arena, uint64_t arena_bytes, int jcap, int64_t prm_
 // Admits one plan (op stream of nops rows (code, a, b), uint8 tables).  Returns its slot, or
 // TG_ERR_NOMEM when the arena, the pools or the plan slots have no room now (collect finished
 // plans with tg_server_poll and retry), or another negative status.
+static int server_submit(Server &S, const DensePlan &P);
+
 int tg_server_submit(void *p, const int64_t *ops, int64_t nops) {
     if (!p || (!ops && nops)) return set_error(TG_ERR_ARG, "null argument");
     Server &S = *static_cast<Server *>(p);
     if (S.free_slots.empty()) return TG_ERR_NOMEM;
     DensePlan P;
-    int st = build_dense_plan(ops, nops, 1, nullptr, 0, P);
+    const int st = build_dense_plan(ops, nops, 1, nullptr, 0, P);
     if (st) return st;
+    return server_submit(S, P);
+}
+
+// Admits a plan scheduled ahead of time by tg_dense_plan (uint8 entries); same returns as
+// tg_server_submit.  The plan handle stays the caller's.
+int tg_server_submit_plan(void *p, void *plan) {
+    if (!p || !plan) return set_error(TG_ERR_ARG, "null argument");
+    Server &S = *static_cast<Server *>(p);
+    const DensePlan &P = *static_cast<const DensePlan *>(plan);
+    if (P.eb != 1) return set_error(TG_ERR_ARG, "served plans have uint8 entries");
+    if (S.free_slots.empty()) return TG_ERR_NOMEM;
+    return server_submit(S, P);
+}
+
+static int server_submit(Server &S, const DensePlan &P) {
+    int st = TG_OK;
     for (const Seg &G : P.segs)
         if ((G.kind == 0 && G.sp.max_bits > 15) || (G.kind == 1 && G.pp.d > 16))
             return set_error(TG_ERR_TOO_BIG, "served plans need sweeps of <= 15 bits and tiles of <= 16 bits");
@@ -753,8 +779,9 @@ int tg_server_submit(void *p, const int64_t *ops, int64_t nops) {
             poff += sizeof(SweepParams);
         } else if (G.kind == 1) {
             J.kind = 1;
-            J.grain = pass_grain(G.pp.ntiles);
-            J.nunits = (uint32_t)((G.pp.ntiles + J.grain - 1) / J.grain);
+            const uint64_t nt = pass_units(G.pp);
+            J.grain = pass_grain(nt);
+            J.nunits = (uint32_t)((nt + J.grain - 1) / J.grain);
             poff = align_up(poff, 16);
             memcpy(prm.data() + poff, &G.pp, sizeof(PassParams));
             J.params_off = R.prm_off + poff;

@@ -262,11 +262,16 @@ class PersistentServer:
     def _admit(self, req):
         """Submit every feasible plan of the request; False (nothing submitted) if there is no room."""
         from . import _lib
-        encs = [(k, pl.encode()) for k, pl in enumerate(req.plans) if pl.feasible]
         slots = []
-        for k, enc in encs:
-            enc = np.ascontiguousarray(enc)
-            r = self.L.tg_server_submit(self.handle, enc.ctypes.data, len(enc))
+        for k, pl in enumerate(req.plans):
+            if not pl.feasible:
+                continue
+            cp = req.cps[k] if req.cps is not None else None
+            if cp is not None:
+                r = self.L.tg_server_submit_plan(self.handle, cp.handle)
+            else:
+                enc = np.ascontiguousarray(pl.encode())
+                r = self.L.tg_server_submit(self.handle, enc.ctypes.data, len(enc))
             if r == -3 and not slots and not self.owner:
                 _lib.check(r)               # does not fit even in an empty server
             if r == -3:
@@ -344,6 +349,7 @@ class _Sub:
 
     def __init__(self, req, todo):
         self.plans = [req.plans[k] for k in todo]
+        self.cps = [req.cps[k] for k in todo] if req.cps is not None else None
 
 
 def serve_persistent(reqs, arrivals, **kw):
