@@ -262,11 +262,16 @@ def main():
     acc = [0.0] * 12
     e0.record(st)
     for _ in range(args.steps):
-        step(acc)
+        step()
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    # per-launch breakdown (an event pair around every launch), outside the timed region: the same
+    # steps again; events between launches serialise them, so these launch times are conservative
+    for _ in range(args.steps):
+        step(acc)
+    torch.cuda.synchronize()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -312,8 +317,9 @@ def main():
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_launch": bytes_fp / n_fp if n_fp else None,
                 "avg_launch_us": 1e3 * ms_fp / n_fp if n_fp else None, "launches": int(n_fp),
-                "share_of_gpu_time": ms_fp / ms if ms else None,
+                "share_of_gpu_time": ms_fp / sum(acc[1::3]) if sum(acc[1::3]) else None,
                 "traffic": (tr["ratio"] * bytes_fp / n_fp) if (tr and n_fp) else None,
+                "whole_step_gbs": (sum(acc[2::3]) / args.steps) / (ms / args.steps / 1e3) / 1e9 if ms else None,
                 "traffic_source": ("ncu DRAM bytes / algorithmic bytes = %.3f on %s, scaled to the average launch"
                                    % (tr["ratio"], tr["source"])) if tr else None}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

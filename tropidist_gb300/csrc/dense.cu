@@ -265,6 +265,9 @@ __global__ void __launch_bounds__(FP_THREADS, 1) k_stream_pass_u8(const __grid_c
                                                                  const uint8_t *__restrict__ in,
                                                                  uint8_t *__restrict__ out) {
     extern __shared__ uint4 smem_raw[];
+    // the next pass may be scheduled on an SM as soon as this block leaves it (it waits for the
+    // whole grid before touching memory)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const uint64_t nsteps = (P.ntiles + (1ull << (9 - P.nk)) - 1) >> (9 - P.nk);
     const uint64_t per = nsteps / gridDim.x, rem = nsteps % gridDim.x;
     const uint64_t s0 = blockIdx.x * per + ((uint64_t)blockIdx.x < rem ? (uint64_t)blockIdx.x : rem);
@@ -1105,8 +1108,21 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
             if (sizeof(E) == 1 && S.pp.stream) {
                 const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nk)) - 1) >> (9 - S.pp.nk);
                 const uint64_t grid = std::min<uint64_t>(nsteps, (uint64_t)sm_count());
-                k_stream_pass_u8<<<(unsigned)grid, FP_THREADS, 16 * FS_WARP_BYTES, st>>>(S.pp, (const uint8_t *)src,
-                                                                                    (uint8_t *)dst);
+                // programmatic dependent launch: this pass's blocks start (and run their prologue)
+                // while the previous pass drains
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3((unsigned)grid);
+                cfg.blockDim = dim3(FP_THREADS);
+                cfg.dynamicSmemBytes = 16 * FS_WARP_BYTES;
+                cfg.stream = st;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+                attr[0].val.programmaticStreamSerializationAllowed = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                e = cuda_check(cudaLaunchKernelEx(&cfg, k_stream_pass_u8, S.pp, (const uint8_t *)src, (uint8_t *)dst),
+                               "stream pass launch");
+                if (e) return e;
             } else if (sizeof(E) == 1 && S.pp.use_groups) {
                 // persistent: one CTA per SM, three tile buffers
                 uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());

@@ -503,6 +503,9 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
         if ((s0 >> (q - ng)) & 1ull) { ib += P.outer_in[q]; ob += P.outer_out[q]; }
     const uint64_t ntiles = P.ntiles;
     __syncthreads();
+    // programmatic dependent launch: everything above overlapped the previous pass; its writes (our
+    // input) and reads (our output buffer) are complete past this point
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     uint8_t *const stage0 = reinterpret_cast<uint8_t *>(smem_raw) + (size_t)warp * FS_WARP_BYTES + lane * 16u;
     auto issue = [&](uint64_t s, uint64_t b, int st) {
