@@ -53,7 +53,8 @@ int tg_dense_plan_info(void *plan, int64_t *info, int ninfo);
  *       update ops, pass bytes, sweep bytes */
 /* per segment 8 int64: kind (0 sweep, 1 fused tile pass, 2 one-op pass, 3 coset-streaming pass),
  * width in, width out, ops done, tile bits, updates, register groups (kind 3: residual updates,
- * + 16 when coset members are word-permuted), store mode */
+ * + 16 when coset members are word-permuted, + 32 with a lane dimension, + 64 when its update has
+ * an in-chunk part), store mode */
 int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg);
 void tg_dense_plan_free(void *plan);
 int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, void *stream);
@@ -67,6 +68,9 @@ int tg_dense_segment_ms(void *plan, float *out, int64_t maxseg);
 int tg_dense_run(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
                  uint32_t *value, void *stream);
 int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16);
+/* coset-streaming passes: update span (3, or 4 with a lane-pair dimension) and the span of passes
+ * in which an in-chunk row closes (<= span, 2 or 3); default 3, 2 */
+int tg_dense_set_stream_span(int span, int span_sel);
 
 /* Allocation-free whole-plan run (uint8 tables).  No counterpart in the reference: its C kernels
  * never allocate, because numpy owns the one table buffer (cdist/kernel.py:101-103), whereas the

@@ -30,7 +30,9 @@ TUNINGS = [(16, 15, 15, 14), (12, 11, 10, 9), (8, 7, 6, 5), (6, 5, 4, 3)]
 def default_tuning():
     from tropidist_gb300 import _lib
     _lib.lib().tg_dense_set_tuning(*TUNINGS[0])
+    _lib.lib().tg_dense_set_stream_span(3, 2)
     yield
+    _lib.lib().tg_dense_set_stream_span(3, 2)
 
 
 def gpu_tables(plan, ks, dtype="u8"):
@@ -70,6 +72,28 @@ def test_checkpoint_tables_bit_identical(tune):
         assert v == case["value_c"]
         for k, t in zip(ks, tabs):
             assert sha(t) == case["table_sha"][str(k)], (tune, k)
+
+
+@pytest.mark.parametrize("span", [(3, 3), (4, 3)])
+@pytest.mark.parametrize("prob", [(120, 240, 24, 3), (160, 320, 26, 1)])
+def test_lane_dimension_tables_bit_identical(prob, span):
+    """Streaming passes whose updates span a fourth dimension across a lane pair (with and without
+    an in-chunk part), and passes closing an in-chunk row with 3 dimensions: checkpoint tables and
+    the value against the oracle."""
+    from tropidist_gb300 import _lib, kernel, synth, trellis
+    from oracle import dense as od
+    _lib.lib().tg_dense_set_stream_span(*span)
+    m, n, win, seed = prob
+    p = synth.banded(m, n, win, seed=seed)
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    ks = list(range(len(plan.ops) // 5, len(plan.ops), len(plan.ops) // 5))
+    flags = [int(s[6]) for s in kernel.CompiledPlan(plan, "u8", ks).segments() if s[0] == 3]
+    if span[0] == 4:
+        assert sum(1 for f in flags if f & 32) > 0 and sum(1 for f in flags if f & 64) > 0
+    v, tabs = gpu_tables(plan, ks)
+    assert v == od.run_plan_numpy(plan)
+    for k, t in zip(ks, tabs):
+        assert np.array_equal(t, od.table_after(plan, k)), (prob, span, k)
 
 
 def test_synth_checkpoints_and_values():

@@ -17,6 +17,42 @@ TUNINGS = [(16, 15, 15, 14), (12, 11, 10, 9), (8, 7, 6, 5), (6, 5, 4, 3)]
 def restore_tuning(lib):
     yield
     lib.tg_dense_set_tuning(*TUNINGS[0])
+    lib.tg_dense_set_stream_span(3, 2)
+
+
+@pytest.mark.parametrize("span", [(3, 3), (4, 3), (4, 2)])
+def test_lane_dimension_schedules(lib, span):
+    """Streaming passes with a lane-pair dimension: emulated schedules against the oracle's tables."""
+    lib.tg_dense_set_stream_span(*span)
+    rng = random.Random(5)
+    for tune in TUNINGS[:3]:
+        lib.tg_dense_set_tuning(*tune)
+        for _ in range(30):
+            m = rng.randint(8, 15)
+            n = rng.randint(m + 3, m + 14)
+            h = [rng.randrange(1, 1 << m) for _ in range(n)]
+            l = [rng.randrange(0, 2) for _ in range(n)]
+            plan = trellis.build_plan(h, l, 1, list(range(n)), m)
+            if not plan.feasible:
+                continue
+            assert emulate(plan)[0] == od.run_plan_numpy(plan)
+        for case in golden("dense_synth.json"):
+            h, l = unhex(case["h"]), unhex(case["l"])
+            plan = trellis.build_plan(h, l, 1, list(range(len(h))), case["nrows"])
+            ks = [int(k) for k in case["table_sha"]]
+            v, tabs, info = emulate(plan, checkpoints=ks)
+            assert v == case["value"]
+            for k, t in zip(ks, tabs):
+                assert sha(t) == case["table_sha"][str(k)]
+    # a wider banded plan: lane passes with and without an in-chunk part
+    lib.tg_dense_set_tuning(*TUNINGS[0])
+    p = synth.banded(120, 240, 24, seed=3)
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    ks = list(range(len(plan.ops) // 4, len(plan.ops), len(plan.ops) // 4))
+    v, tabs, info = emulate(plan, checkpoints=ks)
+    assert v == od.run_plan_numpy(plan)
+    for k, t in zip(ks, tabs):
+        assert np.array_equal(t, od.table_after(plan, k))
 
 
 def test_random_plans_all_tunings(lib):
@@ -61,6 +97,15 @@ def test_synth_checkpoints(lib):
             assert v == case["value"]
             for k, t in zip(ks, tabs):
                 assert sha(t) == case["table_sha"][str(k)]
+    # a wider banded plan: lane passes with and without an in-chunk part
+    lib.tg_dense_set_tuning(*TUNINGS[0])
+    p = synth.banded(120, 240, 24, seed=3)
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    ks = list(range(len(plan.ops) // 4, len(plan.ops), len(plan.ops) // 4))
+    v, tabs, info = emulate(plan, checkpoints=ks)
+    assert v == od.run_plan_numpy(plan)
+    for k, t in zip(ks, tabs):
+        assert np.array_equal(t, od.table_after(plan, k))
 
 
 def test_weighted_and_wide_masks(lib):

@@ -100,6 +100,7 @@ def _declare(L):
         "tg_dense_run_noalloc": (ci, [vp, i64, vp, u64, c.POINTER(c.c_uint32), vp]),
         "tg_dense_run": (ci, [vp, i64, ci, vp, vp, c.POINTER(c.c_uint32), vp]),
         "tg_dense_set_tuning": (ci, [ci, ci, ci, ci]),
+        "tg_dense_set_stream_span": (ci, [ci, ci]),
         "tg_debug_emulate_dense": (ci, [vp, vp, vp, vp]),
     }
     from . import _sigs_extra

@@ -121,7 +121,7 @@ __device__ void run_unit(const BJob &J, unsigned unit, uint8_t *arena, const uin
         } else {
             const PassParams &P = *reinterpret_cast<const PassParams *>(PRM);
             const uint64_t t0 = (uint64_t)unit * J.grain;
-            const uint64_t nt = P.stream ? (P.ntiles + (1ull << (9 - P.nk)) - 1) >> (9 - P.nk) : P.ntiles;
+            const uint64_t nt = P.stream ? (P.ntiles + (1ull << (9 - P.nkt)) - 1) >> (9 - P.nkt) : P.ntiles;
             const uint64_t t1 = t0 + J.grain < nt ? t0 + J.grain : nt;
             if (P.stream) u8_stream_range(P, t0, t1, src, dst, TC);     // a unit: a range of steps
             else if (P.use_groups) u8_pass_range(P, t0, t1, src, dst, TC);
@@ -214,7 +214,7 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // work items of a fused pass: tiles, or steps of 512 >> nk tiles in the streaming form
 static uint64_t pass_units(const PassParams &pp) {
-    return pp.stream ? (pp.ntiles + (1ull << (9 - pp.nk)) - 1) >> (9 - pp.nk) : pp.ntiles;
+    return pp.stream ? (pp.ntiles + (1ull << (9 - pp.nkt)) - 1) >> (9 - pp.nkt) : pp.ntiles;
 }
 // items per unit: at least 16, about one unit per SM for a lone plan
 static uint32_t pass_grain(uint64_t nt) {

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(FP_THREADS, 1) k_stream_pass_u8(const __grid_c
     // the next pass may be scheduled on an SM as soon as this block leaves it (it waits for the
     // whole grid before touching memory)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    const uint64_t nsteps = (P.ntiles + (1ull << (9 - P.nk)) - 1) >> (9 - P.nk);
+    const uint64_t nsteps = (P.ntiles + (1ull << (9 - P.nkt)) - 1) >> (9 - P.nkt);
     const uint64_t per = nsteps / gridDim.x, rem = nsteps % gridDim.x;
     const uint64_t s0 = blockIdx.x * per + ((uint64_t)blockIdx.x < rem ? (uint64_t)blockIdx.x : rem);
     const uint64_t s1 = s0 + per + (blockIdx.x < rem ? 1 : 0);
@@ -345,6 +345,8 @@ static int g_dmax8 = 16, g_dmax16 = 15;          // fused tile bits
 static int g_sweep_bits8 = 15, g_sweep_bits16 = 14; // shared-memory sweep capacity (bits)
 static bool g_relayout = true;                       // uint8 layout planning between passes
 static bool g_cosets = true;                         // coset-streaming form of one-group uint8 passes
+static int g_span = 3, g_span_sel = 2;               // streaming passes: update span (4: lane dimension),
+                                                     // span when an in-chunk row closes in the pass
 
 // Groups of the pass's updates whose chunk masks (mask >> 4) span <= 3 dimensions, every update
 // in a group (the in-chunk part of a mask is free in the register form; see fused_u8.cuh).  Also
@@ -480,7 +482,7 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
                          const std::vector<int> &sel_rows, const std::vector<int> &sel_tg, int w_in, int w_out) {
     const int CB = 4, nb = pp.d - CB;
     pp.stream = 0;
-    if (!pp.use_groups || pp.ngroups != 1 || nb < 3 || w_in > 32 || w_out > 32) return;
+    if (!pp.use_groups || nb < 3 || w_in > 32 || w_out > 32) return;
     if (pp.store_mode == 0) pp.s_mode = 0;
     else if (pp.store_mode == 1) pp.s_mode = 1;
     else return;
@@ -502,7 +504,7 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
     std::vector<int> Bu, res;
     for (int u = 0; u < pp.nupd; u++) {
         const uint32_t y = pp.upd_mask[u] >> CB;
-        if (y && B.size() < 3 && reduce(y, echelon(B))) {
+        if (y && B.size() < 4 && reduce(y, echelon(B))) {
             B.push_back(y);
             Bm.push_back(pp.upd_mask[u] & 15u);
             Bu.push_back(u);
@@ -511,7 +513,25 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
         }
     }
     for (int u : res)
-        if (reduce(pp.upd_mask[u] >> CB, echelon(B))) return;          // more than 3 dimensions
+        if (reduce(pp.upd_mask[u] >> CB, echelon(B))) return;          // more than 4 dimensions
+    // a fourth dimension goes to the lane pair: a vector other than chunk bit 0, preferably one
+    // whose update has no in-chunk part (the straight-line lane update)
+    pp.s_lane = 0;
+    pp.s_lgen = 0;
+    uint32_t LV = 0, LM = 0;
+    const bool need_e0 = pp.s_mode == 1 && B.size() == 3 && reduce(1u, echelon(B)) != 0;
+    if (B.size() == 4 || need_e0) {
+        int jl = -1;
+        for (int q = 0; q < 4 && jl < 0; q++) if (B[q] != 1u && Bm[q] == 0) jl = q;
+        for (int q = 0; q < 4 && jl < 0; q++) if (B[q] != 1u) jl = q;
+        LV = B[jl];
+        LM = Bm[jl];
+        pp.s_lw = pp.upd_w[Bu[jl]];
+        B.erase(B.begin() + jl); Bm.erase(Bm.begin() + jl); Bu.erase(Bu.begin() + jl);
+        pp.s_lane = 1;
+        pp.s_lgen = LM != 0;
+        pp.s_lcode = (uint8_t)((2u * (LM >> 2) + (LM & 1u)) | (((LM >> 1) & 1u) << 6));
+    }
     int pb = -1;                        // mode 1: x bit of chunk bit 0 (the pairs of the output chunks)
     std::vector<uint32_t> ext;
     if (pp.s_mode == 1) {
@@ -541,12 +561,18 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
     }
     const int nc = (int)B.size();
     for (uint32_t e : ext) { B.push_back(e); Bm.push_back(0); }
-    for (int b = nb - 1; b >= 0 && B.size() < 3; b--)
-        if (reduce(1u << b, echelon(B))) { B.push_back(1u << b); Bm.push_back(0); }
+    for (int b = nb - 1; b >= 0 && B.size() < 3; b--) {
+        std::vector<uint32_t> cur = B;
+        if (pp.s_lane) cur.push_back(LV);
+        if (reduce(1u << b, echelon(cur))) { B.push_back(1u << b); Bm.push_back(0); }
+    }
     if (B.size() != 3) return;
     if (pp.s_mode == 1)
         for (int q = 0; q < 3; q++) if (B[q] == 1u) pb = q;
-    std::vector<uint32_t> E = echelon(B);
+    std::vector<uint32_t> BL = B;
+    if (pp.s_lane) BL.push_back(LV);
+    std::vector<uint32_t> E = echelon(BL);
+    if (E.size() != BL.size()) return;
     uint32_t piv = 0, supp = 0;
     for (uint32_t e : E) { piv |= 1u << (31 - __builtin_clz(e)); supp |= e; }
     for (int x = 0; x < 8; x++) {
@@ -574,7 +600,7 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
         const uint32_t y = pp.upd_mask[u] >> CB, mlo = pp.upd_mask[u] & 15u;
         int c = -1;
         for (int x = 0; x < 8; x++) if (pp.sxoff[x] == y) c = x;
-        if (c < 0) return;
+        if (c < 0) return;                 // a residual along the lane dimension: not this form
         const uint32_t r = mlo ^ pp.sshift[c];
         pp.s_rcode[q] = (uint8_t)((8u * c + 2u * (r >> 2) + (r & 1u)) | (((r >> 1) & 1u) << 6));
         pp.s_rw[q] = pp.upd_w[u];
@@ -614,8 +640,9 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
         const uint64_t wa = inw(a) ? inw(a) : ~0ull, wb = inw(b) ? inw(b) : ~0ull;
         return wa < wb;
     });
-    if (kp.size() > 9) return;
+    if ((int)kp.size() + pp.s_lane > 9 || (pp.s_lane && kp.size() < 4)) return;
     pp.nk = (int)kp.size();
+    pp.nkt = pp.nk + pp.s_lane;
     for (int q = 0; q < pp.nk; q++) {
         pp.kpos[q] = (uint8_t)kp[q];
         pp.kin[q] = (uint32_t)inw(kp[q]);
@@ -633,6 +660,12 @@ static void build_stream(PassParams &pp, const std::vector<int> &local, int d_in
         if ((pp.cfix >> b) & 1u) { fa ^= inw(b); fo ^= outw(b); }
     pp.fin = (uint32_t)fa;
     pp.fout = (uint32_t)fo;
+    pp.s_lvec = LV;
+    uint64_t la = 0, lo = 0;
+    for (int b = 0; b < nb; b++)
+        if ((LV >> b) & 1u) { la ^= inw(b); lo ^= outw(b); }
+    pp.s_lin = (uint32_t)la;
+    pp.s_lout = (uint32_t)lo;
     pp.s_pb = pb < 0 ? 0 : pb;
     if (pp.s_mode == 1) {
         const int sb = pp.sel_low;
@@ -935,8 +968,9 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             int nupd = 0;
             int64_t j = i;
             // coset-streaming passes (uint8): the updates' masks outside the in-chunk rows span at most
-            // 3 dimensions (one register group), at most one in-chunk row closes, and then at most 2
-            // (the row entering the in-chunk positions joins the coset)
+            // g_span dimensions (3 in a thread's registers, a 4th across a lane pair), at most one
+            // in-chunk row closes, and then at most g_span_sel (the row entering the in-chunk
+            // positions joins the coset, in the registers)
             const bool srule = eb == 1 && g_cosets && relayout;
             std::vector<int> srows;                     // row -> bit of the span vectors
             std::vector<uint64_t> sbasis;
@@ -983,7 +1017,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                     } else if (o.code == 2 && has_row(inchunk, RI.sel_row[j])) {
                         ns2++;
                     }
-                    if (ns2 > 1 || (int)b2.size() > (ns2 ? 2 : 3)) break;
+                    if (ns2 > 1 || (int)b2.size() > (ns2 ? g_span_sel : g_span)) break;
                     sbasis.swap(b2);
                     nsel_in = ns2;
                 }
@@ -1106,7 +1140,7 @@ static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStr
         } else {
             size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
             if (sizeof(E) == 1 && S.pp.stream) {
-                const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nk)) - 1) >> (9 - S.pp.nk);
+                const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nkt)) - 1) >> (9 - S.pp.nkt);
                 const uint64_t grid = std::min<uint64_t>(nsteps, (uint64_t)sm_count());
                 // programmatic dependent launch: this pass's blocks start (and run their prologue)
                 // while the previous pass drains
@@ -1209,23 +1243,38 @@ static void emulate_groups(const PassParams &pp, uint8_t *T) {
 // the coset-streaming pass (u8_stream_range) on host memory: the same steps, coset map, entry
 // permutations, update codes, offsets and store forms, thread by thread
 static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *dst) {
-    const int g = 9 - pp.nk;
+    const int g = 9 - pp.nkt;
     const int ng = std::min(g, pp.n_outer);
     const uint64_t nsteps = (pp.ntiles + (1ull << g) - 1) >> g;
     auto reg = [](int x, uint32_t q) { return 8 * x + 2 * (int)(q >> 2) + (int)(q & 1u); };
+    auto sw = [](uint32_t v) { return (v >> 16) | (v << 16); };
+    auto addmin = [](uint32_t b, uint32_t w_, uint32_t a) {
+        uint32_t lo = std::min((b & 0xFFFFu) + w_, a & 0xFFFFu);
+        uint32_t hi = std::min((b >> 16) + w_, a >> 16);
+        return lo | (hi << 16);
+    };
+    std::vector<uint32_t> RA((size_t)FP_THREADS * 64);
+    std::vector<uint32_t> C0(FP_THREADS), OUTC(FP_THREADS);
+    std::vector<uint64_t> OB(FP_THREADS);
+    std::vector<char> VALID(FP_THREADS);
     for (uint64_t s = 0; s < nsteps; s++) {
         for (uint32_t tid = 0; tid < FP_THREADS; tid++) {
-            const uint32_t k = tid & ((1u << pp.nk) - 1u), j = tid >> pp.nk;
-            if (((s << g) | j) >= pp.ntiles) continue;
+            const uint32_t k = tid & ((1u << pp.nkt) - 1u), j = tid >> pp.nkt;
+            VALID[tid] = ((s << g) | j) < pp.ntiles;
+            if (!VALID[tid]) continue;
             uint32_t c0 = pp.cfix, inc = pp.fin, outc = pp.fout;
-            for (int q = 0; q < pp.nk; q++)
-                if ((k >> q) & 1u) { c0 |= 1u << pp.kpos[q]; inc ^= pp.kin[q]; outc ^= pp.kout[q]; }
+            for (int q = 0; q < pp.nk; q++) {
+                const int bit = (pp.s_lane && q >= 4) ? q + 1 : q;
+                if ((k >> bit) & 1u) { c0 ^= 1u << pp.kpos[q]; inc ^= pp.kin[q]; outc ^= pp.kout[q]; }
+            }
+            if (pp.s_lane && ((k >> 4) & 1u)) { c0 ^= pp.s_lvec; inc ^= pp.s_lin; outc ^= pp.s_lout; }
             uint64_t ib = 0, ob = 0;
             for (int q = 0; q < ng; q++)
                 if ((j >> q) & 1u) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
             for (int q = ng; q < pp.n_outer; q++)
                 if ((s >> (q - ng)) & 1ull) { ib += pp.outer_in[q]; ob += pp.outer_out[q]; }
-            uint32_t R[64] = {0};
+            uint32_t *R = &RA[(size_t)tid * 64];
+            std::fill(R, R + 64, 0u);
             for (int x = 0; x < 8; x++) {
                 const uint32_t c = c0 ^ pp.sxoff[x];
                 uint8_t ch[16];
@@ -1234,8 +1283,31 @@ static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *ds
                 for (uint32_t q = 0; q < 16; q++)       // storage position q holds entry q ^ shift
                     R[reg(x, q)] |= (uint32_t)ch[q ^ pp.sshift[x]] << (16 * ((q >> 1) & 1u));
             }
-            for (int u = 0; u < pp.s_nres; u++) emu_reg_update(R, pp.s_rcode[u], pp.s_rw[u]);
-            for (int u = 0; u < pp.s_nc; u++) emu_reg_update(R, 8u << u, pp.s_cw[u]);
+            uint32_t (&Rr)[64] = *reinterpret_cast<uint32_t(*)[64]>(R);
+            for (int u = 0; u < pp.s_nres; u++) emu_reg_update(Rr, pp.s_rcode[u], pp.s_rw[u]);
+            for (int u = 0; u < pp.s_nc; u++) emu_reg_update(Rr, 8u << u, pp.s_cw[u]);
+            C0[tid] = c0;
+            OUTC[tid] = outc;
+            OB[tid] = ob;
+        }
+        if (pp.s_lane) {                 // the lane update: pairs (tid, tid ^ 16) from the old values
+            const uint32_t X = pp.s_lcode & 63u, HS = pp.s_lcode >> 6;
+            std::vector<uint32_t> old(RA);
+            for (uint32_t tid = 0; tid < FP_THREADS; tid++) {
+                if (!VALID[tid]) continue;
+                const uint32_t *P2 = &old[(size_t)(tid ^ 16u) * 64];
+                uint32_t *R = &RA[(size_t)tid * 64];
+                for (uint32_t i = 0; i < 64; i++) {
+                    const uint32_t v = P2[i ^ X];
+                    R[i] = addmin(HS ? sw(v) : v, pp.s_lw, old[(size_t)tid * 64 + i]);
+                }
+            }
+        }
+        for (uint32_t tid = 0; tid < FP_THREADS; tid++) {
+            if (!VALID[tid]) continue;
+            const uint32_t *R = &RA[(size_t)tid * 64];
+            const uint32_t c0 = C0[tid], outc = OUTC[tid];
+            const uint64_t ob = OB[tid];
             uint8_t W[8][16];
             for (int x = 0; x < 8; x++)
                 for (uint32_t e = 0; e < 16; e++) {
@@ -1250,8 +1322,8 @@ static void emulate_stream(const PassParams &pp, const uint8_t *src, uint8_t *ds
                     memcpy(dst + ob + (outc ^ pp.xout[x]), W[x], 16);
                 } else if (!(x & PB)) {
                     const int sb = pp.s_bit;
-                    const bool sw = pp.sxoff[x] & 1u;
-                    const uint8_t *A = sw ? W[x | PB] : W[x], *B = sw ? W[x] : W[x | PB];
+                    const bool swp = (pp.sxoff[x] ^ c0) & 1u;
+                    const uint8_t *A = swp ? W[x | PB] : W[x], *B = swp ? W[x] : W[x | PB];
                     for (uint32_t t = 0; t < 2; t++) {
                         if (!pp.s_both && t != pp.s_tgt) continue;
                         uint8_t *o = dst + ob + (outc ^ pp.xout[x]) + (pp.s_both ? t * pp.s_w : 0);
@@ -1528,7 +1600,7 @@ int tg_dense_plan_segments(void *plan, int64_t *out, int64_t maxseg) {
         if (S.kind == 1 && S.pp.stream) {
             int ws = 0;
             for (int x = 0; x < 8; x++) ws |= S.pp.s_wsw[x] != 0;
-            o[6] = S.pp.s_nres + 16 * ws;
+            o[6] = S.pp.s_nres + 16 * ws + 32 * S.pp.s_lane + 64 * S.pp.s_lgen;
         } else {
             o[6] = S.kind == 1 && S.pp.use_groups ? S.pp.ngroups : 0;
         }
@@ -1656,6 +1728,16 @@ int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, u
     e = cuda_check(cudaStreamSynchronize(st), "result sync");
     if (e) return e;
     *value = v;
+    return TG_OK;
+}
+
+// Update span of the coset-streaming passes (3: a thread's registers; 4: with the lane
+// dimension), and the span when an in-chunk row closes in the pass (2 or 3).
+int tg_dense_set_stream_span(int span, int span_sel) {
+    if (span < 2 || span > 4 || span_sel < 1 || span_sel > 3 || span_sel > span)
+        return set_error(TG_ERR_ARG, "stream span out of range");
+    g_span = span;
+    g_span_sel = span_sel;
     return TG_OK;
 }
 

@@ -160,6 +160,13 @@ struct PassParams {
     int s_nc, s_nres;
     int s_ws;                          // 1: some member is word-permuted (s_wsw)
     int s_pb;                          // mode 1: x bit of the member pairs (chunk bit 0)
+    // lane dimension: a fourth coset dimension split across the lane pair (l, l ^ 16): the thread
+    // with coset-number bit 4 set holds the coset shifted by s_lvec; the update along it exchanges
+    // registers with __shfl_xor (code s_lcode: register xor | lane swap << 6, weight s_lw)
+    int s_lane, nkt;                   // nkt = nk + s_lane: coset-number bits of a tile
+    int s_lgen;                        // 1: the lane update has an in-chunk part (general path)
+    uint32_t s_lvec, s_lin, s_lout;
+    uint8_t s_lcode, s_lw;
     uint8_t s_cw[4];
     uint8_t s_rcode[FP_MAXU], s_rw[FP_MAXU];
 };
@@ -371,18 +378,60 @@ static __device__ __forceinline__ void u8_pass_range(const PassParams &P, uint64
 
 
 // ------------------------------------------------------------------ coset-streaming pass (uint8)
+// the update along the lane dimension: register I takes min(R[I], partner lane's R[I ^ X] + w)
+// (lanes swapped when HS); pairs (I, I ^ X) read both partner values before writing
+template <int X, int HS, int I>
+struct LanePairs {
+    static __device__ __forceinline__ void run(uint32_t (&R)[64], uint32_t w2) {
+        if constexpr (X == 0) {
+            uint32_t v = __shfl_xor_sync(0xFFFFFFFFu, R[I], 16);
+            if constexpr (HS) v = swap_halves(v);
+            R[I] = __viaddmin_u16x2(v, w2, R[I]);
+        } else if constexpr (I < (I ^ X)) {
+            uint32_t a = __shfl_xor_sync(0xFFFFFFFFu, R[I ^ X], 16), b = __shfl_xor_sync(0xFFFFFFFFu, R[I], 16);
+            if constexpr (HS) { a = swap_halves(a); b = swap_halves(b); }
+            R[I] = __viaddmin_u16x2(a, w2, R[I]);
+            R[I ^ X] = __viaddmin_u16x2(b, w2, R[I ^ X]);
+        }
+        if constexpr (I < 63) LanePairs<X, HS, I + 1>::run(R, w2);
+    }
+};
+
+// code: register xor (bits 0..2: word and parity of the in-chunk part) | lane swap << 6
+static __device__ __forceinline__ void lane_dispatch(uint32_t code, uint32_t (&R)[64], uint32_t w2) {
+    switch (code) {
+        case 0: LanePairs<0, 0, 0>::run(R, w2); break;
+        case 1: LanePairs<1, 0, 0>::run(R, w2); break;
+        case 2: LanePairs<2, 0, 0>::run(R, w2); break;
+        case 3: LanePairs<3, 0, 0>::run(R, w2); break;
+        case 4: LanePairs<4, 0, 0>::run(R, w2); break;
+        case 5: LanePairs<5, 0, 0>::run(R, w2); break;
+        case 6: LanePairs<6, 0, 0>::run(R, w2); break;
+        case 7: LanePairs<7, 0, 0>::run(R, w2); break;
+        case 64: LanePairs<0, 1, 0>::run(R, w2); break;
+        case 65: LanePairs<1, 1, 0>::run(R, w2); break;
+        case 66: LanePairs<2, 1, 0>::run(R, w2); break;
+        case 67: LanePairs<3, 1, 0>::run(R, w2); break;
+        case 68: LanePairs<4, 1, 0>::run(R, w2); break;
+        case 69: LanePairs<5, 1, 0>::run(R, w2); break;
+        case 70: LanePairs<6, 1, 0>::run(R, w2); break;
+        case 71: LanePairs<7, 1, 0>::run(R, w2); break;
+        default: break;
+    }
+}
+
 // mode-1 output chunks of a coset: the member pairs (x, x ^ PB) that differ in chunk bit 0, without
 // in-chunk bit s_bit
 template <int PB>
 static __device__ __forceinline__ void u8_stream_pairs(const PassParams &P, const uint32_t (&W)[32], uint32_t keep,
-                                                      uint8_t *dst, uint32_t outc) {
+                                                      uint8_t *dst, uint32_t outc, uint32_t c0b) {
 #pragma unroll
     for (int x = 0; x < 8; x++) {
         if (x & PB) continue;
         if (!((keep >> x) & 1u)) continue;
         const uint4 M0 = make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]);
         const uint4 M1 = make_uint4(W[4 * (x | PB)], W[4 * (x | PB) + 1], W[4 * (x | PB) + 2], W[4 * (x | PB) + 3]);
-        const bool sw = P.sxoff[x] & 1u;           // member x has chunk bit 0 set: it is the upper one
+        const bool sw = (P.sxoff[x] ^ c0b) & 1u;   // member x has chunk bit 0 set: it is the upper one
         const uint4 A = sw ? M1 : M0, B = sw ? M0 : M1;
         uint8_t *const o = dst + (outc ^ P.xout[x]);
         if (P.s_both) {
@@ -399,7 +448,7 @@ static __device__ __forceinline__ void u8_stream_pairs(const PassParams &P, cons
 // member x with member x ^ 2^j), back to entry order and out to the output chunks (`keep`).
 template <int NC, bool WS, bool GEN = false>
 static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, const uint8_t *src, uint32_t inf,
-                                                      uint32_t keep, uint8_t *dst, uint32_t outc) {
+                                                      uint32_t keep, uint8_t *dst, uint32_t outc, uint32_t c0b) {
     uint32_t R[64];
 #pragma unroll
     for (int x = 0; x < 8; x++) {
@@ -432,6 +481,11 @@ static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, cons
     if constexpr (!GEN && NC >= 1) { const uint32_t w = P.s_cw[0]; RegPairs<8, 0, 0>::run(R, w | (w << 16)); }
     if constexpr (!GEN && NC >= 2) { const uint32_t w = P.s_cw[1]; RegPairs<16, 0, 0>::run(R, w | (w << 16)); }
     if constexpr (!GEN && NC >= 3) { const uint32_t w = P.s_cw[2]; RegPairs<32, 0, 0>::run(R, w | (w << 16)); }
+    if (P.s_lane) {                    // uniform: every lane of the warp takes this branch
+        const uint32_t w = P.s_lw;
+        if (GEN) lane_dispatch(P.s_lcode, R, w | (w << 16));
+        else LanePairs<0, 0, 0>::run(R, w | (w << 16));
+    }
     uint32_t W[32];
 #pragma unroll
     for (int x = 0; x < 8; x++) {
@@ -453,11 +507,11 @@ static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, cons
                 __stcs(reinterpret_cast<uint4 *>(dst + (outc ^ P.xout[x])),
                        make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]));
     } else if (P.s_pb == 0) {
-        u8_stream_pairs<1>(P, W, keep, dst, outc);
+        u8_stream_pairs<1>(P, W, keep, dst, outc, c0b);
     } else if (P.s_pb == 1) {
-        u8_stream_pairs<2>(P, W, keep, dst, outc);
+        u8_stream_pairs<2>(P, W, keep, dst, outc, c0b);
     } else {
-        u8_stream_pairs<4>(P, W, keep, dst, outc);
+        u8_stream_pairs<4>(P, W, keep, dst, outc, c0b);
     }
 }
 
@@ -474,8 +528,8 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
                                                    uint4 *smem_raw) {
     __shared__ int64_t s_cin[FP_MAXOUTER], s_cout[FP_MAXOUTER];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const int g = 9 - P.nk;                            // log2 of the tiles per step
-    const uint32_t k = tid & ((1u << P.nk) - 1u), j = tid >> P.nk;
+    const int g = 9 - P.nkt;                           // log2 of the tiles per step
+    const uint32_t k = tid & ((1u << P.nkt) - 1u), j = tid >> P.nkt;
     const int ng = min(g, P.n_outer);
     if (tid < (uint32_t)P.n_outer && (int)tid >= ng) {
         // carry table of the step index: base(s + 1) - base(s) when bit tid - ng is the lowest zero bit of s
@@ -486,8 +540,11 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
     }
     // the thread's coset (constant for the launch): its chunk offsets, kept and INF members
     uint32_t c0 = P.cfix, inc = P.fin, outc = P.fout;
-    for (int q = 0; q < P.nk; q++)
-        if ((k >> q) & 1u) { c0 |= 1u << P.kpos[q]; inc ^= P.kin[q]; outc ^= P.kout[q]; }
+    for (int q = 0; q < P.nk; q++) {
+        const int bit = (P.s_lane && q >= 4) ? q + 1 : q;      // bit 4 is the lane dimension
+        if ((k >> bit) & 1u) { c0 ^= 1u << P.kpos[q]; inc ^= P.kin[q]; outc ^= P.kout[q]; }
+    }
+    if (P.s_lane && ((k >> 4) & 1u)) { c0 ^= P.s_lvec; inc ^= P.s_lin; outc ^= P.s_lout; }
     uint32_t keep = 0, inf = 0;
 #pragma unroll
     for (int x = 0; x < 8; x++) {
@@ -541,16 +598,16 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
         cp_async_wait_group<2>();
         if (((s << g) | j) < ntiles) {
             const uint8_t *src = stage0 + st * 4096;
-            if (P.s_nres) u8_stream_coset<0, true, true>(P, src, inf, keep, out + ob, outc);
+            if (P.s_nres || P.s_lgen) u8_stream_coset<0, true, true>(P, src, inf, keep, out + ob, outc, c0 & 1u);
             else switch (P.s_nc + 4 * P.s_ws) {
-                case 0: u8_stream_coset<0, false>(P, src, inf, keep, out + ob, outc); break;
-                case 1: u8_stream_coset<1, false>(P, src, inf, keep, out + ob, outc); break;
-                case 2: u8_stream_coset<2, false>(P, src, inf, keep, out + ob, outc); break;
-                case 3: u8_stream_coset<3, false>(P, src, inf, keep, out + ob, outc); break;
-                case 4: u8_stream_coset<0, true>(P, src, inf, keep, out + ob, outc); break;
-                case 5: u8_stream_coset<1, true>(P, src, inf, keep, out + ob, outc); break;
-                case 6: u8_stream_coset<2, true>(P, src, inf, keep, out + ob, outc); break;
-                default: u8_stream_coset<3, true>(P, src, inf, keep, out + ob, outc); break;
+                case 0: u8_stream_coset<0, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 1: u8_stream_coset<1, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 2: u8_stream_coset<2, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 3: u8_stream_coset<3, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 4: u8_stream_coset<0, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 5: u8_stream_coset<1, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                case 6: u8_stream_coset<2, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
+                default: u8_stream_coset<3, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
             }
         }
         st = st == FS_STAGES - 1 ? 0 : st + 1;
