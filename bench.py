@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sections", default="batched,served,sparse",
+                    help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
 
 
@@ -210,6 +212,144 @@ def traffic_per_launch(kernel):
     return None
 
 
+# ---------------------------------------------------------------------- secondary workloads
+def _time_gpu(fn, reps=1):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps, out
+
+
+def section_batched(args):
+    """256 uneven banded instances (widths 12-26, 1-12 logical rows) in one persistent launch
+    against the same plans run one instance at a time with the plain path; the autotuned schedule
+    knobs per width."""
+    from tropidist_gb300 import auto, autotune, kernel, synth
+    from tropidist_gb300.batch import DenseBatch
+    ps = synth.batch_instances(seed=0, count=256, wmin=12, wmax=26, max_obs=12)
+    owner, plans = [], []
+    for k, p in enumerate(ps):
+        for _, pl in auto._plans(p, list(range(p.ncols))):
+            owner.append(k)
+            plans.append(pl)
+    tuner = autotune.Tuner().tune([16, 20, 24, 26], reps=2)
+    batch = DenseBatch(plans)
+    batch.run()
+    tb, vals = _time_gpu(batch.run)
+    cps = [autotune.compiled(pl, tuner) if pl.feasible else None for pl in plans]
+    peak = max(cp.peak_bits for cp in cps if cp is not None)
+    import torch
+    a = torch.empty(1 << peak, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+
+    def plain():
+        out = []
+        for k in range(len(ps)):                     # one instance at a time, its result read back
+            best = None
+            for i, cp in enumerate(cps):
+                if owner[i] != k or cp is None:
+                    continue
+                cp.execute(a, b)
+                v = cp.result(a, b)
+                best = v if best is None else min(best, v)
+            out.append(best)
+        return out
+    plain()
+    ts, seq = _time_gpu(plain)
+    per = [None] * len(ps)
+    for i, v in enumerate(vals):
+        if v is not None:
+            per[owner[i]] = v if per[owner[i]] is None else min(per[owner[i]], v)
+    for cp in cps:
+        if cp is not None:
+            cp.free()
+    return {"workload": "256 banded instances, widths 12-26, n = 8 w U(4,12), m = n/2, 1-12 logical rows, "
+                        "unit weights (seed 0)", "plans": len(plans), "solves_per_s": len(ps) / tb,
+            "plain_solves_per_s": len(ps) / ts, "speedup": ts / tb, "seconds": tb, "plain_seconds": ts,
+            "distances_equal": per == seq, "autotuned": tuner.report(),
+            "plain": "one instance at a time: its plans' schedules (autotuned per width) then its result"}
+
+
+def _serve_requests(seed=11):
+    from tropidist_gb300 import auto, serve, synth
+    ps = synth.batch_instances(seed=seed, count=96, wmin=10, wmax=28, max_obs=12)
+    dense = [serve.compile_request(k, [pl for _, pl in auto._plans(p, list(range(p.ncols)))])
+             for k, p in enumerate(ps)]
+    sparse = []
+    for j, n in enumerate([2000, 5000, 10000, 20000, 2000, 5000, 10000, 20000]):
+        p = synth.circuit_dem(seed=100 + j, rounds=max(4, n // 500), checks=24, ncols=n)
+        sparse.append(serve.SparseRequest(1000 + j, p, kmax=30))
+    # interleave: a sparse problem after every 12 dense ones
+    out, si = [], 0
+    for k, r in enumerate(dense):
+        out.append(r)
+        if k % 12 == 11 and si < len(sparse):
+            out.append(sparse[si])
+            si += 1
+    return out + sparse[si:]
+
+
+def section_served(args):
+    """Poisson request streams mixing banded instances (widths 10-28) and circuit-style sparse
+    problems (n = 2000-20000, 24 checks per round), served by the persistent-kernel request loop
+    with continuous batching, against the plain path (one request at a time), same distances."""
+    from tropidist_gb300 import serve
+    res = {"workload": "96 banded instances (widths 10-28, 1-12 logical rows, seed 11) + 8 circuit-style "
+                       "sparse problems (n 2000-20000), Poisson arrivals",
+           "admission": "dense tables in a persistent-kernel arena of 60 % of free HBM, sparse tables "
+                        "against 20 % (80 % in all)", "rates": {}}
+    for rate in (20, 2000):
+        arr = serve.poisson_arrivals(104, rate, seed=rate)
+        r1, w1, peak = serve.serve_persistent(_serve_requests(), arr, budget_frac=0.8, sparse_frac=0.2,
+                                              sparse_sms=24, jobs=1 << 21, param_bytes=2 << 30, plans=4096)
+        r2, w2 = serve.serve_plain(_serve_requests(), arr)
+        same = [a.distance for a in r1] == [b.distance for b in r2]
+        s1, s2 = serve.summarize(r1, w1), serve.summarize(r2, w2)
+        res["rates"][str(rate)] = {"served": s1, "plain": s2, "solves_ratio": s1["solves_per_s"] / s2["solves_per_s"],
+                                   "peak_plans_in_flight": peak, "distances_equal": same}
+    return res
+
+
+def section_sparse(args):
+    """The circuit-style detector error model scaled to 24 checks per round (40 rounds, n=20000,
+    weights {1,2,3}; 37 row slots: the as-written 150 checks need about 260 slots, beyond the
+    56-slot states of the reference's C tables and of these device tables) through the sparse DP
+    with meet in the middle at a weight threshold whose tables fit the device; the numpy
+    restatement of the reference's tables times the same query at a lower threshold on the host."""
+    import torch
+    from tropidist_gb300 import sparse_dp, synth
+    from oracle import sparse as osp
+    p = synth.circuit_dem(seed=0, rounds=40, checks=24, ncols=20000)
+    order = sparse_dp.default_order(p)
+    tr = sparse_dp.Trellis.for_query(p, 0, order)
+    out = {"workload": "circuit DEM 40 rounds x 24 checks, n=20000, weights {1,2,3}, seed 0",
+           "slots": tr.nslots}
+    for K in (4, 8):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = sparse_dp.query(tr, K, mode="mitm", backend="gpu", witness=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        sm = sparse_dp.summary(r)
+        steps = sum(v for k, v in sm.items() if k.endswith("_states_total"))
+        out["K%d" % K] = {"value": r["value"], "seconds": dt, "state_steps": int(steps),
+                          "state_steps_per_s": steps / dt, "peak_states": sm.get("peak_states")}
+    t0 = time.perf_counter()
+    r = sparse_dp.query(tr, 4, mode="mitm", backend=osp.NumpyTables(tr), witness=False)
+    dt = time.perf_counter() - t0
+    sm = sparse_dp.summary(r)
+    steps = sum(v for k, v in sm.items() if k.endswith("_states_total"))
+    out["cpu_baseline"] = {"K": 4, "value": r["value"], "seconds": dt, "state_steps_per_s": steps / dt,
+                           "kind": "port", "cores": 1, "sample": "the K=4 query, numpy restatement"}
+    return out
+
+
+SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse}
+
+
 # ---------------------------------------------------------------------- GPU arm
 def main():
     args = parse()
@@ -338,6 +478,15 @@ def main():
         rate, cwork, secs, desc, cores = cpu_window(plans[0], args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc,
                                 "seconds": secs}
+    del a, b, cps
+    torch.cuda.empty_cache()
+    sections = [x for x in args.sections.split(",") if x] if rank == 0 and world == 1 else []
+    for name in sections:
+        try:
+            line[name] = SECTIONS[name](args)
+        except Exception as e:          # a section's failure is reported in the line, not hidden
+            line[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()

@@ -109,6 +109,21 @@ int tg_sp_build(const void *A, uint64_t n, void *H, int lg, int below, void *kep
 /* replaces sp_join (cdist/sparse_dp.c:207-236): result (device uint64) = min (total << 56 | fkey) */
 int tg_sp_join(const void *F, uint64_t nf, const void *Hb, int lgb, uint64_t tmask, void *result, void *stream);
 int tg_sp_lookup(const void *H, int lg, const void *keys, uint64_t n, void *vals, void *stream);
+/* A run of column steps in one call (no counterpart in the reference, whose Python loop calls
+ * sp_candidates + sp_merge once per column): steps described by spec rows (host int64[16]), tables
+ * in caller-provided scratch, kept tables copied to a caller-provided arena, joins against backward
+ * indexes accumulated per step on the device; see csrc/sparse.cu for the fields.  Returns nsteps,
+ * or the step where scratch / arena ran out (need[0] states, need[1] bytes; run again). */
+int64_t tg_sp_walk_scratch_bytes(uint64_t cap_n);
+/* host planning (no GPU): the lookahead classes of every cut (the per-cut loop of
+ * cdist/sparse_dp.py:148-192), CSR inputs; see csrc/sparse.cu */
+int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
+                     const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows, const int32_t *row_start,
+                     const int32_t *row_end, const int32_t *slot, int L, int forward, int maxc, int32_t *ncls,
+                     uint64_t *masks, int64_t *weights, int64_t *extra);
+int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int64_t *weights, int stride, int K,
+               const void *A0, uint64_t n0, const void *H0, int lg0, void *scratch, uint64_t cap_n, void *arena,
+               uint64_t arena_bytes, int64_t *out, void *join_results, int64_t *need, void *counters, void *stream);
 /* replaces sp_hist (cdist/sparse_dp.c:239-242): hist is a device uint64[256] */
 int tg_sp_hist(const void *A, uint64_t n, void *hist, void *stream);
 

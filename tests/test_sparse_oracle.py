@@ -115,3 +115,19 @@ def test_weighted_columns_against_brute_force():
             assert r["value"] == truth, (mode, r["value"], truth)
             if truth is not None:
                 assert sum(wts[j] for j in r["witness"]) == truth
+
+
+def test_bound_data_host_routine_matches_restatement():
+    """The library's host routine for the lookahead classes equals the numpy restatement of
+    cdist/sparse_dp.py:148-192 cut for cut, in both directions."""
+    from tropidist_gb300 import sparse_dp, synth
+    for seed, rounds, checks, n in [(0, 6, 12, 600), (1, 8, 16, 1500)]:
+        p = synth.circuit_dem(seed=seed, rounds=rounds, checks=checks, ncols=n)
+        tr = sparse_dp.Trellis.for_query(p, 0, sparse_dp.default_order(p))
+        for fwd in (True, False):
+            a, b = tr._bound_data(fwd), tr._bound_data_py(fwd)
+            assert len(a) == len(b)
+            for x, y in zip(a, b):
+                assert [int(v) for v in x[0]] == [int(v) for v in y[0]]
+                assert [int(v) for v in x[1]] == [int(v) for v in y[1]]
+                assert int(x[2]) == int(y[2])

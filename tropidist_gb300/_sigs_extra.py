@@ -11,6 +11,9 @@ SIGNATURES = {
     "tg_sp_join": (ci, [vp, u64, vp, ci, u64, vp, vp]),
     "tg_sp_lookup": (ci, [vp, ci, vp, u64, vp, vp]),
     "tg_sp_hist": (ci, [vp, u64, vp, vp]),
+    "tg_sp_walk_scratch_bytes": (i64, [u64]),
+    "tg_sp_bound_data": (ci, [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, ci, ci, ci, vp, vp, vp, vp]),
+    "tg_sp_walk": (ci, [ci, vp, vp, vp, ci, ci, vp, u64, vp, ci, vp, u64, vp, u64, vp, vp, vp, vp, vp]),
     "tg_tab_create": (vp, [ci, ci, c.POINTER(ci)]),
     "tg_tab_free": (None, [vp]),
     "tg_tab_count": (i64, [vp]),

@@ -19,6 +19,7 @@
 #include "tg_common.cuh"
 #include "tg_capi.h"
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -231,6 +232,55 @@ static int load_bound(BoundParams &B, int on, int K, int ncls, const uint64_t *m
     return TG_OK;
 }
 
+
+// ------------------------------------------------------------------ walks: many steps per call
+// Host-side loop over a run of column steps with the tables in caller-provided scratch (three
+// table slots, a changed list), the kept tables copied into a caller-provided arena, and joins
+// against backward indexes accumulated per step on the device: one call per run of steps instead
+// of one per column, and no allocation.
+#define SPW_FIELDS 16
+enum { SW_UPD, SW_SELM, SW_SELB, SW_TMASK, SW_JTAB, SW_JTMASK, SW_EXTRA, SW_CAP, SW_KB, SW_W, SW_WANT, SW_TRUNC,
+       SW_KEEP, SW_JLG, SW_NCLS, SW_USEH };
+
+static int lg_for(uint64_t n) {          // index size for up to n states at load <= 1/2 (>= 64 slots)
+    const uint64_t x = 2 * (n ? n : 1) - 1;
+    int b = 0;
+    while ((x >> b) != 0) b++;
+    return b + 1 > 6 ? b + 1 : 6;
+}
+
+__global__ void k_sp_join_acc(const unsigned long long *__restrict__ F, uint64_t nf, const unsigned long long *Hb,
+                              int lgb, uint64_t tmask, unsigned long long *result) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nf; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = F[i];
+        const uint64_t key = x & SP_KEYMASK;
+        const uint32_t bv = sp_lookup(Hb, lgb, key ^ tmask);
+        if (bv != 255u) atomicMin(result, (((x >> 56) + bv) << 56) | key);
+    }
+}
+
+struct WalkScratch {
+    uint64_t cap_n;
+    int lgc;
+    unsigned long long *arr[3], *idx[3], *changed;
+};
+
+static uint64_t walk_scratch_bytes(uint64_t cap_n, int &lgc) {
+    lgc = lg_for(cap_n);
+    return 8 * (4 * cap_n + 3 * (1ull << lgc));
+}
+
+static bool walk_layout(void *scratch, uint64_t cap_n, WalkScratch &W) {
+    W.cap_n = cap_n;
+    walk_scratch_bytes(cap_n, W.lgc);
+    unsigned long long *p = static_cast<unsigned long long *>(scratch);
+    for (int k = 0; k < 3; k++) { W.arr[k] = p; p += cap_n; }
+    W.changed = p;
+    p += cap_n;
+    for (int k = 0; k < 3; k++) { W.idx[k] = p; p += 1ull << W.lgc; }
+    return true;
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -280,6 +330,215 @@ int tg_sp_step(const void *A, uint64_t n, const void *Hold, int lg_old, void *Hn
     k_sp_compact<<<sp_grid(capn), 256, 0, st>>>((const unsigned long long *)Hnew, capn, (unsigned long long *)Anew,
                                                 anew_cap, (unsigned long long *)counters);
     return cuda_check(cudaGetLastError(), "sparse step");
+}
+
+// Bytes of scratch for a walk whose tables hold up to cap_n states (three table slots with their
+// indexes and a changed list).
+int64_t tg_sp_walk_scratch_bytes(uint64_t cap_n) {
+    int lgc;
+    return (int64_t)walk_scratch_bytes(cap_n, lgc);
+}
+
+// A run of nsteps column steps from the table (A0, n0, H0, lg0) (device; left unchanged).
+// spec: host int64[nsteps][16]: upd, sel_mask, sel_bits, lookahead tmask, join index (device
+// pointer, 0: no join), join tmask, lookahead extra, cap, keep_below (-1: none), w, want_changed,
+// trunc_below (-1: none; else the table after the step keeps values < trunc_below and the table
+// before is joined in full), keep, join lg, ncls, use_h.  masks / weights: host [nsteps][stride]
+// lookahead classes.  scratch: tg_sp_walk_scratch_bytes(cap_n) bytes.  Kept tables are copied into
+// the arena (array, then index, 256-byte aligned).  out: host int64[nsteps][6]: states after the
+// step, changed states, arena byte offsets of the kept array and index (-1: not kept), index lg,
+// states before truncation.  join_results: device uint64[nsteps], each the packed minimum
+// (total << 56 | forward key) of the step's joins (all ones: no pair).  Returns nsteps, or the
+// step at which the scratch (need[0]: states per table) or the arena (need[1]: bytes) ran out
+// (nothing of the run is usable then: run it again with more room); negative status on errors.
+int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int64_t *weights, int stride, int K,
+               const void *A0, uint64_t n0, const void *H0, int lg0, void *scratch, uint64_t cap_n, void *arena,
+               uint64_t arena_bytes, int64_t *out, void *join_results, int64_t *need, void *counters, void *stream) {
+    if (nsteps < 0 || (nsteps && !spec) || !out || !scratch || !counters || (n0 && (!A0 || !H0)) ||
+        (nsteps && !join_results) || !need || cap_n < 2)
+        return set_error(TG_ERR_ARG, "bad walk");
+    cudaStream_t st = (cudaStream_t)stream;
+    WalkScratch W;
+    walk_layout(scratch, cap_n, W);
+    unsigned long long *cnt = static_cast<unsigned long long *>(counters);
+    unsigned long long *res = static_cast<unsigned long long *>(join_results);
+    static thread_local unsigned long long *hb = nullptr;        // pinned readback of the counters
+    if (!hb && cudaMallocHost(&hb, 64) != cudaSuccess) {
+        cudaGetLastError();
+        hb = nullptr;
+        return set_error(TG_ERR_NOMEM, "pinned walk buffer");
+    }
+    int e = TG_OK;
+    if (nsteps) e = cuda_check(cudaMemsetAsync(res, 0xFF, 8 * (size_t)nsteps, st), "join init");
+    if (e) return e;
+    auto read_counters = [&]() -> int {
+        int r = cuda_check(cudaMemcpyAsync(hb, cnt, 32, cudaMemcpyDeviceToHost, st), "walk counters");
+        if (!r) r = cuda_check(cudaStreamSynchronize(st), "walk sync");
+        if (!r && hb[2]) r = set_error(TG_ERR_STATE, "walk table overflow");
+        return r;
+    };
+    const unsigned long long *curA = static_cast<const unsigned long long *>(A0);
+    const unsigned long long *curH = static_cast<const unsigned long long *>(H0);
+    uint64_t n = n0;
+    int lg = lg0, cur = -1;
+    uint64_t used = 0;
+    need[0] = need[1] = 0;
+    for (int i = 0; i < nsteps; i++) {
+        const int64_t *f = spec + (size_t)SPW_FIELDS * i;
+        int64_t *o = out + 6 * (size_t)i;
+        if (2 * n > cap_n) { need[0] = (int64_t)(2 * n); return i; }
+        if (f[SW_CAP] > 254 || f[SW_W] < 1 || f[SW_W] > 254) return set_error(TG_ERR_ARG, "values beyond 8 bits");
+        int os = 0;
+        while (os == cur) os++;
+        const int lgn = lg_for(2 * n);
+        StepParams P;
+        P.upd = (uint64_t)f[SW_UPD] & SP_KEYMASK;
+        P.sel_mask = (uint64_t)f[SW_SELM];
+        P.sel_bits = (uint64_t)f[SW_SELB];
+        P.cap = (int)f[SW_CAP];
+        P.keep_below = (int)f[SW_KB];
+        P.w = (int)f[SW_W];
+        P.want_changed = f[SW_WANT] != 0;
+        P.lg_old = lg;
+        P.lg_new = lgn;
+        BoundParams B;
+        e = load_bound(B, (int)f[SW_USEH], K, (int)f[SW_NCLS], masks + (size_t)stride * i, weights + (size_t)stride * i,
+                       f[SW_EXTRA], (uint64_t)f[SW_TMASK]);
+        if (e) return e;
+        e = cuda_check(cudaMemsetAsync(cnt, 0, 32, st), "walk counters");
+        if (e) return e;
+        const uint64_t capn = 1ull << lgn;
+        k_sp_fill<<<sp_grid(capn), 256, 0, st>>>(W.idx[os], capn);
+        if (n) k_sp_step<<<sp_grid(n), 256, 0, st>>>(P, B, curA, n, curH, W.idx[os], W.changed, W.cap_n, cnt);
+        k_sp_compact<<<sp_grid(capn), 256, 0, st>>>(W.idx[os], capn, W.arr[os], W.cap_n, cnt);
+        e = cuda_check(cudaGetLastError(), "walk step");
+        if (!e) e = read_counters();
+        if (e) return e;
+        uint64_t nn = hb[3];
+        const uint64_t nch = P.want_changed ? hb[1] : 0;
+        const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[SW_JTAB]);
+        const uint64_t jt = (uint64_t)f[SW_JTMASK] & SP_KEYMASK;
+        o[5] = (int64_t)nn;
+        if (jH && nch)
+            k_sp_join_acc<<<sp_grid(nch), 256, 0, st>>>(W.changed, nch, jH, (int)f[SW_JLG], jt, res + i);
+        const unsigned long long *nA = W.arr[os], *nH = W.idx[os];
+        int nlg = lgn, ns = os;
+        if (f[SW_TRUNC] >= 0) {
+            if (jH && nn) k_sp_join_acc<<<sp_grid(nn), 256, 0, st>>>(nA, nn, jH, (int)f[SW_JLG], jt, res + i);
+            int ts = 0;
+            while (ts == os) ts++;
+            const int lgt = lg_for(nn);
+            e = cuda_check(cudaMemsetAsync(cnt, 0, 32, st), "walk counters");
+            if (e) return e;
+            k_sp_fill<<<sp_grid(1ull << lgt), 256, 0, st>>>(W.idx[ts], 1ull << lgt);
+            if (nn) k_sp_build<<<sp_grid(nn), 256, 0, st>>>(nA, nn, W.idx[ts], lgt, (int)f[SW_TRUNC], W.arr[ts], cnt);
+            e = cuda_check(cudaGetLastError(), "walk truncate");
+            if (!e) e = read_counters();
+            if (e) return e;
+            nn = hb[3];
+            nA = W.arr[ts];
+            nH = W.idx[ts];
+            nlg = lgt;
+            ns = ts;
+        }
+        o[0] = (int64_t)nn;
+        o[1] = (int64_t)nch;
+        o[2] = o[3] = -1;
+        o[4] = nlg;
+        if (f[SW_KEEP]) {
+            // the kept copy gets an index of its own at load <= 1/2 (half the working index)
+            const int lgk = lg_for(nn);
+            const uint64_t ab = (8 * nn + 255) / 256 * 256, ib = 8ull << lgk;
+            if (!arena || used + ab + ib > arena_bytes) { need[1] = (int64_t)(used + ab + ib); return i; }
+            uint8_t *base = static_cast<uint8_t *>(arena);
+            unsigned long long *kA = reinterpret_cast<unsigned long long *>(base + used);
+            unsigned long long *kH = reinterpret_cast<unsigned long long *>(base + used + ab);
+            if (nn) e = cuda_check(cudaMemcpyAsync(kA, nA, 8 * nn, cudaMemcpyDeviceToDevice, st), "keep array");
+            if (e) return e;
+            k_sp_fill<<<sp_grid(1ull << lgk), 256, 0, st>>>(kH, 1ull << lgk);
+            if (nn) k_sp_build<<<sp_grid(nn), 256, 0, st>>>(kA, nn, kH, lgk, -1, nullptr, cnt);
+            e = cuda_check(cudaGetLastError(), "keep index");
+            if (e) return e;
+            o[2] = (int64_t)used;
+            o[3] = (int64_t)(used + ab);
+            o[4] = lgk;
+            used += ab + ib;
+        }
+        curA = nA;
+        curH = nH;
+        n = nn;
+        lg = nlg;
+        cur = ns;
+    }
+    return nsteps;
+}
+
+// Lookahead classes of every cut of a sparse trellis (host work, no GPU; the per-cut loop of
+// cdist/sparse_dp.py:148-192 in C++).  Rows are given as sorted column positions (row_ptr /
+// row_cols, CSR), columns as rows (col_ptr / col_rows), the active rows of each cut (act_ptr /
+// act_rows), each row's first and last position and slot, the target row L.  For cut c the
+// relevant rows are the active ones (plus L while it lies wholly on the remaining side); row r gets
+// weight Q / (max over the remaining columns j containing r of |supp(j) ∩ relevant|); rows are
+// grouped into classes of equal weight (masks of slots, weights ascending), L's weight is `extra`.
+// Output per cut: ncls[c], masks / weights [c][maxc], extra[c].  Returns 0, or -4 if a cut has
+// more than maxc classes.
+int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
+                     const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows, const int32_t *row_start,
+                     const int32_t *row_end, const int32_t *slot, int L, int forward, int maxc, int32_t *ncls,
+                     uint64_t *masks, int64_t *weights, int64_t *extra) {
+    if (N < 0 || nrows <= 0 || !row_ptr || !col_ptr || !act_ptr || !ncls || !masks || !weights || !extra || maxc < 1)
+        return set_error(TG_ERR_ARG, "bad bound data");
+    std::vector<char> inrel(nrows, 0);
+    std::vector<int> rel;
+    std::vector<std::pair<int64_t, uint64_t>> cls;
+    for (int c = 0; c <= N; c++) {
+        rel.assign(act_rows + act_ptr[c], act_rows + act_ptr[c + 1]);
+        const bool lone = forward ? row_start[L] >= c : row_end[L] < c;
+        if (lone && std::find(rel.begin(), rel.end(), L) == rel.end()) rel.push_back(L);
+        ncls[c] = 0;
+        extra[c] = 0;
+        if (rel.empty()) continue;
+        int lo, hi;
+        if (forward) {
+            lo = c;
+            hi = 0;
+            for (int r : rel) hi = std::max(hi, row_end[r] + 1);
+        } else {
+            lo = N;
+            for (int r : rel) lo = std::min(lo, row_start[r]);
+            hi = c;
+        }
+        for (int r : rel) inrel[r] = 1;
+        cls.clear();
+        for (int r : rel) {
+            const int32_t *b = row_cols + row_ptr[r], *e = row_cols + row_ptr[r + 1];
+            int worst = 0;
+            for (const int32_t *q = std::lower_bound(b, e, lo); q < e && *q < hi; q++) {
+                int cnt = 0;
+                for (int64_t k = col_ptr[*q]; k < col_ptr[*q + 1]; k++) cnt += inrel[col_rows[k]];
+                worst = std::max(worst, cnt);
+            }
+            if (worst < 1) {
+                for (int r2 : rel) inrel[r2] = 0;
+                return set_error(TG_ERR_STATE, "a relevant row without a remaining column");
+            }
+            const int64_t wr = SP_QW / worst;
+            if (lone && r == L) { extra[c] = wr; continue; }
+            bool found = false;
+            for (auto &x : cls)
+                if (x.first == wr) { x.second |= 1ull << slot[r]; found = true; break; }
+            if (!found) cls.push_back({wr, 1ull << slot[r]});
+        }
+        for (int r : rel) inrel[r] = 0;
+        if ((int)cls.size() > maxc) return set_error(TG_ERR_TOO_BIG, "more lookahead classes than the output holds");
+        std::sort(cls.begin(), cls.end());
+        ncls[c] = (int32_t)cls.size();
+        for (size_t k = 0; k < cls.size(); k++) {
+            weights[(size_t)c * maxc + k] = cls[k].first;
+            masks[(size_t)c * maxc + k] = cls[k].second;
+        }
+    }
+    return TG_OK;
 }
 
 // Index (2^lg slots, cleared by the call) of an array of distinct packed states.  below >= 0:

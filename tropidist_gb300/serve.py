@@ -10,7 +10,9 @@ Server             accepts distance requests (dense Rank DP problems, as their s
 PersistentServer   the same interface on one long-lived persistent kernel (csrc/batch.cu k_server):
                    admitted plans are handed to the running kernel through a device mailbox and
                    their passes are interleaved with the plans already in flight at tile-range
-                   granularity, with no kernel launches per pass.
+                   granularity, with no kernel launches per pass.  Sparse requests (SparseRequest:
+                   circuit-style problems for the sparse Rank DP) run beside it on their own stream
+                   and SMs, admitted against their share of the memory budget.
 serve_plain        the same requests one at a time on one stream (the plain GPU path).
 poisson_arrivals   seeded exponential inter-arrival times.
 Latency = completion time - arrival time; p50 / p99 and solves/s are computed by `summarize`.
@@ -46,6 +48,33 @@ def compile_request(rid, plans):
     """A request whose plans are scheduled ahead of time (scheduling is host work, outside the GPU
     timing of both serving modes)."""
     return Request(rid, plans, [kernel.CompiledPlan(pl) if pl.feasible else None for pl in plans])
+
+
+class SparseRequest:
+    """A distance problem for the sparse Rank DP (iterative deepening over the weight threshold,
+    meet in the middle; the problem's tables live on the device while it runs)."""
+    kind = "sparse"
+
+    def __init__(self, rid, problem, kmax=30, max_states=1 << 26):
+        self.rid = rid
+        self.problem = problem
+        self.kmax = kmax
+        self.max_states = max_states
+        self.footprint = 24 * max_states          # packed states + index + changed list, bytes
+        self.arrival = self.admitted = self.done = None
+        self.distance = None
+        self.values = None
+        self.error = None
+
+
+def _run_sparse(req):
+    from . import sparse_dp
+    try:
+        r = sparse_dp.distance(req.problem, kmax=req.kmax, witness=False)
+        req.distance = r["distance"]
+    except (sparse_dp.BudgetExceeded, MemoryError, ValueError) as e:
+        req.error = "%s: %s" % (type(e).__name__, e)
+    req.values = [req.distance]
 
 
 def _launch(req, stream):
@@ -205,6 +234,12 @@ def serve_plain(reqs, arrivals):
             time.sleep(at - now)
         req.arrival = t0 + at
         req.admitted = time.perf_counter()
+        if getattr(req, "kind", None) == "sparse":
+            with torch.cuda.stream(stream):
+                _run_sparse(req)
+            stream.synchronize()
+            req.done = time.perf_counter()
+            continue
         _launch(req, stream)
         req.event.synchronize()
         req.done = time.perf_counter()
@@ -224,17 +259,21 @@ class PersistentServer:
     the arena (device tables) and the descriptor pools have room; finished plans are collected by
     polling, and a request completes when all of its plans have."""
 
-    def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192):
+    def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192,
+                 sparse_frac=0.0, sparse_sms=0):
         import ctypes
         import torch
         from . import _lib
         device.require_gpu()
         self.torch, self.ctypes, self.L = torch, ctypes, _lib.lib()
+        free = device.free_bytes()
         if arena_bytes is None:
-            arena_bytes = int(budget_frac * device.free_bytes()) - param_bytes - 64 * jobs
+            arena_bytes = int((budget_frac - sparse_frac) * free) - param_bytes - 64 * jobs
         self.arena = device.empty(arena_bytes)
         st = ctypes.c_int(0)
-        self.handle = self.L.tg_server_create(self.arena.data_ptr(), arena_bytes, jobs, param_bytes, plans, 0,
+        # sparse requests run beside the persistent kernel: it leaves `sparse_sms` SMs to them
+        blocks = max(1, _lib.lib().tg_sm_count() - int(sparse_sms)) if sparse_sms else 0
+        self.handle = self.L.tg_server_create(self.arena.data_ptr(), arena_bytes, jobs, param_bytes, plans, blocks,
                                               ctypes.byref(st))
         if not self.handle:
             _lib.check(st.value)
@@ -251,13 +290,44 @@ class PersistentServer:
         self.vals = np.zeros(plans, dtype=np.uint32)
         self.thread = threading.Thread(target=self._loop, daemon=True)
         self.thread.start()
+        # sparse requests: a worker on its own stream, admitted one at a time against the sparse share
+        # of the memory budget
+        self.sparse_budget = int(sparse_frac * free)
+        self.sparse_q = collections.deque()
+        self.sparse_wake = threading.Event()
+        self.sparse_thread = threading.Thread(target=self._sparse_loop, daemon=True)
+        self.sparse_thread.start()
 
     def submit(self, req, arrival=None):
         req.arrival = time.perf_counter() if arrival is None else arrival
         with self.lock:
-            self.pending.append(req)
             self.submitted += 1
+            if getattr(req, "kind", None) == "sparse":
+                if req.footprint > self.sparse_budget:
+                    self.submitted -= 1
+                    raise MemoryError("sparse request %s needs %d bytes, beyond the sparse budget" %
+                                      (req.rid, req.footprint))
+                self.sparse_q.append(req)
+                self.sparse_wake.set()
+            else:
+                self.pending.append(req)
         return req
+
+    def _sparse_loop(self):
+        stream = self.torch.cuda.Stream()
+        while not self.stop_flag:
+            with self.lock:
+                req = self.sparse_q.popleft() if self.sparse_q else None
+            if req is None:
+                self.sparse_wake.wait(0.001)
+                self.sparse_wake.clear()
+                continue
+            req.admitted = time.perf_counter()
+            with self.torch.cuda.stream(stream):
+                _run_sparse(req)
+            stream.synchronize()
+            req.done = time.perf_counter()
+            self.finished.append(req)
 
     def _admit(self, req):
         """Submit every feasible plan of the request; False (nothing submitted) if there is no room."""
@@ -339,6 +409,8 @@ class PersistentServer:
     def close(self):
         self.stop_flag = True
         self.thread.join(timeout=10)
+        self.sparse_wake.set()
+        self.sparse_thread.join(timeout=60)
         if self.handle:
             self.L.tg_server_free(self.handle)
             self.handle = None

@@ -127,6 +127,45 @@ class Trellis:
 
     # ------------------------------------------------------------------ lookahead bound
     def _bound_data(self, forward):
+        """Per cut: (masks, weights, extra) of the lookahead bound, computed by the library's host
+        routine (tg_sp_bound_data; the same rule as _bound_data_py)."""
+        N, rows = self.N, self.rows
+        nr = len(rows)
+        rc = [_bits(row) for row in rows]
+        row_ptr = np.zeros(nr + 1, dtype=np.int64)
+        row_ptr[1:] = np.cumsum([len(x) for x in rc])
+        row_cols = np.array([j for x in rc for j in x], dtype=np.int32)
+        cr = [[] for _ in range(N)]
+        for r, x in enumerate(rc):
+            for j in x:
+                cr[j].append(r)
+        col_ptr = np.zeros(N + 1, dtype=np.int64)
+        col_ptr[1:] = np.cumsum([len(x) for x in cr])
+        col_rows = np.array([r for x in cr for r in x], dtype=np.int32)
+        act = [list(self.active_rows[c]) for c in range(N + 1)]
+        act_ptr = np.zeros(N + 2, dtype=np.int64)
+        act_ptr[1:] = np.cumsum([len(x) for x in act])
+        act_rows = np.array([r for x in act for r in x], dtype=np.int32)
+        start = np.array(self.start, dtype=np.int32)
+        end = np.array(self.end, dtype=np.int32)
+        slot = np.array(self.slot, dtype=np.int32)
+        maxc = 48
+        ncls = np.zeros(N + 1, dtype=np.int32)
+        masks = np.zeros((N + 1, maxc), dtype=U64)
+        wts = np.zeros((N + 1, maxc), dtype=np.int64)
+        extra = np.zeros(N + 1, dtype=np.int64)
+        ptr = lambda a: a.ctypes.data if a.size else None
+        _lib.check(_lib.lib().tg_sp_bound_data(N, nr, ptr(row_ptr), ptr(row_cols), ptr(col_ptr), ptr(col_rows),
+                                               ptr(act_ptr), ptr(act_rows), ptr(start), ptr(end), ptr(slot), self.L,
+                                               int(bool(forward)), maxc, ptr(ncls), ptr(masks), ptr(wts),
+                                               ptr(extra)))
+        out = []
+        for c in range(N + 1):
+            k = int(ncls[c])
+            out.append((tuple(masks[c, :k]), tuple(wts[c, :k]), int(extra[c])))
+        return out
+
+    def _bound_data_py(self, forward):
         """Per cut: (masks, weights, extra) of h(s) = ceil((extra + sum_k w_k |(s ^ tmask) & mask_k|) / Q).
         Row r relevant at cut c gets weight y_r = 1 / max over remaining columns j containing r of
         |supp(j) ∩ relevant rows| (a dual solution of the covering LP), rounded down to 1/Q; the
@@ -351,6 +390,54 @@ class GpuTables:
         bval = self.lookup(btab, bkey)
         return total, fkey, total - bval, bkey
 
+    def walk(self, tab, rows, masks, weights, K, max_states=None):
+        """Run the column steps of `rows` (int64 [m, 16] spec rows, csrc/sparse.cu tg_sp_walk) from
+        `tab` in one call: (out int64 [m, 6], {step: kept table}, join results uint64 [m])."""
+        torch = self.torch
+        m = len(rows)
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        masks = np.ascontiguousarray(masks, dtype=U64)
+        weights = np.ascontiguousarray(weights, dtype=np.int64)
+        stride = masks.shape[1] if masks.ndim == 2 else 0
+        cap = max(getattr(self, "_walk_cap", 1 << 12), 4 * tab.n)
+        arena_bytes = max(getattr(self, "_arena_guess", 1 << 20), 1 << 16)
+        out = np.zeros((max(1, m), 6), dtype=np.int64)
+        need = np.zeros(2, dtype=np.int64)
+        res = torch.empty(max(1, m), dtype=torch.int64, device="cuda")
+        L = self.L
+        while True:
+            if max_states is not None and cap > 4 * max(max_states, 1) + 4 * tab.n:
+                raise BudgetExceeded("a walk needs tables of %d states" % (cap // 2), "states")
+            sb = int(L.tg_sp_walk_scratch_bytes(cap))
+            if getattr(self, "_scratch", None) is None or self._scratch.numel() * 8 < sb:
+                self._scratch = None
+                self._scratch = torch.empty((sb + 7) // 8, dtype=torch.int64, device="cuda")
+            arena = None
+            arena = torch.empty((arena_bytes + 7) // 8, dtype=torch.int64, device="cuda")
+            r = L.tg_sp_walk(m, rows.ctypes.data, masks.ctypes.data, weights.ctypes.data, stride, int(K),
+                             tab.arr.data_ptr() if tab.n else None, tab.n, tab.H.data_ptr(), tab.lg,
+                             self._scratch.data_ptr(), cap, arena.data_ptr(), arena_bytes, out.ctypes.data,
+                             res.data_ptr(), need.ctypes.data, self.counters.data_ptr(), device.stream_ptr())
+            if r < 0:
+                _lib.check(r)
+            if r == m:
+                break
+            if need[0]:
+                cap = max(2 * cap, 2 * int(need[0]))
+            if need[1]:
+                # bytes for the steps done so far, extrapolated to the whole run
+                arena_bytes = max(arena_bytes + (arena_bytes >> 1), int(need[1]) * m // max(1, r + 1) + (1 << 20))
+        self._walk_cap = cap
+        kept, used = {}, 0
+        for i in range(m):
+            if out[i, 2] >= 0:
+                n, lg = int(out[i, 0]), int(out[i, 4])
+                a0, h0 = int(out[i, 2]) // 8, int(out[i, 3]) // 8
+                kept[i] = _Tab(arena[a0:a0 + n], n, arena[h0:h0 + (1 << lg)], lg)
+                used = max(used, 8 * (h0 + (1 << lg)))
+        self._arena_guess = max(1 << 16, used + (used >> 2))
+        return out[:m], kept, res[:m].cpu().numpy().view(U64)
+
     def hist(self, tab):
         import torch
         h = torch.zeros(256, dtype=torch.int64, device="cuda")
@@ -430,6 +517,98 @@ class Sweep:
             return cut, self.be.truncate(tab, self.caps[cut]), ch, tab
         return cut, tab, ch, None
 
+    # ---- device walks (GpuTables): a run of steps per library call
+    def _rows(self, positions, keep, joins=None):
+        """Spec rows of tg_sp_walk for the steps at `positions` (as _step), with lookahead arrays;
+        keep: per step 0/1; joins: per step None or (backward table, tmask)."""
+        tr, fwd = self.tr, self.direction > 0
+        m = len(positions)
+        rows = np.zeros((m, 16), dtype=np.int64)
+        hds = []
+        for k, p in enumerate(positions):
+            cut = p + 1 if fwd else p
+            sm, sb = (tr.fsel_mask[p], tr.fsel_bits[p]) if fwd else (tr.bsel_mask[p], tr.bsel_bits[p])
+            cap, kb = self.caps[cut], -1
+            if self.frontier:
+                cap = kb = self.caps[p]
+            trunc = self.caps[cut] if (self.frontier and self.caps[cut] < cap) else -1
+            hd = self.hd[cut] if self.hd else None
+            hds.append(hd)
+            jt, jtm, jlg = 0, 0, 0
+            if joins is not None and joins[k] is not None:
+                btab, jtm = joins[k]
+                jt, jlg = btab.H.data_ptr(), btab.lg
+            rows[k] = [int(tr.col[p]) & KEYMASK, int(sm), int(sb), int(tr.tmask[cut]) & KEYMASK, jt,
+                       int(jtm) & KEYMASK, int(hd[2]) if hd is not None else 0, int(cap), int(kb), int(tr.cw[p]),
+                       1 if joins is not None else 0, int(trunc), int(keep[k]), int(jlg),
+                       len(hd[0]) if hd is not None else 0, 1 if hd is not None else 0]
+        stride = max([len(h[0]) for h in hds if h is not None] + [1])
+        masks = np.zeros((m, stride), dtype=U64)
+        weights = np.zeros((m, stride), dtype=np.int64)
+        for k, hd in enumerate(hds):
+            if hd is not None and len(hd[0]):
+                masks[k, :len(hd[0])] = hd[0]
+                weights[k, :len(hd[1])] = hd[1]
+        return rows, masks, weights
+
+    def _positions(self, c, stop):
+        return list(range(c, stop)) if self.direction > 0 else list(range(c - 1, stop - 1, -1))
+
+    def _cut_of(self, p):
+        return p + 1 if self.direction > 0 else p
+
+    def _next_ckpt(self, c, stop):
+        if self.direction > 0:
+            return min(stop, (c // self.every + 1) * self.every)
+        return max(stop, (c - 1) // self.every * self.every)
+
+    def _run_walk(self, join_with=None, lower=0):
+        """run() on device walks, one per checkpoint interval; join_with: the backward sweep whose
+        tables the changed states of every cut are joined with (the meet in the middle).  Returns
+        (last cut, best join (total, cut, forward key) or None)."""
+        c0, tab = self.first()
+        self.ckpt[c0] = tab
+        self.counts[c0] = self.changed_counts[c0] = 1
+        self.peak = 1
+        best = None
+        cache = {}
+        if join_with is not None:
+            r = self.be.join(_as_changed(self.be, tab), join_with.table(c0, cache), self.tr.tmask[c0])
+            if r is not None:
+                best = (r[0], c0, r[1])
+        stop = self.tr.N if self.direction > 0 else 0
+        ck_bytes = self.be.nbytes(tab)
+        c = c0
+        while c != stop and not (best is not None and best[0] <= max(lower, 0)):
+            c1 = self._next_ckpt(c, stop)
+            pos = self._positions(c, c1)
+            keep = [0] * (len(pos) - 1) + [1]
+            joins = None
+            if join_with is not None:
+                joins = [(join_with.table(self._cut_of(p), cache), self.tr.tmask[self._cut_of(p)]) for p in pos]
+            rows, masks, weights = self._rows(pos, keep, joins)
+            out, kept, res = self.be.walk(tab, rows, masks, weights, self.K, self.max_states)
+            self.steps_done += len(pos)
+            for k, p in enumerate(pos):
+                cut = self._cut_of(p)
+                self.counts[cut] = int(out[k, 0])
+                self.changed_counts[cut] = int(out[k, 1])
+                self.peak = max(self.peak, int(out[k, 0]), int(out[k, 1]), int(out[k, 5]))
+                if join_with is not None and int(res[k]) != 0xFFFFFFFFFFFFFFFF:
+                    total = int(res[k]) >> 56
+                    if best is None or total < best[0]:
+                        best = (total, cut, int(res[k]) & KEYMASK)
+            tab = kept[len(pos) - 1]
+            c = c1
+            self.ckpt[c] = tab
+            ck_bytes += self.be.nbytes(tab)
+            self.peak_bytes = max(self.peak_bytes, ck_bytes + 8 * int(out[:, 5].max()))
+            if self.max_states is not None and self.peak > self.max_states:
+                raise BudgetExceeded("%d states before cut %d" % (self.peak, c), "states")
+            if self.deadline is not None and time.monotonic() > self.deadline:
+                raise BudgetExceeded("deadline at cut %d" % c, "deadline")
+        return c, best
+
     def _walk(self, cut, tab, stop, want_changed=False):
         rng = range(cut, stop) if self.direction > 0 else range(cut - 1, stop - 1, -1)
         for p in rng:
@@ -442,6 +621,8 @@ class Sweep:
     def run(self, on_cut=None):
         """Full sweep keeping checkpoints and per-cut counts; on_cut(cut, table, changed, extra) may
         return True to stop.  Returns the last cut reached."""
+        if on_cut is None and isinstance(self.be, GpuTables):
+            return self._run_walk()[0]
         c0, tab = self.first()
         self.ckpt[c0] = tab
         self.counts[c0] = self.changed_counts[c0] = 1
@@ -470,6 +651,8 @@ class Sweep:
 
     def segment(self, lo, hi):
         """Tables at the cuts lo..hi, recomputed from the nearest checkpoint: {cut: table}."""
+        if isinstance(self.be, GpuTables):
+            return self._segment_walk(lo, hi)
         out = {}
         if self.direction > 0:
             c0 = max(c for c in self.ckpt if c <= lo)
@@ -487,6 +670,27 @@ class Sweep:
             for c, tab, _, _ in self._walk(c0, tab, lo):
                 if c <= hi:
                     out[c] = self.be.persistent(tab)
+        return out
+
+    def _segment_walk(self, lo, hi):
+        if self.direction > 0:
+            c0 = max(c for c in self.ckpt if c <= lo)
+            stop = hi
+        else:
+            c0 = min(c for c in self.ckpt if c >= hi)
+            stop = lo
+        out = {}
+        tab = self.ckpt[c0]
+        if lo <= c0 <= hi:
+            out[c0] = tab
+        pos = self._positions(c0, stop)
+        if pos:
+            keep = [1 if lo <= self._cut_of(p) <= hi else 0 for p in pos]
+            rows, masks, weights = self._rows(pos, keep)
+            _, kept, _ = self.be.walk(tab, rows, masks, weights, self.K, self.max_states)
+            for k, p in enumerate(pos):
+                if keep[k]:
+                    out[self._cut_of(p)] = kept[k]
         return out
 
     def table(self, c, cache):
@@ -756,7 +960,17 @@ def query(tr, K, mode="mitm", split=None, use_h=True, witness=True, lower=0, eve
                 best[0] = (r[0], c) + tuple(r[1:])
         return best[0] is not None and best[0][0] <= max(lower, 0)
 
-    fw.run(on_cut=join)
+    if isinstance(fw.be, GpuTables) and isinstance(bw.be, GpuTables):
+        # device walks: the joins of every cut run inside the walk calls
+        _, b = fw._run_walk(join_with=bw, lower=lower)
+        joins[0] = int(sum(fw.changed_counts))
+        if b is not None:
+            total, c, fkey = b
+            bkey = fkey ^ (int(tr.tmask[c]) & KEYMASK)
+            bval = bw.be.lookup(bw.table(c, cache), bkey)
+            best[0] = (total, c, fkey, total - bval, bkey)
+    else:
+        fw.run(on_cut=join)
     cache.clear()
     rec.update(forward_counts=fw.counts, backward_counts=bw.counts, changed_counts=fw.changed_counts,
                peak_states=max(fw.peak, bw.peak), peak_table_bytes=fw.peak_bytes + bw.peak_bytes,
