@@ -279,14 +279,14 @@ def _serve_requests(seed=11):
     dense = [serve.compile_request(k, [pl for _, pl in auto._plans(p, list(range(p.ncols)))])
              for k, p in enumerate(ps)]
     sparse = []
-    for j, n in enumerate([2000, 5000, 10000, 20000, 2000, 5000, 10000, 20000]):
+    for j, n in enumerate([2000, 5000, 10000, 20000]):
         p = synth.circuit_dem(seed=100 + j, rounds=max(4, n // 500), checks=24, ncols=n)
         sparse.append(serve.SparseRequest(1000 + j, p, kmax=30))
-    # interleave: a sparse problem after every 12 dense ones
+    # interleave: a sparse problem after every 24 dense ones
     out, si = [], 0
     for k, r in enumerate(dense):
         out.append(r)
-        if k % 12 == 11 and si < len(sparse):
+        if k % 24 == 23 and si < len(sparse):
             out.append(sparse[si])
             si += 1
     return out + sparse[si:]
@@ -297,12 +297,12 @@ def section_served(args):
     problems (n = 2000-20000, 24 checks per round), served by the persistent-kernel request loop
     with continuous batching, against the plain path (one request at a time), same distances."""
     from tropidist_gb300 import serve
-    res = {"workload": "96 banded instances (widths 10-28, 1-12 logical rows, seed 11) + 8 circuit-style "
-                       "sparse problems (n 2000-20000), Poisson arrivals",
+    res = {"workload": "96 banded instances (widths 10-28, 1-12 logical rows, seed 11) + 4 circuit-style "
+                       "sparse problems (n 2000-20000, 24 checks per round), Poisson arrivals",
            "admission": "dense tables in a persistent-kernel arena of 60 % of free HBM, sparse tables "
                         "against 20 % (80 % in all)", "rates": {}}
     for rate in (20, 2000):
-        arr = serve.poisson_arrivals(104, rate, seed=rate)
+        arr = serve.poisson_arrivals(100, rate, seed=rate)
         r1, w1, peak = serve.serve_persistent(_serve_requests(), arr, budget_frac=0.8, sparse_frac=0.2,
                                               sparse_sms=24, jobs=1 << 21, param_bytes=2 << 30, plans=4096)
         r2, w2 = serve.serve_plain(_serve_requests(), arr)

@@ -75,3 +75,24 @@ def test_persistent_server_reuses_slots_under_a_small_arena():
     done, wall, peak = serve_persistent(reqs, poisson_arrivals(len(reqs), 5000.0, seed=3), arena_bytes=3 * biggest,
                                         jobs=1 << 14, param_bytes=1 << 25, plans=8)
     assert [r.distance for r in done] == alone
+
+
+def test_persistent_server_mixes_sparse_requests():
+    """Circuit-style problems for the sparse DP served beside dense ones: each distance is the one the
+    sparse DP gives alone, and the dense results are unchanged by the mix."""
+    from tropidist_gb300 import auto, sparse_dp, synth
+    from tropidist_gb300.serve import SparseRequest, poisson_arrivals, serve_persistent
+    ps, reqs = _requests(5, 8)
+    sps = [synth.circuit_dem(seed=30 + j, rounds=4, checks=12, ncols=300 + 100 * j) for j in range(3)]
+    alone_sparse = [sparse_dp.distance(p, kmax=30, witness=False)["distance"] for p in sps]
+    alone_dense = [auto.dp_distance(p, list(range(p.ncols)))[0] for p in ps]
+    mixed = reqs[:3] + [SparseRequest(100, sps[0])] + reqs[3:6] + [SparseRequest(101, sps[1])] + reqs[6:] + \
+        [SparseRequest(102, sps[2])]
+    arr = poisson_arrivals(len(mixed), rate=500.0, seed=3)
+    done, wall, peak = serve_persistent(mixed, arr, budget_frac=0.5, sparse_frac=0.1, sparse_sms=16,
+                                        jobs=1 << 16, param_bytes=64 << 20, plans=512)
+    got_dense = [r.distance for r in done if getattr(r, "kind", None) != "sparse"]
+    got_sparse = [r.distance for r in done if getattr(r, "kind", None) == "sparse"]
+    assert got_dense == alone_dense
+    assert got_sparse == alone_sparse
+    assert all(getattr(r, "error", None) is None for r in done)

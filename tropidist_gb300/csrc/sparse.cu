@@ -242,7 +242,7 @@ static int load_bound(BoundParams &B, int on, int K, int ncls, const uint64_t *m
 enum { SW_UPD, SW_SELM, SW_SELB, SW_TMASK, SW_JTAB, SW_JTMASK, SW_EXTRA, SW_CAP, SW_KB, SW_W, SW_WANT, SW_TRUNC,
        SW_KEEP, SW_JLG, SW_NCLS, SW_USEH };
 
-static int lg_for(uint64_t n) {          // index size for up to n states at load <= 1/2 (>= 64 slots)
+__host__ __device__ static int lg_for(uint64_t n) {  // index size for up to n states at load <= 1/2 (>= 64 slots)
     const uint64_t x = 2 * (n ? n : 1) - 1;
     int b = 0;
     while ((x >> b) != 0) b++;
@@ -256,6 +256,186 @@ __global__ void k_sp_join_acc(const unsigned long long *__restrict__ F, uint64_t
         const uint64_t key = x & SP_KEYMASK;
         const uint32_t bv = sp_lookup(Hb, lgb, key ^ tmask);
         if (bv != 255u) atomicMin(result, (((x >> 56) + bv) << 56) | key);
+    }
+}
+
+// ---- small tables: one block runs many steps per launch (no host round trip per column)
+#define SPW_SMALL_MAX 4096              // states per table in the one-block walk
+#define SPW_SMALL_THREADS 1024
+
+struct WalkSmall {
+    const int64_t *spec;                // device copies of the walk's rows, lookahead classes
+    const uint64_t *masks;
+    const int64_t *weights;
+    int stride, K, i0, nsteps;
+    const unsigned long long *A0, *H0;  // the table before step i0
+    uint64_t n0;
+    int lg0, slot0;                     // slot0: scratch slot of that table (-1: outside the scratch)
+    unsigned long long *arr[3], *idx[3], *changed;
+    unsigned long long *arena;
+    uint64_t arena_bytes, used0;
+    int64_t *out;                       // device int64 [nsteps][6]
+    unsigned long long *res;
+    unsigned long long *state;          // out: [0] next step, [1] slot, [2] n, [3] lg, [4] arena used, [5] stop reason
+};
+
+// stop reasons: 1 a table beyond SPW_SMALL_MAX (continue with the per-step path), 2 arena full,
+// 4 index full
+__global__ void __launch_bounds__(SPW_SMALL_THREADS) k_sp_walk_small(const __grid_constant__ WalkSmall P) {
+    __shared__ unsigned long long c_ch, c_out, c_flag;
+    __shared__ BoundParams B;
+    const unsigned long long *curA = P.A0, *curH = P.H0;
+    uint64_t n = P.n0;
+    int lg = P.lg0, cur = P.slot0;
+    uint64_t used = P.used0;
+    int i = P.i0, reason = 0;
+    const unsigned tid = threadIdx.x, NT = blockDim.x;
+    for (; i < P.nsteps; i++) {
+        const int64_t *f = P.spec + (size_t)SPW_FIELDS * i;
+        if (2 * n > SPW_SMALL_MAX) { reason = 1; break; }
+        int os = 0;
+        while (os == cur) os++;
+        const int lgn = lg_for(2 * n);
+        const uint64_t capn = 1ull << lgn;
+        if (tid == 0) {
+            c_ch = c_out = c_flag = 0;
+            B.on = (int)f[SW_USEH];
+            B.ncls = (int)f[SW_NCLS];
+            B.K = P.K;
+            B.extra = f[SW_EXTRA];
+            B.tmask = (uint64_t)f[SW_TMASK];
+        }
+        for (int c = tid; c < (int)f[SW_NCLS] && c < SP_MAXCLS; c += NT) {
+            B.mask[c] = P.masks[(size_t)P.stride * i + c];
+            B.w[c] = P.weights[(size_t)P.stride * i + c];
+        }
+        unsigned long long *H = P.idx[os];
+        for (uint64_t k = tid; k < capn; k += NT) H[k] = SP_EMPTY;
+        __syncthreads();
+        const uint64_t upd = (uint64_t)f[SW_UPD] & SP_KEYMASK, selm = (uint64_t)f[SW_SELM], selb = (uint64_t)f[SW_SELB];
+        const uint64_t clr = ~selm & SP_KEYMASK;
+        const int cap = (int)f[SW_CAP], kb = (int)f[SW_KB], w = (int)f[SW_W];
+        const bool want = f[SW_WANT] != 0;
+        for (uint64_t k = tid; k < n; k += NT) {
+            const unsigned long long x = curA[k];
+            const uint64_t key = x & SP_KEYMASK;
+            const uint32_t v = (uint32_t)(x >> 56);
+            if ((key & selm) == selb) {
+                const uint64_t k2 = key & clr;
+                if ((int)v <= cap && sp_keep(B, k2, v)) {
+                    const int r = sp_insert_min(H, lgn, k2, v);
+                    if (r < 0) atomicOr(&c_flag, 1ull);
+                }
+            }
+            if (upd && (int)v < cap) {
+                const uint64_t t = key ^ upd;
+                const uint32_t vc = v + (uint32_t)w;
+                if ((t & selm) == selb) {
+                    const uint64_t t2 = t & clr;
+                    if ((int)vc <= cap && sp_keep(B, t2, vc)) {
+                        const uint32_t vo = sp_lookup(curH, lg, t);
+                        const bool hit = vo != 255u;
+                        if (vc < vo && want) P.changed[atomicAdd(&c_ch, 1ull)] = t2 | ((unsigned long long)vc << 56);
+                        if (hit || kb < 0 || (int)vc < kb) {
+                            const int r = sp_insert_min(H, lgn, t2, vc);
+                            if (r < 0) atomicOr(&c_flag, 1ull);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        unsigned long long *A = P.arr[os];
+        for (uint64_t k = tid; k < capn; k += NT) {
+            const unsigned long long x = H[k];
+            if (x != SP_EMPTY) A[atomicAdd(&c_out, 1ull)] = x;
+        }
+        __syncthreads();
+        if (c_flag) { reason = 4; break; }
+        uint64_t nn = c_out;
+        const uint64_t nch = want ? c_ch : 0;
+        __syncthreads();                // every thread has read the counters before they are reused
+        const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[SW_JTAB]);
+        const uint64_t jt = (uint64_t)f[SW_JTMASK] & SP_KEYMASK;
+        const int jlg = (int)f[SW_JLG];
+        unsigned long long best = ~0ull;
+        if (jH)
+            for (uint64_t k = tid; k < nch; k += NT) {
+                const unsigned long long x = P.changed[k];
+                const uint32_t bv = sp_lookup(jH, jlg, (x & SP_KEYMASK) ^ jt);
+                if (bv != 255u) best = min(best, (((x >> 56) + bv) << 56) | (x & SP_KEYMASK));
+            }
+        int64_t *o = P.out + 6 * (size_t)i;
+        if (tid == 0) o[5] = (int64_t)nn;
+        const unsigned long long *nA = A, *nH = H;
+        int nlg = lgn, ns = os;
+        if (f[SW_TRUNC] >= 0) {
+            if (jH)
+                for (uint64_t k = tid; k < nn; k += NT) {
+                    const unsigned long long x = A[k];
+                    const uint32_t bv = sp_lookup(jH, jlg, (x & SP_KEYMASK) ^ jt);
+                    if (bv != 255u) best = min(best, (((x >> 56) + bv) << 56) | (x & SP_KEYMASK));
+                }
+            int ts = 0;
+            while (ts == os) ts++;
+            const int lgt = lg_for(nn);
+            unsigned long long *T = P.idx[ts], *TA = P.arr[ts];
+            for (uint64_t k = tid; k < (1ull << lgt); k += NT) T[k] = SP_EMPTY;
+            if (tid == 0) c_out = 0;
+            __syncthreads();
+            const int below = (int)f[SW_TRUNC];
+            for (uint64_t k = tid; k < nn; k += NT) {
+                const unsigned long long x = A[k];
+                if ((int)(x >> 56) >= below) continue;
+                if (sp_insert_min(T, lgt, x & SP_KEYMASK, (uint32_t)(x >> 56)) < 0) atomicOr(&c_flag, 1ull);
+                TA[atomicAdd(&c_out, 1ull)] = x;
+            }
+            __syncthreads();
+            nn = c_out;
+            nA = TA;
+            nH = T;
+            nlg = lgt;
+            ns = ts;
+        }
+        if (jH && best != ~0ull) atomicMin(P.res + i, best);
+        int64_t a_off = -1, h_off = -1;
+        if (f[SW_KEEP]) {
+            const int lgk = lg_for(nn);
+            const uint64_t ab = (8 * nn + 255) / 256 * 256, ib = 8ull << lgk;
+            if (used + ab + ib > P.arena_bytes) { reason = 2; break; }
+            unsigned long long *kA = P.arena + used / 8, *kH = P.arena + (used + ab) / 8;
+            for (uint64_t k = tid; k < nn; k += NT) kA[k] = nA[k];
+            for (uint64_t k = tid; k < (1ull << lgk); k += NT) kH[k] = SP_EMPTY;
+            __syncthreads();
+            for (uint64_t k = tid; k < nn; k += NT)
+                if (sp_insert_min(kH, lgk, kA[k] & SP_KEYMASK, (uint32_t)(kA[k] >> 56)) < 0) atomicOr(&c_flag, 1ull);
+            a_off = (int64_t)used;
+            h_off = (int64_t)(used + ab);
+            used += ab + ib;
+            if (tid == 0) o[4] = lgk;   // the working index stays the table's index for the next step
+        } else if (tid == 0) {
+            o[4] = nlg;
+        }
+        if (tid == 0) {
+            o[0] = (int64_t)nn;
+            o[1] = (int64_t)nch;
+            o[2] = a_off;
+            o[3] = h_off;
+        }
+        curA = nA;
+        curH = nH;
+        n = nn;
+        lg = nlg;
+        cur = ns;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        P.state[0] = (unsigned long long)i;
+        P.state[1] = (unsigned long long)(long long)cur;
+        P.state[2] = n;
+        P.state[3] = (unsigned long long)lg;
+        P.state[4] = used;
+        P.state[5] = (unsigned long long)reason;
     }
 }
 
@@ -383,7 +563,74 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
     int lg = lg0, cur = -1;
     uint64_t used = 0;
     need[0] = need[1] = 0;
+    // device copies of the rows for the one-block walk of small tables
+    static thread_local uint8_t *dbuf = nullptr;
+    static thread_local size_t dbuf_bytes = 0;
+    const size_t b_spec = 8 * (size_t)SPW_FIELDS * nsteps, b_cls = 8 * (size_t)stride * nsteps;
+    const size_t b_out = 8 * 6 * (size_t)nsteps, b_all = b_spec + 2 * b_cls + b_out + 64;
+    const bool small_ok = cap_n >= SPW_SMALL_MAX && nsteps > 0;
+    if (small_ok) {
+        if (dbuf_bytes < b_all) {
+            if (dbuf) cudaFree(dbuf);
+            dbuf = nullptr;
+            dbuf_bytes = 0;
+            if (cudaMalloc(&dbuf, b_all) != cudaSuccess) {
+                cudaGetLastError();
+                return set_error(TG_ERR_NOMEM, "walk rows");
+            }
+            dbuf_bytes = b_all;
+        }
+        e = cuda_check(cudaMemcpyAsync(dbuf, spec, b_spec, cudaMemcpyHostToDevice, st), "walk rows");
+        if (!e && b_cls) e = cuda_check(cudaMemcpyAsync(dbuf + b_spec, masks, b_cls, cudaMemcpyHostToDevice, st), "walk rows");
+        if (!e && b_cls) e = cuda_check(cudaMemcpyAsync(dbuf + b_spec + b_cls, weights, b_cls, cudaMemcpyHostToDevice, st), "walk rows");
+        if (e) return e;
+    }
     for (int i = 0; i < nsteps; i++) {
+        if (small_ok && 2 * n <= SPW_SMALL_MAX) {
+            WalkSmall S;
+            S.spec = reinterpret_cast<const int64_t *>(dbuf);
+            S.masks = reinterpret_cast<const uint64_t *>(dbuf + b_spec);
+            S.weights = reinterpret_cast<const int64_t *>(dbuf + b_spec + b_cls);
+            S.stride = stride;
+            S.K = K;
+            S.i0 = i;
+            S.nsteps = nsteps;
+            S.A0 = curA;
+            S.H0 = curH;
+            S.n0 = n;
+            S.lg0 = lg;
+            S.slot0 = cur;
+            for (int k = 0; k < 3; k++) { S.arr[k] = W.arr[k]; S.idx[k] = W.idx[k]; }
+            S.changed = W.changed;
+            S.arena = static_cast<unsigned long long *>(arena);
+            S.arena_bytes = arena ? arena_bytes : 0;
+            S.used0 = used;
+            S.out = reinterpret_cast<int64_t *>(dbuf + b_spec + 2 * b_cls);
+            S.res = res;
+            unsigned long long *dstate = reinterpret_cast<unsigned long long *>(dbuf + b_spec + 2 * b_cls + b_out);
+            S.state = dstate;
+            k_sp_walk_small<<<1, SPW_SMALL_THREADS, 0, st>>>(S);
+            e = cuda_check(cudaGetLastError(), "small walk");
+            if (!e) e = cuda_check(cudaMemcpyAsync(hb, dstate, 48, cudaMemcpyDeviceToHost, st), "small walk state");
+            if (!e) e = cuda_check(cudaMemcpyAsync(out + 6 * (size_t)i, S.out + 6 * (size_t)i, 48 * (size_t)(nsteps - i),
+                                                   cudaMemcpyDeviceToHost, st), "small walk rows");
+            if (!e) e = cuda_check(cudaStreamSynchronize(st), "small walk sync");
+            if (e) return e;
+            const int i1 = (int)hb[0];
+            const int reason = (int)hb[5];
+            if (i1 > i) {
+                cur = (int)(long long)hb[1];
+                n = hb[2];
+                lg = (int)hb[3];
+                used = hb[4];
+                curA = W.arr[cur];
+                curH = W.idx[cur];
+            }
+            if (reason == 2) { need[1] = (int64_t)(2 * arena_bytes + (1 << 20)); return i1; }
+            if (reason == 4) return set_error(TG_ERR_STATE, "walk table overflow");
+            if (i1 >= nsteps) break;
+            i = i1;
+        }
         const int64_t *f = spec + (size_t)SPW_FIELDS * i;
         int64_t *o = out + 6 * (size_t)i;
         if (2 * n > cap_n) { need[0] = (int64_t)(2 * n); return i; }

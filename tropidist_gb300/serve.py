@@ -11,8 +11,9 @@ PersistentServer   the same interface on one long-lived persistent kernel (csrc/
                    admitted plans are handed to the running kernel through a device mailbox and
                    their passes are interleaved with the plans already in flight at tile-range
                    granularity, with no kernel launches per pass.  Sparse requests (SparseRequest:
-                   circuit-style problems for the sparse Rank DP) run beside it on their own stream
-                   and SMs, admitted against their share of the memory budget.
+                   circuit-style problems for the sparse Rank DP) run beside it on worker threads
+                   with their own streams and SMs, each worker admitting one request at a time
+                   against its share of the memory budget.
 serve_plain        the same requests one at a time on one stream (the plain GPU path).
 poisson_arrivals   seeded exponential inter-arrival times.
 Latency = completion time - arrival time; p50 / p99 and solves/s are computed by `summarize`.
@@ -260,7 +261,7 @@ class PersistentServer:
     polling, and a request completes when all of its plans have."""
 
     def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192,
-                 sparse_frac=0.0, sparse_sms=0):
+                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2):
         import ctypes
         import torch
         from . import _lib
@@ -292,11 +293,12 @@ class PersistentServer:
         self.thread.start()
         # sparse requests: a worker on its own stream, admitted one at a time against the sparse share
         # of the memory budget
-        self.sparse_budget = int(sparse_frac * free)
+        self.sparse_budget = int(sparse_frac * free) // max(1, sparse_workers)
         self.sparse_q = collections.deque()
         self.sparse_wake = threading.Event()
-        self.sparse_thread = threading.Thread(target=self._sparse_loop, daemon=True)
-        self.sparse_thread.start()
+        self.sparse_threads = [threading.Thread(target=self._sparse_loop, daemon=True) for _ in range(sparse_workers)]
+        for t in self.sparse_threads:
+            t.start()
 
     def submit(self, req, arrival=None):
         req.arrival = time.perf_counter() if arrival is None else arrival
@@ -410,7 +412,8 @@ class PersistentServer:
         self.stop_flag = True
         self.thread.join(timeout=10)
         self.sparse_wake.set()
-        self.sparse_thread.join(timeout=60)
+        for t in self.sparse_threads:
+            t.join(timeout=60)
         if self.handle:
             self.L.tg_server_free(self.handle)
             self.handle = None

@@ -498,6 +498,7 @@ class Sweep:
         self.peak = 0
         self.peak_bytes = 0
         self.steps_done = 0
+        self._all = None
 
     def first(self):
         return (0 if self.direction > 0 else self.tr.N), self.be.start()
@@ -521,11 +522,33 @@ class Sweep:
     def _rows(self, positions, keep, joins=None):
         """Spec rows of tg_sp_walk for the steps at `positions` (as _step), with lookahead arrays;
         keep: per step 0/1; joins: per step None or (backward table, tmask)."""
+        if getattr(self, "_all", None) is None:
+            self._all = self._all_rows()
+        rows0, masks0, weights0 = self._all
+        pos = np.asarray(positions, dtype=np.int64)
+        rows = rows0[pos].copy()
+        rows[:, 12] = np.asarray(keep, dtype=np.int64)
+        if joins is not None:
+            rows[:, 10] = 1
+            for k, j in enumerate(joins):
+                if j is not None:
+                    btab, jtm = j
+                    rows[k, 4] = btab.H.data_ptr()
+                    rows[k, 5] = int(jtm) & KEYMASK
+                    rows[k, 13] = btab.lg
+        return rows, masks0[pos], weights0[pos]
+
+    def _all_rows(self):
+        """Spec rows of every step position of this sweep (without keep / join columns)."""
         tr, fwd = self.tr, self.direction > 0
-        m = len(positions)
-        rows = np.zeros((m, 16), dtype=np.int64)
-        hds = []
-        for k, p in enumerate(positions):
+        N = tr.N
+        rows = np.zeros((max(1, N), 16), dtype=np.int64)
+        stride = 1
+        if self.hd:
+            stride = max([len(h[0]) for h in self.hd] + [1])
+        masks = np.zeros((max(1, N), stride), dtype=U64)
+        weights = np.zeros((max(1, N), stride), dtype=np.int64)
+        for p in range(N):
             cut = p + 1 if fwd else p
             sm, sb = (tr.fsel_mask[p], tr.fsel_bits[p]) if fwd else (tr.bsel_mask[p], tr.bsel_bits[p])
             cap, kb = self.caps[cut], -1
@@ -533,22 +556,12 @@ class Sweep:
                 cap = kb = self.caps[p]
             trunc = self.caps[cut] if (self.frontier and self.caps[cut] < cap) else -1
             hd = self.hd[cut] if self.hd else None
-            hds.append(hd)
-            jt, jtm, jlg = 0, 0, 0
-            if joins is not None and joins[k] is not None:
-                btab, jtm = joins[k]
-                jt, jlg = btab.H.data_ptr(), btab.lg
-            rows[k] = [int(tr.col[p]) & KEYMASK, int(sm), int(sb), int(tr.tmask[cut]) & KEYMASK, jt,
-                       int(jtm) & KEYMASK, int(hd[2]) if hd is not None else 0, int(cap), int(kb), int(tr.cw[p]),
-                       1 if joins is not None else 0, int(trunc), int(keep[k]), int(jlg),
+            rows[p] = [int(tr.col[p]) & KEYMASK, int(sm), int(sb), int(tr.tmask[cut]) & KEYMASK, 0, 0,
+                       int(hd[2]) if hd is not None else 0, int(cap), int(kb), int(tr.cw[p]), 0, int(trunc), 0, 0,
                        len(hd[0]) if hd is not None else 0, 1 if hd is not None else 0]
-        stride = max([len(h[0]) for h in hds if h is not None] + [1])
-        masks = np.zeros((m, stride), dtype=U64)
-        weights = np.zeros((m, stride), dtype=np.int64)
-        for k, hd in enumerate(hds):
             if hd is not None and len(hd[0]):
-                masks[k, :len(hd[0])] = hd[0]
-                weights[k, :len(hd[1])] = hd[1]
+                masks[p, :len(hd[0])] = hd[0]
+                weights[p, :len(hd[1])] = hd[1]
         return rows, masks, weights
 
     def _positions(self, c, stop):
