@@ -48,6 +48,12 @@ uint64_t dp16_select(uint16_t *T, uint64_t n, int pos, int target);
  * ckpt_ops: op counts k after which the table (2^width(k) entries) is copied to ckpt_bufs[i]. */
 void *tg_dense_plan(const int64_t *ops, int64_t nops, int entry_bytes, const int64_t *ckpt_ops,
                     int64_t nckpt, int *status);
+/* a plan of ops that follow a table of width w_start (canonical order, put in buffer a by the
+ * caller before tg_dense_execute; no counterpart in the reference, which never restarts a sweep); it
+ * may end at any width, with its final table (canonical order) in the final buffer.  Used to
+ * recompute segments between checkpoints for the witness traceback. */
+void *tg_dense_plan_from(const int64_t *ops, int64_t nops, int entry_bytes, int w_start, const int64_t *ckpt_ops,
+                         int64_t nckpt, int *status);
 int tg_dense_plan_info(void *plan, int64_t *info, int ninfo);
 /* info: peak_bits, segments, fused passes, shared-memory sweeps, final buffer (0 a / 1 b),
  *       update ops, pass bytes, sweep bytes */

@@ -251,3 +251,26 @@ def test_full_width_schedules_agree():
         del tabs
     assert res[0][0] == res[1][0] and res[0][1] == res[1][1]
     assert torch.equal(res[0][2], res[1][2])
+
+
+@pytest.mark.parametrize("case", [(60, 120, 14, 3, None), (80, 160, 16, 5, None), (60, 120, 12, 7, (1, 2, 3))])
+def test_witness_traceback_on_device(case):
+    """dp_witness: device checkpoints and a bisection traceback give a logical of the distance's
+    weight (zero syndrome, the observable flipped), small budgets forcing several checkpoints."""
+    from tropidist_gb300 import auto, synth
+    from tropidist_gb300.problem import verify_witness
+    m, n, win, seed, wts = case
+    p = synth.banded(m, n, win, seed=seed, nobs=2)
+    if wts is not None:
+        import random
+        rng = random.Random(seed)
+        p.weights = [rng.choice(wts) for _ in range(p.ncols)]
+    order = list(range(p.ncols))
+    best, per = auto.dp_distance(p, order)
+    for budget in (None, 1 << 16):
+        r = auto.dp_witness(p, order, budget_bytes=budget, leaf=4)
+        assert r["distance"] == best
+        cols = r["witness"]
+        assert verify_witness(p, cols, r["observable"])
+        w = sum(p.weights[j] for j in cols) if getattr(p, "weights", None) is not None else len(cols)
+        assert w == best

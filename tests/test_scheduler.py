@@ -167,3 +167,34 @@ def test_random_checkpoint_sets(lib):
         assert v == want
         for k, t in zip(ks, tabs):
             assert np.array_equal(t, tabs_ref[k - 1]), (trial, k)
+
+
+def test_plans_from_a_given_table(lib):
+    """Plans that start from a table of the sweep (tg_dense_plan_from) reproduce the oracle's table
+    at the end of any op range, under every tuning (emulated on the host)."""
+    import ctypes
+    from tropidist_gb300 import kernel
+    rng = random.Random(11)
+    for tune in TUNINGS[:3]:
+        lib.tg_dense_set_tuning(*tune)
+        p = synth.banded(60, 120, 14, seed=rng.randrange(1000))
+        plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+        if not plan.feasible:
+            continue
+        enc = plan.encode()
+        n = len(plan.ops)
+        for _ in range(6):
+            lo = rng.randrange(0, n - 1)
+            hi = rng.randrange(lo + 1, n + 1)
+            t_lo = od.table_after(plan, lo)
+            want = od.table_after(plan, hi)
+            cp = kernel.CompiledPlan(None, "u8", (), w_start=int(np.log2(len(t_lo))) if lo else 0, ops=enc[lo:hi])
+            size = 1 << max(cp.peak_bits, 1)
+            a = np.zeros(size, dtype=np.uint8)
+            b = np.zeros(size, dtype=np.uint8)
+            a[:len(t_lo)] = t_lo
+            arr = (ctypes.c_void_p * 1)()
+            _lib.check(lib.tg_debug_emulate_dense(cp.handle, a.ctypes.data, b.ctypes.data, arr))
+            got = (b if cp.final_buf else a)[:len(want)]
+            assert np.array_equal(got, want), (tune, lo, hi)
+            cp.free()

@@ -90,6 +90,7 @@ def _declare(L):
         "dp16_expand_update": (ci, [vp, u64, u64, ci]),
         "dp16_select": (u64, [vp, u64, ci, ci]),
         "tg_dense_plan": (vp, [vp, i64, ci, vp, i64, c.POINTER(ci)]),
+        "tg_dense_plan_from": (vp, [vp, i64, ci, ci, vp, i64, c.POINTER(ci)]),
         "tg_dense_plan_info": (ci, [vp, vp, ci]),
         "tg_dense_plan_segments": (ci, [vp, vp, i64]),
         "tg_dense_plan_free": (None, [vp]),

@@ -106,3 +106,123 @@ def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
         if v is not None and (best is None or v < best):
             best = v
     return best, per
+
+
+# ---------------------------------------------------------------------- witness
+def _widths(ops):
+    """Table width before every op and after the last one."""
+    w, out = 0, [0]
+    for op in ops:
+        w += 1 if op[0] == "expand" else -1 if op[0] == "select" else 0
+        out.append(w)
+    return out
+
+
+def dp_witness(p, order, obs=None, dtype=None, budget_bytes=None, leaf=16):
+    """Columns (problem indices) of a minimum-weight solution, with its weight and observable:
+    {"distance", "witness", "observable"} (cdist/auto.py:126-182), or None if no logical exists.
+
+    The reference keeps the table before every update and walks back through them.  Here the
+    tables stay on the device: the sweep keeps canonical tables at checkpoints (as many as fit
+    `budget_bytes`, default a quarter of the free device memory), and each segment between two
+    checkpoints is walked back by bisection — the table at the segment's midpoint is recomputed
+    from its start by a plan that begins with that table (tg_dense_plan_from), the second half is
+    traced first — so only O(log segment) tables exist at once.  A leaf of at most `leaf` ops is
+    recomputed with a table after every op; the walk reads two entries per update op."""
+    import torch
+    from . import device
+    dtype = dtype or _dtype_for(p)
+    eb = kernel.entry_bytes(dtype)
+    dt = torch.uint8 if eb == 1 else torch.int16
+    inf = kernel.INF if eb == 1 else 65535
+    best = None
+    for i, plan in _plans(p, order):
+        if obs is not None and i != obs:
+            continue
+        if not plan.feasible:
+            continue
+        v, _ = kernel.run_plan(plan, dtype=dtype)
+        if v is not None and (best is None or v < best[0]):
+            best = (v, i, plan)
+    if best is None:
+        return None
+    value, i, plan = best
+    ops, enc = plan.ops, plan.encode()
+    n = len(ops)
+    wid = _widths(ops)
+    col_of = {}
+    u = 0
+    for k, op in enumerate(ops):
+        if op[0] == "update":
+            col_of[k] = order[plan.columns[u]]
+            u += 1
+    if budget_bytes is None:
+        budget_bytes = device.free_bytes() // 4
+    step = max(leaf, 1)
+    while True:
+        cks = list(range(step, n, step))
+        if sum(eb << wid[c] for c in cks) <= budget_bytes or step >= n:
+            break
+        step *= 2
+    cks = [c for c in range(step, n, step)]
+    cp = kernel.CompiledPlan(plan, dtype, cks)
+    a, b = cp.buffers()
+    ck_tabs = [torch.empty(1 << wid[c], dtype=dt, device="cuda") for c in cp.ckpts]
+    cp.execute(a, b, [t.view(torch.uint8) for t in ck_tabs])
+    cp.free()
+    tabs = {0: torch.zeros(1, dtype=dt, device="cuda")}
+    for c, t in zip(cp.ckpts, ck_tabs):
+        tabs[int(c)] = t
+    del a, b
+
+    def entry(t, s):
+        x = int(t[s].item())
+        return x & 0xFFFF if eb == 2 else x
+
+    def run_from(t0, lo, hi, keep_all=False):
+        """Tables after ops lo..hi-1 from table t0 (before op lo): the last one, or all of them."""
+        sub = enc[lo:hi]
+        ck = list(range(1, hi - lo)) if keep_all else []
+        c2 = kernel.CompiledPlan(None, dtype, ck, w_start=wid[lo], ops=sub)
+        n_a = max(1 << max(wid[lo:hi + 1]), 1)
+        a2 = torch.empty(n_a, dtype=dt, device="cuda")
+        b2 = torch.empty(n_a, dtype=dt, device="cuda")
+        a2[:t0.numel()].copy_(t0)
+        outs = [torch.empty(1 << wid[lo + k], dtype=dt, device="cuda") for k in ck]
+        c2.execute(a2.view(torch.uint8), b2.view(torch.uint8), [o.view(torch.uint8) for o in outs])
+        last = (b2 if c2.final_buf else a2)[:1 << wid[hi]].clone()
+        c2.free()
+        return (outs + [last]) if keep_all else last
+
+    used = []
+
+    def trace(lo, hi, t_lo, s, v):
+        if hi - lo <= leaf:
+            after = run_from(t_lo, lo, hi, keep_all=True) if hi - lo > 1 else []
+            before = [t_lo] + after[:-1] if after else [t_lo]
+            for k in range(hi - 1, lo - 1, -1):
+                op, t = ops[k], before[k - lo]
+                if op[0] == "select":
+                    pos, tgt = op[1], op[2]
+                    s = ((s >> pos) << (pos + 1)) | (tgt << pos) | (s & ((1 << pos) - 1))
+                elif op[0] == "expand":
+                    assert s >> wid[k] == 0, "traceback through an INF half"
+                elif entry(t, s) != v:
+                    mask, w = op[1], (op[2] if len(op) > 2 else 1)
+                    s ^= mask
+                    v -= w
+                    assert entry(t, s) == v, "traceback lost the path"
+                    used.append(col_of[k])
+            return s, v
+        mid = (lo + hi) // 2
+        t_mid = run_from(t_lo, lo, mid)
+        s, v = trace(mid, hi, t_mid, s, v)
+        del t_mid
+        return trace(lo, mid, t_lo, s, v)
+
+    bounds = [0] + [int(c) for c in cp.ckpts] + [n]
+    s, v = 0, value
+    for lo, hi in reversed(list(zip(bounds, bounds[1:]))):
+        s, v = trace(lo, hi, tabs[lo], s, v)
+    assert s == 0 and v == 0, (s, v)
+    return {"distance": value, "witness": sorted(used), "observable": i}

@@ -310,10 +310,11 @@ __global__ void k_single_op(const E *__restrict__ src, E *__restrict__ dst, int 
 }
 
 // ------------------------------------------------------------------ host scheduler
-static int parse_ops(const int64_t *ops, int64_t nops, int eb, std::vector<HostOp> &out, int &peak, int &final_w) {
+static int parse_ops(const int64_t *ops, int64_t nops, int eb, std::vector<HostOp> &out, int &peak, int &final_w,
+                     int w0 = 0) {
     out.resize(nops);
-    int w = 0;
-    peak = 0;
+    int w = w0;
+    peak = w0;
     for (int64_t i = 0; i < nops; i++) {
         HostOp o{(int)ops[3 * i], (uint64_t)ops[3 * i + 1], ops[3 * i + 2]};
         if (o.code == 0) {
@@ -697,13 +698,17 @@ struct RowInfo {
     }
 };
 
-static void row_info(const std::vector<HostOp> &hops, RowInfo &R) {
+static void row_info(const std::vector<HostOp> &hops, RowInfo &R, int w0 = 0) {
     const int64_t n = (int64_t)hops.size();
     R.upd_rows.assign(n, {});
     R.sel_row.assign(n, -1);
     R.exp_row.assign(n, -1);
     std::vector<int> canon;
     int next = 0;
+    for (; next < w0; next++) {     // rows of the start table
+        canon.push_back(next);
+        R.uses.emplace_back();
+    }
     for (int64_t i = 0; i < n; i++) {
         const HostOp &o = hops[i];
         if (o.code == 0) {
@@ -723,12 +728,15 @@ static void row_info(const std::vector<HostOp> &hops, RowInfo &R) {
 
 
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt,
-                     DensePlan &P) {
+                     DensePlan &P, int w_start, bool open_end) {
     std::vector<HostOp> hops;
     int peak = 0, final_w = 0;
-    int e = parse_ops(ops, nops, eb, hops, peak, final_w);
+    if (w_start < 0 || w_start > 40) return set_error(TG_ERR_ARG, "start width out of range");
+    int e = parse_ops(ops, nops, eb, hops, peak, final_w, w_start);
     if (e) return e;
-    if (final_w != 0) return set_error(TG_ERR_ARG, "op stream does not end at width 0");
+    if (final_w != 0 && !open_end) return set_error(TG_ERR_ARG, "op stream does not end at width 0");
+    P.w_start = w_start;
+    P.final_w = final_w;
     const int CB = eb == 1 ? 4 : 3;
     const int DMAX = eb == 1 ? g_dmax8 : g_dmax16;
     const int SWB = eb == 1 ? g_sweep_bits8 : g_sweep_bits16;
@@ -744,10 +752,12 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
     std::vector<char> is_ckpt(nops + 1, 0);
     for (auto c : P.ckpt_ops) is_ckpt[c] = 1;
     RowInfo RI;
-    row_info(hops, RI);
+    row_info(hops, RI, w_start);
 
     std::vector<int> canon;    // canonical order: position -> row (the positions the ops refer to)
     std::vector<int> phys;     // physical order of the table in memory
+    for (int r = 0; r < w_start; r++) canon.push_back(r);
+    phys = canon;
     int64_t i = 0;
     int buf = 0;
     auto apply_canon = [&](int64_t k, std::vector<int> &c) {
@@ -933,7 +943,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             SweepParams &sp = S.sp;
             memset(&sp, 0, sizeof(sp));
             sp.w_in = w_in;
-            sp.has_in = i > 0 ? 1 : 0;
+            sp.has_in = (i > 0 || w_start > 0) ? 1 : 0;
             sp.max_bits = SWB;
             int w = w_in;
             int64_t j = i;
@@ -1057,7 +1067,9 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             }
         }
         buf ^= 1;
-        if (is_ckpt[S.op_end] && phys != canon) {
+        // checkpoints and the end of a plan that ends with a table are in canonical order
+        const bool end_table = open_end && S.op_end == nops;
+        if ((is_ckpt[S.op_end] || end_table) && phys != canon) {
             P.segs.push_back(S);
             Seg R;
             R.w_in = (int)canon.size();
@@ -1345,7 +1357,7 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
     const uint32_t INF = Entry<E>::INF;
     E *bufs[2] = {a, b};
     int cur = 0;
-    a[0] = 0;
+    if (P.w_start == 0) a[0] = 0;      // a plan from a given table finds it in a
     for (const Seg &S : P.segs) {
         E *src = bufs[cur], *dst = bufs[cur ^ 1];
         if (S.kind == 2) {
@@ -1571,6 +1583,24 @@ void *tg_dense_plan(const int64_t *ops, int64_t nops, int entry_bytes, const int
     return P;
 }
 
+// A plan of the ops that follow a table of width w_start (canonical order, given by the caller in
+// buffer a at execution); it may end at any width, with its final table in canonical order.
+// For recomputing segments of a sweep from a checkpoint (the witness traceback).
+void *tg_dense_plan_from(const int64_t *ops, int64_t nops, int entry_bytes, int w_start, const int64_t *ckpt_ops,
+                         int64_t nckpt, int *status) {
+    int st = TG_OK;
+    DensePlan *P = nullptr;
+    if (entry_bytes != 1 && entry_bytes != 2) st = set_error(TG_ERR_ARG, "entry_bytes must be 1 or 2");
+    else if (nops < 0 || (nops > 0 && !ops) || nckpt < 0 || (nckpt > 0 && !ckpt_ops)) st = set_error(TG_ERR_ARG, "bad op stream");
+    else {
+        P = new DensePlan();
+        st = build_dense_plan(ops, nops, entry_bytes, ckpt_ops, nckpt, *P, w_start, true);
+        if (st) { delete P; P = nullptr; }
+    }
+    if (status) *status = st;
+    return P;
+}
+
 int tg_dense_plan_info(void *plan, int64_t *info, int ninfo) {
     if (!plan || !info) return set_error(TG_ERR_ARG, "null plan");
     const DensePlan &P = *static_cast<DensePlan *>(plan);
@@ -1624,10 +1654,9 @@ int tg_dense_execute(void *plan, void *buf_a, void *buf_b, void **ckpt_bufs, voi
     if (!plan || !buf_a || !buf_b) return set_error(TG_ERR_ARG, "null plan or buffer");
     const DensePlan &P = *static_cast<DensePlan *>(plan);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // the start table {0: 0} in buffer a
-    int e;
-    if (P.eb == 1) e = cuda_check(cudaMemsetAsync(buf_a, 0, 1, st), "init");
-    else e = cuda_check(cudaMemsetAsync(buf_a, 0, 2, st), "init");
+    // the start table {0: 0} in buffer a (a plan from a given table finds it there)
+    int e = TG_OK;
+    if (P.w_start == 0) e = cuda_check(cudaMemsetAsync(buf_a, 0, P.eb, st), "init");
     if (e) return e;
     if (P.nops == 0) return TG_OK;
     if (P.eb == 1) return launch_plan<uint8_t>(P, (uint8_t *)buf_a, (uint8_t *)buf_b, ckpt_bufs, st);

@@ -208,6 +208,8 @@ struct DensePlan {
     std::vector<Seg> segs;
     std::vector<int64_t> ckpt_ops;
     int final_buf;          // buffer holding the final table (0: a, 1: b)
+    int w_start = 0;        // width of the start table (0: {0: 0}; else given in buffer a, canonical)
+    int final_w = 0;        // width of the final table (canonical order)
     int64_t n_updates;
     double pass_bytes;      // algorithmic bytes moved by the fused passes
     std::vector<float> seg_ms;  // per-segment launch time of the last timed execution
@@ -616,7 +618,8 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
     cp_async_wait_group<0>();
 }
 
-int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P);
+int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P,
+                     int w_start = 0, bool open_end = false);
 int set_dense_attrs();
 
 }  // namespace tg

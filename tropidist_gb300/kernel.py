@@ -38,16 +38,25 @@ def entry_bytes(dtype):
 class CompiledPlan:
     """A plan scheduled into launches by the library (reusable for repeated runs)."""
 
-    def __init__(self, plan, dtype="u8", checkpoints=()):
+    def __init__(self, plan, dtype="u8", checkpoints=(), w_start=0, ops=None):
+        """plan: a Plan (or None with `ops`, an encoded op stream); w_start > 0: the ops follow a
+        table of that width, put in buffer a (canonical order) before execute, and the plan may
+        end at any width (tg_dense_plan_from)."""
         self.plan = plan
         self.eb = entry_bytes(dtype)
-        self.ops = np.ascontiguousarray(plan.encode())
+        self.ops = np.ascontiguousarray(plan.encode() if ops is None else ops, dtype=np.int64).reshape(-1, 3)
         self.ckpts = np.ascontiguousarray(np.array(sorted(checkpoints), dtype=np.int64))
         L = _lib.lib()
         st = ctypes.c_int(0)
-        self.handle = L.tg_dense_plan(self.ops.ctypes.data, len(self.ops), self.eb,
-                                      self.ckpts.ctypes.data if len(self.ckpts) else None, len(self.ckpts),
-                                      ctypes.byref(st))
+        if w_start or ops is not None:
+            self.handle = L.tg_dense_plan_from(self.ops.ctypes.data if len(self.ops) else None, len(self.ops),
+                                               self.eb, int(w_start),
+                                               self.ckpts.ctypes.data if len(self.ckpts) else None,
+                                               len(self.ckpts), ctypes.byref(st))
+        else:
+            self.handle = L.tg_dense_plan(self.ops.ctypes.data, len(self.ops), self.eb,
+                                          self.ckpts.ctypes.data if len(self.ckpts) else None, len(self.ckpts),
+                                          ctypes.byref(st))
         if not self.handle:
             _lib.check(st.value)
         info = np.zeros(8, dtype=np.int64)
