@@ -121,6 +121,10 @@ int tg_sp_lookup(const void *H, int lg, const void *keys, uint64_t n, void *vals
  * indexes accumulated per step on the device; see csrc/sparse.cu for the fields.  Returns nsteps,
  * or the step where scratch / arena ran out (need[0] states, need[1] bytes; run again). */
 int64_t tg_sp_walk_scratch_bytes(uint64_t cap_n);
+/* host planning (no GPU): GF(2) rank of the first i columns of an order, i = 0..ncols
+ * (cdist/trellis.py:20-36); columns as CSR lists of rows */
+int tg_rank_profile(int ncols, int nrows, const int64_t *col_ptr, const int32_t *col_rows, const int32_t *order,
+                    int32_t *out);
 /* host planning (no GPU): the lookahead classes of every cut (the per-cut loop of
  * cdist/sparse_dp.py:148-192), CSR inputs; see csrc/sparse.cu */
 int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,

@@ -56,3 +56,19 @@ def test_estimate_counts_work():
     est = auto.estimate(p, list(range(p.ncols)))
     plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
     assert est["work"] == plan.work() and est["peak_bits"] == plan.peak_bits
+
+
+def test_rank_profile_host_routine_matches_restatement():
+    """The library's bitset rank profile equals the Python restatement of cdist/trellis.py:20-36."""
+    import random
+    from tropidist_gb300 import synth, trellis
+    rng = random.Random(4)
+    for _ in range(30):
+        n = rng.randint(1, 80)
+        h = [rng.randrange(0, 1 << rng.randint(1, 70)) for _ in range(n)]
+        order = list(range(n))
+        rng.shuffle(order)
+        assert trellis.rank_profile(h, order) == trellis.rank_profile_py(h, order)
+    p = synth.circuit_dem(seed=2, rounds=6, checks=20, ncols=800)
+    order = list(range(p.ncols))
+    assert trellis.rank_profile(p.h, order) == trellis.rank_profile_py(p.h, order)

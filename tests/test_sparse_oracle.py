@@ -125,7 +125,7 @@ def test_bound_data_host_routine_matches_restatement():
         p = synth.circuit_dem(seed=seed, rounds=rounds, checks=checks, ncols=n)
         tr = sparse_dp.Trellis.for_query(p, 0, sparse_dp.default_order(p))
         for fwd in (True, False):
-            a, b = tr._bound_data(fwd), tr._bound_data_py(fwd)
+            a, b = tr.bound_data(fwd), tr._bound_data_py(fwd)
             assert len(a) == len(b)
             for x, y in zip(a, b):
                 assert [int(v) for v in x[0]] == [int(v) for v in y[0]]

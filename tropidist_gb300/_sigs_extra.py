@@ -12,6 +12,7 @@ SIGNATURES = {
     "tg_sp_lookup": (ci, [vp, ci, vp, u64, vp, vp]),
     "tg_sp_hist": (ci, [vp, u64, vp, vp]),
     "tg_sp_walk_scratch_bytes": (i64, [u64]),
+    "tg_rank_profile": (ci, [ci, ci, vp, vp, vp, vp]),
     "tg_sp_bound_data": (ci, [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, ci, ci, ci, vp, vp, vp, vp]),
     "tg_sp_walk": (ci, [ci, vp, vp, vp, ci, ci, vp, u64, vp, ci, vp, u64, vp, u64, vp, vp, vp, vp, vp]),
     "tg_tab_create": (vp, [ci, ci, c.POINTER(ci)]),

@@ -788,6 +788,41 @@ int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *ro
     return TG_OK;
 }
 
+// GF(2) rank of the first i columns of `order` for i = 0..ncols (host work, no GPU; the rank
+// profile of cdist/trellis.py:20-36 with word-parallel bitsets).  Columns as rows (col_ptr /
+// col_rows CSR over nrows rows); out: int32[ncols + 1].
+int tg_rank_profile(int ncols, int nrows, const int64_t *col_ptr, const int32_t *col_rows, const int32_t *order,
+                    int32_t *out) {
+    if (ncols < 0 || nrows < 0 || !col_ptr || !order || !out) return set_error(TG_ERR_ARG, "bad rank profile");
+    const int W = (nrows + 63) / 64;
+    std::vector<uint64_t> piv((size_t)std::max(nrows, 1) * std::max(W, 1), 0);   // pivot vector by its top bit
+    std::vector<char> has(std::max(nrows, 1), 0);
+    std::vector<uint64_t> v(std::max(W, 1));
+    int rank = 0;
+    out[0] = 0;
+    for (int i = 0; i < ncols; i++) {
+        std::fill(v.begin(), v.end(), 0ull);
+        const int j = order[i];
+        for (int64_t k = col_ptr[j]; k < col_ptr[j + 1]; k++) v[col_rows[k] >> 6] ^= 1ull << (col_rows[k] & 63);
+        int top_word = W - 1;
+        while (true) {
+            while (top_word >= 0 && v[top_word] == 0) top_word--;
+            if (top_word < 0) break;
+            const int top = top_word * 64 + 63 - __builtin_clzll(v[top_word]);
+            if (!has[top]) {
+                has[top] = 1;
+                std::copy(v.begin(), v.end(), piv.begin() + (size_t)top * W);
+                rank++;
+                break;
+            }
+            const uint64_t *p = piv.data() + (size_t)top * W;
+            for (int w = 0; w <= top_word; w++) v[w] ^= p[w];
+        }
+        out[i + 1] = rank;
+    }
+    return TG_OK;
+}
+
 // Index (2^lg slots, cleared by the call) of an array of distinct packed states.  below >= 0:
 // only states with value < below are indexed, and copied to `kept` (room for n) when it is given.
 int tg_sp_build(const void *A, uint64_t n, void *H, int lg, int below, void *kept, void *counters, void *stream) {

@@ -159,11 +159,8 @@ class Trellis:
                                                ptr(act_ptr), ptr(act_rows), ptr(start), ptr(end), ptr(slot), self.L,
                                                int(bool(forward)), maxc, ptr(ncls), ptr(masks), ptr(wts),
                                                ptr(extra)))
-        out = []
-        for c in range(N + 1):
-            k = int(ncls[c])
-            out.append((tuple(masks[c, :k]), tuple(wts[c, :k]), int(extra[c])))
-        return out
+        k = max(1, int(ncls.max()) if ncls.size else 1)
+        return ncls, masks[:, :k].copy(), wts[:, :k].copy(), extra
 
     def _bound_data_py(self, forward):
         """Per cut: (masks, weights, extra) of h(s) = ceil((extra + sum_k w_k |(s ^ tmask) & mask_k|) / Q).
@@ -202,18 +199,41 @@ class Trellis:
             out.append((tuple(U64(masks[k]) for k in ks), tuple(np.int64(k) for k in ks), extra))
         return out
 
+    def bound_raw(self, forward):
+        """(ncls int32[N+1], masks uint64[N+1, k], weights int64[N+1, k], extra int64[N+1])."""
+        key = ("raw", forward)
+        if key not in self._bd:
+            self._bd[key] = self._bound_data(forward)
+        return self._bd[key]
+
     def bound_data(self, forward):
+        """Per cut: (masks, weights, extra) tuples."""
         if forward not in self._bd:
-            self._bd[forward] = self._bound_data(forward)
+            ncls, masks, wts, extra = self.bound_raw(forward)
+            self._bd[forward] = [(tuple(masks[c, :int(ncls[c])]), tuple(wts[c, :int(ncls[c])]), int(extra[c]))
+                                 for c in range(self.N + 1)]
         return self._bd[forward]
 
     def bound_arrays(self, forward):
-        """bound_data as contiguous arrays: per cut (masks uint64, weights int64, extra)."""
+        """Per cut (masks uint64, weights int64, extra), built on access."""
         key = ("arrays", forward)
         if key not in self._bd:
-            self._bd[key] = [(np.array(m, dtype=U64), np.array(w, dtype=np.int64), int(e))
-                             for m, w, e in self.bound_data(forward)]
+            self._bd[key] = _BoundView(*self.bound_raw(forward))
         return self._bd[key]
+
+
+class _BoundView:
+    """The lookahead data of every cut as a sequence of (masks, weights, extra), views of arrays."""
+
+    def __init__(self, ncls, masks, weights, extra):
+        self.ncls, self.masks, self.weights, self.extra = ncls, masks, weights, extra
+
+    def __len__(self):
+        return len(self.ncls)
+
+    def __getitem__(self, c):
+        k = int(self.ncls[c])
+        return self.masks[c, :k], self.weights[c, :k], int(self.extra[c])
 
 
 def bound(keys, tmask, hd):
@@ -542,27 +562,34 @@ class Sweep:
         """Spec rows of every step position of this sweep (without keep / join columns)."""
         tr, fwd = self.tr, self.direction > 0
         N = tr.N
+        p = np.arange(N)
+        cut = p + 1 if fwd else p
+        u64 = lambda xs: np.array([int(x) for x in xs], dtype=U64).view(np.int64)
+        caps = np.asarray(self.caps, dtype=np.int64)
         rows = np.zeros((max(1, N), 16), dtype=np.int64)
-        stride = 1
-        if self.hd:
-            stride = max([len(h[0]) for h in self.hd] + [1])
-        masks = np.zeros((max(1, N), stride), dtype=U64)
-        weights = np.zeros((max(1, N), stride), dtype=np.int64)
-        for p in range(N):
-            cut = p + 1 if fwd else p
-            sm, sb = (tr.fsel_mask[p], tr.fsel_bits[p]) if fwd else (tr.bsel_mask[p], tr.bsel_bits[p])
-            cap, kb = self.caps[cut], -1
-            if self.frontier:
-                cap = kb = self.caps[p]
-            trunc = self.caps[cut] if (self.frontier and self.caps[cut] < cap) else -1
-            hd = self.hd[cut] if self.hd else None
-            rows[p] = [int(tr.col[p]) & KEYMASK, int(sm), int(sb), int(tr.tmask[cut]) & KEYMASK, 0, 0,
-                       int(hd[2]) if hd is not None else 0, int(cap), int(kb), int(tr.cw[p]), 0, int(trunc), 0, 0,
-                       len(hd[0]) if hd is not None else 0, 1 if hd is not None else 0]
-            if hd is not None and len(hd[0]):
-                masks[p, :len(hd[0])] = hd[0]
-                weights[p, :len(hd[1])] = hd[1]
-        return rows, masks, weights
+        if N == 0:
+            return rows, np.zeros((1, 1), dtype=U64), np.zeros((1, 1), dtype=np.int64)
+        rows[:, 0] = u64(tr.col) & np.int64(KEYMASK)
+        rows[:, 1] = u64(tr.fsel_mask if fwd else tr.bsel_mask)
+        rows[:, 2] = u64(tr.fsel_bits if fwd else tr.bsel_bits)
+        rows[:, 3] = u64(tr.tmask)[cut] & np.int64(KEYMASK)
+        cap = caps[cut].copy()
+        kb = np.full(N, -1, dtype=np.int64)
+        trunc = np.full(N, -1, dtype=np.int64)
+        if self.frontier:
+            cap = caps[p].copy()
+            kb = cap.copy()
+            drop = caps[cut] < cap
+            trunc[drop] = caps[cut][drop]
+        rows[:, 7], rows[:, 8], rows[:, 11] = cap, kb, trunc
+        rows[:, 9] = np.asarray(tr.cw, dtype=np.int64)
+        if self.use_h:
+            ncls, masks, wts, extra = tr.bound_raw(fwd)
+            rows[:, 6] = extra[cut]
+            rows[:, 14] = ncls[cut]
+            rows[:, 15] = 1
+            return rows, np.ascontiguousarray(masks[cut]), np.ascontiguousarray(wts[cut])
+        return rows, np.zeros((N, 1), dtype=U64), np.zeros((N, 1), dtype=np.int64)
 
     def _positions(self, c, stop):
         return list(range(c, stop)) if self.direction > 0 else list(range(c - 1, stop - 1, -1))

@@ -35,7 +35,35 @@ def lowbit(x):
 
 
 def rank_profile(cols, order):
-    """r[i] = GF(2) rank of the first i columns of `order`, for i = 0..N (cdist/trellis.py:20-36)."""
+    """r[i] = GF(2) rank of the first i columns of `order`, for i = 0..N (cdist/trellis.py:20-36),
+    by the library's host routine (word-parallel bitsets; rank_profile_py restates it in Python)."""
+    import numpy as np
+    from . import _lib
+    n = len(cols)
+    rows_of = [_set_bits(c) for c in cols]
+    nrows = max((r[-1] for r in rows_of if r), default=-1) + 1
+    col_ptr = np.zeros(n + 1, dtype=np.int64)
+    col_ptr[1:] = np.cumsum([len(r) for r in rows_of])
+    col_rows = np.array([x for r in rows_of for x in r], dtype=np.int32)
+    order_a = np.ascontiguousarray(np.asarray(order, dtype=np.int32))
+    out = np.zeros(len(order) + 1, dtype=np.int32)
+    _lib.check(_lib.lib().tg_rank_profile(len(order), nrows, col_ptr.ctypes.data,
+                                          col_rows.ctypes.data if col_rows.size else None,
+                                          order_a.ctypes.data if order_a.size else None, out.ctypes.data))
+    return out.tolist()
+
+
+def _set_bits(x):
+    out = []
+    while x:
+        low = x & -x
+        out.append(low.bit_length() - 1)
+        x ^= low
+    return out
+
+
+def rank_profile_py(cols, order):
+    """Python restatement of rank_profile (cdist/trellis.py:20-36)."""
     pivots = {}
     rank = 0
     out = [0]
