@@ -362,7 +362,7 @@ def main():
         return
     import torch
     import torch.distributed as dist
-    from tropidist_gb300 import _lib, auto, kernel
+    from tropidist_gb300 import _lib, auto, kernel, replicas
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -412,15 +412,7 @@ def main():
     for _ in range(args.steps):
         step(acc)
     torch.cuda.synchronize()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        wt = torch.tensor([float(work)], device="cuda")
-        dist.all_reduce(wt)
-        total_work = float(wt.item())
-    else:
-        total_work = float(work)
+    ms, total_work = replicas.aggregate(ms, work, device="cuda")
     value = total_work * args.steps / (ms / 1e3)
     launches = sum(cp.nsegs for cp in cps) * args.steps
     # distances of the four observables (checked for consistency with the e2e path below)
