@@ -88,24 +88,55 @@ def _dtype_for(p):
 def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
     """Exact distance min over observables i of min{|e| : H e = 0, (L e)_i = 1}; None if no
     logical exists.  MemoryError if a table would exceed max_table_bytes, TimeoutError past the
-    deadline (time.monotonic), OverflowError if a distance reaches the table's INF."""
+    deadline (time.monotonic), OverflowError if a distance reaches the table's INF.
+
+    The observables' sweeps are queued on the stream one after another and their final entries
+    copied on the device; the host plans and schedules observable i + 1 while the GPU sweeps
+    observable i, and waits once at the end."""
+    import torch
+    from . import device
+    device.require_gpu()
     dtype = dtype or _dtype_for(p)
     eb = kernel.entry_bytes(dtype)
-    best = None
-    per = []
+    inf = kernel.INF if eb == 1 else kernel.INF16
+    per, slots = [], []
+    bufs = [None, None]
+    res = None
     for i, plan in _plans(p, order):
         if deadline is not None and time.monotonic() > deadline:
+            torch.cuda.current_stream().synchronize()
             raise TimeoutError("DP stopped at the time limit")
         if not plan.feasible:
             per.append(None)
             continue
         if max_table_bytes is not None and (eb << plan.peak_bits) > max_table_bytes:
             raise MemoryError("DP table of 2^%d entries exceeds the limit" % plan.peak_bits)
-        v, _ = kernel.run_plan(plan, dtype=dtype)
-        per.append(v)
-        if v is not None and (best is None or v < best):
+        cp = kernel.CompiledPlan(plan, dtype)
+        need = eb << cp.peak_bits
+        if bufs[0] is None or bufs[0].numel() < need:
+            bufs = [device.empty(need), device.empty(need)]
+        if res is None:
+            res = torch.zeros(max(1, 2 * p.nobs), dtype=torch.uint8, device="cuda")
+        a, b = bufs
+        cp.execute(a, b)
+        k = len(per)
+        res[eb * k:eb * k + eb].copy_((b if cp.final_buf else a)[:eb])
+        cp.free()
+        per.append(k)
+        slots.append(k)
+    vals = res.cpu().numpy() if res is not None else None
+    best = None
+    out = []
+    for x in per:
+        if x is None:
+            out.append(None)
+            continue
+        raw = int(vals[eb * x]) if eb == 1 else int(vals[eb * x]) | (int(vals[eb * x + 1]) << 8)
+        v = kernel.final_value(raw, inf)
+        out.append(v)
+        if best is None or v < best:
             best = v
-    return best, per
+    return best, out
 
 
 # ---------------------------------------------------------------------- witness
