@@ -355,6 +355,7 @@ class PersistentServer:
 
     def _loop(self):
         partial = None
+        idle = 50e-6
         while not self.stop_flag:
             progressed = False
             n = self.L.tg_server_poll(self.handle, self.slots.ctypes.data, self.vals.ctypes.data, self.plan_cap)
@@ -398,8 +399,13 @@ class PersistentServer:
                 self.peak_running = max(self.peak_running, len(self.owner))
                 if not ok:
                     break
+            # back off while nothing moves (the polling thread shares the interpreter with the
+            # sparse workers' host work), poll fast while results come in
             if not progressed:
-                time.sleep(50e-6)
+                time.sleep(idle)
+                idle = min(2 * idle, 1e-3)
+            else:
+                idle = 50e-6
 
     def drain(self, timeout=600.0):
         t0 = time.perf_counter()
