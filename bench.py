@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sparse-query", type=int, default=0,
+                    help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--sections", default="batched,served,sparse",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
@@ -347,6 +349,22 @@ def section_sparse(args):
     return out
 
 
+def sparse_query(K):
+    """One meet-in-the-middle query of the scaled circuit-style problem at threshold K."""
+    import torch
+    from tropidist_gb300 import sparse_dp, synth
+    p = synth.circuit_dem(seed=0, rounds=40, checks=24, ncols=20000)
+    tr = sparse_dp.Trellis.for_query(p, 0, sparse_dp.default_order(p))
+    t0 = time.perf_counter()
+    r = sparse_dp.query(tr, K, mode="mitm", witness=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    sm = sparse_dp.summary(r)
+    steps = sum(v for k, v in sm.items() if k.endswith("_states_total"))
+    return {"sparse_query": K, "value": r["value"], "seconds": dt, "state_steps_per_s": steps / dt,
+            "peak_states": sm.get("peak_states")}
+
+
 SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse}
 
 
@@ -359,6 +377,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
+        return
+    if args.sparse_query:
+        print(json.dumps(sparse_query(args.sparse_query)), flush=True)
         return
     import torch
     import torch.distributed as dist
