@@ -62,16 +62,43 @@ class SparseRequest:
         self.kmax = kmax
         self.max_states = max_states
         self.footprint = 24 * max_states          # packed states + index + changed list, bytes
+        self.plan = None                          # future of the host planning (server side)
         self.arrival = self.admitted = self.done = None
         self.distance = None
         self.values = None
         self.error = None
 
 
+_PLANNERS = None
+
+
+def _planners(n):
+    """A shared pool of planning processes (spawned: safe beside a CUDA context), warmed up."""
+    global _PLANNERS
+    if _PLANNERS is None and n > 0:
+        import concurrent.futures
+        import multiprocessing
+        _PLANNERS = concurrent.futures.ProcessPoolExecutor(max_workers=n,
+                                                           mp_context=multiprocessing.get_context("spawn"))
+        list(_PLANNERS.map(_warm, range(n)))
+    return _PLANNERS
+
+
+def _warm(_):
+    from . import sparse_dp  # noqa: F401  (imports the package and loads the library once)
+    return 0
+
+
+def _plan_sparse(problem):
+    from . import sparse_dp
+    return sparse_dp.plan_trellises(problem)
+
+
 def _run_sparse(req):
     from . import sparse_dp
     try:
-        r = sparse_dp.distance(req.problem, kmax=req.kmax, witness=False)
+        trs = req.plan.result() if getattr(req, "plan", None) is not None else None
+        r = sparse_dp.distance(req.problem, kmax=req.kmax, witness=False, trellises=trs)
         req.distance = r["distance"]
     except (sparse_dp.BudgetExceeded, MemoryError, ValueError) as e:
         req.error = "%s: %s" % (type(e).__name__, e)
@@ -261,7 +288,7 @@ class PersistentServer:
     polling, and a request completes when all of its plans have."""
 
     def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192,
-                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2):
+                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2, sparse_planners=4):
         import ctypes
         import torch
         from . import _lib
@@ -294,6 +321,8 @@ class PersistentServer:
         # sparse requests: a worker on its own stream, admitted one at a time against the sparse share
         # of the memory budget
         self.sparse_budget = int(sparse_frac * free) // max(1, sparse_workers)
+        # the sparse requests' host planning runs in worker processes as they arrive
+        self.planner = _planners(sparse_planners) if sparse_frac > 0 else None
         self.sparse_q = collections.deque()
         self.sparse_wake = threading.Event()
         self.sparse_threads = [threading.Thread(target=self._sparse_loop, daemon=True) for _ in range(sparse_workers)]
@@ -309,6 +338,8 @@ class PersistentServer:
                     self.submitted -= 1
                     raise MemoryError("sparse request %s needs %d bytes, beyond the sparse budget" %
                                       (req.rid, req.footprint))
+                if self.planner is not None:
+                    req.plan = self.planner.submit(_plan_sparse, req.problem)
                 self.sparse_q.append(req)
                 self.sparse_wake.set()
             else:

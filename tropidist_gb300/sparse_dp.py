@@ -1041,14 +1041,29 @@ def default_order(p):
     return auto.best_order(p)[0]
 
 
-def distance(p, order=None, start=1, kmax=64, mode="mitm", use_h=True, witness=True, log=None, every=None,
-             backend="gpu", dense=None, split=None):
-    """Exact distance by iterative deepening of K from `start` (a lower bound): a dict with the
-    distance (None if none <= kmax), a checked witness and one record per (threshold, observable)
-    (cdist/sparse_dp.py:1110-1151)."""
-    t0 = time.time()
+def plan_trellises(p, order=None):
+    """Host planning of distance(): the order and every observable's trellis with its lookahead
+    data (no GPU; picklable, so it can run in a worker process)."""
     order = default_order(p) if order is None else order
     trs = [Trellis.for_query(p, i, order) for i in range(p.nobs)]
+    for t in trs:
+        if t.feasible:
+            t.bound_raw(True)
+            t.bound_raw(False)
+    return trs
+
+
+def distance(p, order=None, start=1, kmax=64, mode="mitm", use_h=True, witness=True, log=None, every=None,
+             backend="gpu", dense=None, split=None, trellises=None):
+    """Exact distance by iterative deepening of K from `start` (a lower bound): a dict with the
+    distance (None if none <= kmax), a checked witness and one record per (threshold, observable)
+    (cdist/sparse_dp.py:1110-1151).  trellises: the result of plan_trellises, if planned ahead."""
+    t0 = time.time()
+    if trellises is not None:
+        trs = trellises
+    else:
+        order = default_order(p) if order is None else order
+        trs = [Trellis.for_query(p, i, order) for i in range(p.nobs)]
     out = {"distance": None, "witness": None, "runs": [], "lower_bound": start,
            "order_cut_rank": max((max(t.width) for t in trs if t.feasible), default=0)}
     for K in range(start, kmax + 1):
