@@ -294,6 +294,15 @@ def _serve_requests(seed=11):
     return out + sparse[si:]
 
 
+def _finish_times(reqs):
+    """Seconds from the first arrival to the last dense completion and to each sparse completion."""
+    from tropidist_gb300 import serve
+    t0 = min(r.arrival for r in reqs)
+    dense = [r.done - t0 for r in reqs if not isinstance(r, serve.SparseRequest)]
+    sparse = [round(r.done - t0, 3) for r in reqs if isinstance(r, serve.SparseRequest)]
+    return {"dense_last": round(max(dense), 3), "sparse": sparse}
+
+
 def section_served(args):
     """Poisson request streams mixing banded instances (widths 10-28) and circuit-style sparse
     problems (n = 2000-20000, 24 checks per round), served by the persistent-kernel request loop
@@ -311,7 +320,8 @@ def section_served(args):
         same = [a.distance for a in r1] == [b.distance for b in r2]
         s1, s2 = serve.summarize(r1, w1), serve.summarize(r2, w2)
         res["rates"][str(rate)] = {"served": s1, "plain": s2, "solves_ratio": s1["solves_per_s"] / s2["solves_per_s"],
-                                   "peak_plans_in_flight": peak, "distances_equal": same}
+                                   "peak_plans_in_flight": peak, "distances_equal": same,
+                                   "finish_s": {"served": _finish_times(r1), "plain": _finish_times(r2)}}
     return res
 
 

@@ -11,6 +11,7 @@
  */
 #ifndef TROPIDIST_GB300_H
 #define TROPIDIST_GB300_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -173,6 +174,34 @@ int tg_server_submit_plan(void *server, void *plan);
 int tg_server_poll(void *server, int *slots, uint32_t *values, int max);
 int tg_server_stop(void *server);
 void tg_server_free(void *server);
+
+/* ---------------------------------------------------------------- tree DP (exact min-plus on a binary tree)
+ * Per-call entry points with the reference's ctypes signatures (cdist/tree_dp.py:214-222), on DEVICE
+ * tables: the pairs i in [start, stop) of a join in Gray order, out[parent] = min(out[parent], a + b)
+ * over finite a, b (cdist/tree_dp.c:13-39); lm, rm are HOST arrays of `generators` (<= 64) maps. */
+int tree_join_u8(const void *left, const void *right, void *out, const uint64_t *lm, const uint64_t *rm,
+                 unsigned parent_bits, unsigned generators, uint64_t start, uint64_t stop, uint64_t infinity);
+int tree_join_u16(const void *left, const void *right, void *out, const uint64_t *lm, const uint64_t *rm,
+                  unsigned parent_bits, unsigned generators, uint64_t start, uint64_t stop, uint64_t infinity);
+int tree_join_u32(const void *left, const void *right, void *out, const uint64_t *lm, const uint64_t *rm,
+                  unsigned parent_bits, unsigned generators, uint64_t start, uint64_t stop, uint64_t infinity);
+int tree_join_u64(const void *left, const void *right, void *out, const uint64_t *lm, const uint64_t *rm,
+                  unsigned parent_bits, unsigned generators, uint64_t start, uint64_t stop, uint64_t infinity);
+/* cdist/tree_dp.c:45-50 tree_move: memmove between DEVICE addresses */
+int tree_move(void *destination, const void *source, size_t bytes);
+/* Whole-tree plan (replaces the executor loop of cdist/tree_dp.py:442-501): uint32 tables in one
+ * DEVICE arena.  leaves: rows (offset, size 1|2, column, nonzero); joins: rows (lo, ro, po, parent
+ * rank, kernel generators, height >= 1, maps index, 0) in nondecreasing height; maps: uint32 (left,
+ * right) state per generator.  info: heights, steps, launches per run, pairs, arena entries,
+ * leaves, joins, single-block steps.  small_pairs (< 0: default): heights of at most that many pairs
+ * run in one single-block launch; rbits (< 0: default): at most 2^rbits pairs per thread.  run:
+ * target = HOST bit vector of a particular solution (ceil(ncols / 64) words); *value = root entry. */
+void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins, int64_t njoins,
+                   const uint32_t *maps, int64_t nmaps, int64_t arena, int64_t root, int64_t ncols,
+                   int64_t small_pairs, int rbits, int *status);
+int tg_tree_plan_info(void *plan, int64_t *info, int n);
+int tg_tree_run(void *plan, void *arena, const uint64_t *target, uint32_t inf, uint32_t *value, void *stream);
+void tg_tree_plan_free(void *plan);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,8 @@ next to this script; the test-suite reads only those files.
   sparse_random.json  sparse_dp.query results on random small problems (tests/test_sparse_dp.py:41-46)
   sparse_tables.json  the reference's NumpyTables at every cut of a few sweeps (keys/vals digests)
   tables.json         completion-table builds (count) and lookups of random syndromes
+  tree_dp.json        the tree DP (cdist/tree_dp.py) on random matrices and trees, logical queries,
+                      distances beyond 255, larger joins  (`make_golden.py tree` writes only this)
 """
 from __future__ import annotations
 
@@ -278,5 +280,100 @@ def ref_tables(kernel, plan):
         yield i, buf[:n].copy()
 
 
+def tree_main():
+    """tree_dp.json: the reference's tree DP (C executor) on random matrices and tree shapes, the
+    logical-query front end, the distances beyond 255 and a few joins of 2^16-2^22 pairs."""
+    tmp = tempfile.mkdtemp(prefix="tropi_ref_")
+    shutil.copytree(os.path.join(REF, "cdist"), os.path.join(tmp, "cdist"))
+    sys.path[:0] = [tmp]
+    from cdist.tree_dp import CompiledTreeDP, tree_min_distance_for_mask
+
+    def balanced(xs):
+        if not xs:
+            return None
+        if len(xs) == 1:
+            return xs[0]
+        m = len(xs) // 2
+        return [balanced(xs[:m]), balanced(xs[m:])]
+
+    def comb(xs):
+        if not xs:
+            return None
+        t = xs[0]
+        for x in xs[1:]:
+            t = [t, x]
+        return t
+
+    def rtree(xs, rng):
+        if len(xs) == 1:
+            return xs[0]
+        k = rng.randrange(1, len(xs))
+        return [rtree(xs[:k], rng), rtree(xs[k:], rng)]
+
+    def tup(t):
+        return tuple(tup(x) for x in t) if isinstance(t, list) else t
+
+    keys = ("edge_state_dimensions", "max_join_dimension", "join_work", "peak_live_table_bytes",
+            "largest_table_bytes", "dtype", "infinity", "matrix_rank")
+    rng = random.Random(2026)
+    affine = []
+    for trial in range(120):
+        m, n = rng.randint(1, 8), rng.randint(1, 14)
+        cols = [rng.randrange(1 << m) for _ in range(n)]
+        order = list(range(n))
+        rng.shuffle(order)
+        tree = (comb(order), balanced(order), rtree(order, rng))[trial % 3]
+        prog = CompiledTreeDP(cols, tup(tree))
+        pf = prog.preflight()
+        targets = sorted({rng.randrange(1 << m) for _ in range(6)} | {0})
+        affine.append({"columns": cols, "tree": tree, "targets": targets,
+                       "distances": [prog.run(t)[0] for t in targets], "profile": {k: pf[k] for k in keys}})
+    logical = []
+    for trial in range(60):
+        n, m, nobs = rng.randrange(1, 13), rng.randrange(0, 7), rng.randrange(1, 4)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        order = list(range(n))
+        rng.shuffle(order)
+        tree = (comb(order), balanced(order), rtree(order, rng))[trial % 3]
+        mask = rng.randrange(1 << nobs)
+        d, st = tree_min_distance_for_mask(h, l, mask, tup(tree))
+        logical.append({"h": h, "l": l, "mask": mask, "tree": tree, "distance": d,
+                        "edge_state_dimensions": st["edge_state_dimensions"]})
+    chains = []
+    for n in (254, 255, 300):
+        h = [1] + [(1 << (j - 1)) | (1 << j) for j in range(1, n - 1)] + [1 << (n - 2)]
+        l = [1] + [0] * (n - 1)
+        d, st = tree_min_distance_for_mask(h, l, 1, tup(balanced(list(range(n)))))
+        chains.append({"ncols": n, "distance": d, "dtype": st["dtype"], "infinity": st["infinity"]})
+    large = []
+    for trial in range(6):
+        # random sparse columns over 16-22 rows; a balanced tree gives joins of 2^16-2^22 pairs
+        m = rng.randint(16, 22)
+        n = rng.randint(40, 64)
+        cols = [sum(1 << r for r in rng.sample(range(m), rng.randint(1, 3))) for _ in range(n)]
+        order = list(range(n))
+        rng.shuffle(order)
+        tree = balanced(order) if trial % 2 == 0 else rtree(order, rng)
+        prog = CompiledTreeDP(cols, tup(tree))
+        pf = prog.preflight(max_join_work=None, max_memory_bytes=None)
+        if pf["max_join_dimension"] > 24:
+            continue
+        targets = [0] + [rng.randrange(1 << m) for _ in range(3)]
+        ds = [prog.run(t, max_join_work=None, max_memory_bytes=None, max_seconds=None)[0] for t in targets]
+        large.append({"columns": cols, "tree": tree, "targets": targets, "distances": ds,
+                      "profile": {k: pf[k] for k in keys}})
+    out = {"affine": affine, "logical": logical, "chains": chains, "large": large}
+    with open(os.path.join(HERE, "tree_dp.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    print("wrote tree_dp.json", os.path.getsize(os.path.join(HERE, "tree_dp.json")), "bytes;",
+          len(large), "large cases, max join dims", [c["profile"]["max_join_dimension"] for c in large])
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["tree"]:
+        tree_main()
+    else:
+        main()
+        tree_main()
