@@ -108,3 +108,73 @@ def brute_logical(h, l, mask):
             w = sum(bits)
             best = w if best is None else min(best, w)
     return best
+
+
+_PORT = None
+
+
+def port_lib():
+    """oracle/tree_port.so (built by oracle/Makefile)."""
+    global _PORT
+    if _PORT is None:
+        import ctypes
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tree_port.so")
+        L = ctypes.CDLL(path)
+        for b in (8, 16, 32):
+            f = getattr(L, "tree_join_port_u%d" % b)
+            f.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_uint] + [ctypes.c_uint64] * 3
+            f.restype = None
+        _PORT = L
+    return _PORT
+
+
+def run_port(prog, target, chunk=1 << 20):
+    """The reference's executor (cdist/tree_dp.py:442-501: one arena of the table dtype in post-order
+    with stack compaction, joins in chunks of 2^20 pairs) over the C port of its join: the timed
+    single-threaded CPU baseline.  Returns the minimum weight or None."""
+    rep = prog.representative(target)
+    if rep is None:
+        return None
+    if not prog.nodes:
+        return 0
+    L = port_lib()
+    dt = np.dtype(prog.dtype)
+    fn = getattr(L, "tree_join_port_u%d" % (8 * dt.itemsize))
+    inf = prog.infinity
+    arena = np.empty(prog.peak_live_entries, dtype=dt)
+    base, item = arena.ctypes.data, dt.itemsize
+    gl = np.empty(64, dtype=np.uint64)
+    gr = np.empty(64, dtype=np.uint64)
+    stack, live = [], 0
+    for i in prog.order:
+        nd = prog.nodes[i]
+        size = 1 << len(prog.interfaces[i])
+        out = arena[live:live + size]
+        out.fill(inf)
+        if nd.leaf is not None:
+            bit = (rep >> nd.leaf) & 1
+            out[0] = bit if prog.columns[nd.leaf] else 0
+            if size == 2:
+                out[1] = bit ^ 1
+            stack.append((i, live, size))
+            live += size
+            continue
+        b, a = stack.pop(), stack.pop()
+        left, right = (a, b) if a[0] == nd.left else (b, a)
+        jn = prog.joins[i]
+        lo = (1 << jn.left_rank) - 1
+        gens = jn.parent_maps + jn.free_maps
+        for k, g in enumerate(gens):
+            gl[k] = g & lo
+            gr[k] = g >> jn.left_rank
+        for s in range(0, jn.work, chunk):
+            fn(base + left[1] * item, base + right[1] * item, base + live * item, gl.ctypes.data, gr.ctypes.data,
+               jn.parent_rank, s, min(s + chunk, jn.work), inf)
+        dst = a[1]
+        arena[dst:dst + size] = arena[live:live + size].copy()
+        live = dst + size
+        stack.append((i, dst, size))
+    v = int(arena[0])
+    assert v < inf
+    return v

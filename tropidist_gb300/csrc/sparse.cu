@@ -239,6 +239,7 @@ static int load_bound(BoundParams &B, int on, int K, int ncls, const uint64_t *m
 // against backward indexes accumulated per step on the device: one call per run of steps instead
 // of one per column, and no allocation.
 #define SPW_FIELDS 16
+#define SPW_KEEP_SMALL 1024             // keep flag 2: keep the table if it has at most this many states
 enum { SW_UPD, SW_SELM, SW_SELB, SW_TMASK, SW_JTAB, SW_JTMASK, SW_EXTRA, SW_CAP, SW_KB, SW_W, SW_WANT, SW_TRUNC,
        SW_KEEP, SW_JLG, SW_NCLS, SW_USEH };
 
@@ -279,8 +280,241 @@ struct WalkSmall {
     unsigned long long *state;          // out: [0] next step, [1] slot, [2] n, [3] lg, [4] arena used, [5] stop reason
 };
 
+// ---- tiny tables: the same steps with the working tables in shared memory
+// The three scratch slots (states and index), the changed list and a copy of the join table live
+// in shared memory, so a step touches global memory only for its outputs, kept tables and large
+// join tables; the next step's rows are fetched while the current step runs.  It takes tables of at
+// most SPW_TINY_N / 2 states with an index of at most 2^SPW_TINY_LG slots and stops (reason 1) when
+// a step would need more; the table it ends with is written back to its global scratch slot.
+#define SPW_TINY_N 1024
+#define SPW_TINY_LG 12
+#define SPW_TINY_THREADS 512
+#define SPW_TINY_SMEM (8 * (3 * SPW_TINY_N + 3 * (1 << SPW_TINY_LG) + SPW_TINY_N + (1 << SPW_TINY_LG)))
+
+__global__ void __launch_bounds__(SPW_TINY_THREADS) k_sp_walk_tiny(const __grid_constant__ WalkSmall P) {
+    extern __shared__ unsigned long long sm_tiny[];
+    auto sA = [&](int k) { return sm_tiny + k * SPW_TINY_N; };
+    auto sH = [&](int k) { return sm_tiny + 3 * SPW_TINY_N + k * (1 << SPW_TINY_LG); };
+    unsigned long long *sCH = sm_tiny + 3 * SPW_TINY_N + 3 * (1 << SPW_TINY_LG);
+    unsigned long long *sJ = sCH + SPW_TINY_N;
+    __shared__ unsigned long long c_ch, c_out, c_tr, c_flag;
+    __shared__ BoundParams B[2];
+    __shared__ int64_t F[2][SPW_FIELDS];
+    __shared__ const unsigned long long *j_cached;
+    const unsigned tid = threadIdx.x, NT = blockDim.x;
+    int cur = P.slot0;
+    int sc = cur >= 0 ? cur : 2;          // shared slot of the current table (an outside table goes to 2)
+    uint64_t n = P.n0;
+    int lg = P.lg0;
+    uint64_t used = P.used0;
+    int i = P.i0, reason = 0;
+    // the table before step i0, and the rows of step i0
+    for (uint64_t k = tid; k < n; k += NT) sA(sc)[k] = P.A0[k];
+    for (uint64_t k = tid; k < (1ull << lg); k += NT) sH(sc)[k] = P.H0[k];
+    auto load_rows = [&](int step, int buf) {
+        const int64_t *f = P.spec + (size_t)SPW_FIELDS * step;
+        if (tid < SPW_FIELDS) F[buf][tid] = f[tid];
+        const int nc = (int)f[SW_NCLS];
+        for (int c = tid; c < nc && c < SP_MAXCLS; c += NT) {
+            B[buf].mask[c] = P.masks[(size_t)P.stride * step + c];
+            B[buf].w[c] = P.weights[(size_t)P.stride * step + c];
+        }
+        if (tid == 0) {
+            B[buf].on = (int)f[SW_USEH];
+            B[buf].ncls = nc;
+            B[buf].K = P.K;
+            B[buf].extra = f[SW_EXTRA];
+            B[buf].tmask = (uint64_t)f[SW_TMASK];
+        }
+    };
+    if (i < P.nsteps) load_rows(i, i & 1);
+    if (tid == 0) { c_ch = c_out = c_tr = c_flag = 0; j_cached = nullptr; }
+    __syncthreads();
+    for (; i < P.nsteps; i++) {
+        const int b = i & 1;
+        const int64_t *f = F[b];
+        if (2 * n > SPW_TINY_N) { reason = 1; break; }
+        int os = 0;
+        while (os == cur) os++;
+        const int lgn = lg_for(2 * n);
+        const uint64_t capn = 1ull << lgn;
+        unsigned long long *H = sH(os), *A = sA(os);
+        for (uint64_t k = tid; k < capn; k += NT) H[k] = SP_EMPTY;
+        // the next step's rows: loads issued now, stored at the end of the step
+        int64_t pf = 0;
+        uint64_t pm = 0;
+        int64_t pw = 0;
+        const bool more = i + 1 < P.nsteps;
+        if (more) {
+            const int64_t *fn = P.spec + (size_t)SPW_FIELDS * (i + 1);
+            if (tid < SPW_FIELDS) pf = fn[tid];
+            if (tid >= 32 && tid < 32 + (unsigned)SP_MAXCLS && (int)(tid - 32) < P.stride) {
+                pm = P.masks[(size_t)P.stride * (i + 1) + (tid - 32)];
+                pw = P.weights[(size_t)P.stride * (i + 1) + (tid - 32)];
+            }
+        }
+        // a join table small enough is copied once and then probed in shared memory
+        const unsigned long long *jG = reinterpret_cast<const unsigned long long *>((uintptr_t)f[SW_JTAB]);
+        const int jlg = (int)f[SW_JLG];
+        const bool jS = jG && jlg <= SPW_TINY_LG;
+        if (jS && j_cached != jG)
+            for (uint64_t k = tid; k < (1ull << jlg); k += NT) sJ[k] = jG[k];
+        __syncthreads();
+        if (tid == 0 && jS) j_cached = jG;
+        const unsigned long long *curA = sA(sc), *curH = sH(sc);
+        const uint64_t upd = (uint64_t)f[SW_UPD] & SP_KEYMASK, selm = (uint64_t)f[SW_SELM], selb = (uint64_t)f[SW_SELB];
+        const uint64_t clr = ~selm & SP_KEYMASK;
+        const int cap = (int)f[SW_CAP], kb = (int)f[SW_KB], w = (int)f[SW_W];
+        const bool want = f[SW_WANT] != 0;
+        for (uint64_t k = tid; k < n; k += NT) {
+            const unsigned long long x = curA[k];
+            const uint64_t key = x & SP_KEYMASK;
+            const uint32_t v = (uint32_t)(x >> 56);
+            if ((key & selm) == selb) {
+                const uint64_t k2 = key & clr;
+                if ((int)v <= cap && sp_keep(B[b], k2, v)) {
+                    if (sp_insert_min(H, lgn, k2, v) < 0) atomicOr(&c_flag, 1ull);
+                }
+            }
+            if (upd && (int)v < cap) {
+                const uint64_t t = key ^ upd;
+                const uint32_t vc = v + (uint32_t)w;
+                if ((t & selm) == selb) {
+                    const uint64_t t2 = t & clr;
+                    if ((int)vc <= cap && sp_keep(B[b], t2, vc)) {
+                        const uint32_t vo = sp_lookup(curH, lg, t);
+                        const bool hit = vo != 255u;
+                        if (vc < vo && want) {
+                            const unsigned long long q = atomicAdd(&c_ch, 1ull);
+                            if (q < SPW_TINY_N) sCH[q] = t2 | ((unsigned long long)vc << 56);
+                            else atomicOr(&c_flag, 1ull);
+                        }
+                        if (hit || kb < 0 || (int)vc < kb) {
+                            if (sp_insert_min(H, lgn, t2, vc) < 0) atomicOr(&c_flag, 1ull);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (uint64_t k = tid; k < capn; k += NT) {
+            const unsigned long long x = H[k];
+            if (x != SP_EMPTY) {
+                const unsigned long long q = atomicAdd(&c_out, 1ull);
+                if (q < SPW_TINY_N) A[q] = x;
+                else atomicOr(&c_flag, 1ull);
+            }
+        }
+        __syncthreads();
+        if (c_flag) { reason = 4; break; }
+        uint64_t nn = c_out;
+        const uint64_t nch = want ? c_ch : 0;
+        const uint64_t jt = (uint64_t)f[SW_JTMASK] & SP_KEYMASK;
+        const unsigned long long *jH = jS ? sJ : jG;
+        unsigned long long best = ~0ull;
+        if (jH)
+            for (uint64_t k = tid; k < nch; k += NT) {
+                const unsigned long long x = sCH[k];
+                const uint32_t bv = sp_lookup(jH, jlg, (x & SP_KEYMASK) ^ jt);
+                if (bv != 255u) best = min(best, (((x >> 56) + bv) << 56) | (x & SP_KEYMASK));
+            }
+        int64_t *o = P.out + 6 * (size_t)i;
+        if (tid == 0) o[5] = (int64_t)nn;
+        int nlg = lgn, ns = os;
+        if (f[SW_TRUNC] >= 0) {
+            if (jH)
+                for (uint64_t k = tid; k < nn; k += NT) {
+                    const unsigned long long x = A[k];
+                    const uint32_t bv = sp_lookup(jH, jlg, (x & SP_KEYMASK) ^ jt);
+                    if (bv != 255u) best = min(best, (((x >> 56) + bv) << 56) | (x & SP_KEYMASK));
+                }
+            int ts = 0;
+            while (ts == os) ts++;
+            const int lgt = lg_for(nn);
+            unsigned long long *T = sH(ts), *TA = sA(ts);
+            for (uint64_t k = tid; k < (1ull << lgt); k += NT) T[k] = SP_EMPTY;
+            __syncthreads();
+            const int below = (int)f[SW_TRUNC];
+            for (uint64_t k = tid; k < nn; k += NT) {
+                const unsigned long long x = A[k];
+                if ((int)(x >> 56) >= below) continue;
+                if (sp_insert_min(T, lgt, x & SP_KEYMASK, (uint32_t)(x >> 56)) < 0) atomicOr(&c_flag, 1ull);
+                TA[atomicAdd(&c_tr, 1ull)] = x;
+            }
+            __syncthreads();
+            nn = c_tr;
+            nlg = lgt;
+            ns = ts;
+        }
+        if (jH && best != ~0ull) atomicMin(P.res + i, best);
+        int64_t a_off = -1, h_off = -1;
+        if (f[SW_KEEP] == 1 || (f[SW_KEEP] == 2 && nn <= SPW_KEEP_SMALL)) {
+            const int lgk = lg_for(nn);
+            const uint64_t ab = (8 * nn + 255) / 256 * 256, ib = 8ull << lgk;
+            if (used + ab + ib > P.arena_bytes) { reason = 2; break; }
+            unsigned long long *kA = P.arena + used / 8, *kH = P.arena + (used + ab) / 8;
+            const unsigned long long *nA = sA(ns);
+            for (uint64_t k = tid; k < nn; k += NT) kA[k] = nA[k];
+            for (uint64_t k = tid; k < (1ull << lgk); k += NT) kH[k] = SP_EMPTY;
+            __syncthreads();
+            for (uint64_t k = tid; k < nn; k += NT)
+                if (sp_insert_min(kH, lgk, nA[k] & SP_KEYMASK, (uint32_t)(nA[k] >> 56)) < 0) atomicOr(&c_flag, 1ull);
+            a_off = (int64_t)used;
+            h_off = (int64_t)(used + ab);
+            used += ab + ib;
+            if (tid == 0) o[4] = lgk;
+        } else if (tid == 0) {
+            o[4] = nlg;
+        }
+        if (tid == 0) {
+            o[0] = (int64_t)nn;
+            o[1] = (int64_t)nch;
+            o[2] = a_off;
+            o[3] = h_off;
+        }
+        n = nn;
+        lg = nlg;
+        cur = ns;
+        sc = ns;
+        // the next step's rows (fetched above) into the other buffer
+        if (more) {
+            const int nb = b ^ 1;
+            if (tid < SPW_FIELDS) F[nb][tid] = pf;
+            if (tid >= 32 && tid < 32 + (unsigned)SP_MAXCLS && (int)(tid - 32) < P.stride) {
+                B[nb].mask[tid - 32] = pm;
+                B[nb].w[tid - 32] = pw;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (more) {
+                B[b ^ 1].on = (int)F[b ^ 1][SW_USEH];
+                B[b ^ 1].ncls = (int)F[b ^ 1][SW_NCLS];
+                B[b ^ 1].K = P.K;
+                B[b ^ 1].extra = F[b ^ 1][SW_EXTRA];
+                B[b ^ 1].tmask = (uint64_t)F[b ^ 1][SW_TMASK];
+            }
+            c_ch = c_out = c_tr = 0;
+        }
+        __syncthreads();
+    }
+    // the current table back to its global scratch slot (the steps' results are all there)
+    if (i > P.i0 && cur >= 0) {
+        for (uint64_t k = tid; k < n; k += NT) P.arr[cur][k] = sA(sc)[k];
+        for (uint64_t k = tid; k < (1ull << lg); k += NT) P.idx[cur][k] = sH(sc)[k];
+    }
+    if (tid == 0) {
+        P.state[0] = (unsigned long long)i;
+        P.state[1] = (unsigned long long)(long long)cur;
+        P.state[2] = n;
+        P.state[3] = (unsigned long long)lg;
+        P.state[4] = used;
+        P.state[5] = (unsigned long long)reason;
+    }
+}
+
 // stop reasons: 1 a table beyond SPW_SMALL_MAX (continue with the per-step path), 2 arena full,
-// 4 index full
+// 4 index full, 5 the tables fit the shared-memory walk again
 __global__ void __launch_bounds__(SPW_SMALL_THREADS) k_sp_walk_small(const __grid_constant__ WalkSmall P) {
     __shared__ unsigned long long c_ch, c_out, c_flag;
     __shared__ BoundParams B;
@@ -293,6 +527,7 @@ __global__ void __launch_bounds__(SPW_SMALL_THREADS) k_sp_walk_small(const __gri
     for (; i < P.nsteps; i++) {
         const int64_t *f = P.spec + (size_t)SPW_FIELDS * i;
         if (2 * n > SPW_SMALL_MAX) { reason = 1; break; }
+        if (i > P.i0 && 4 * 2 * n <= SPW_TINY_N && lg <= SPW_TINY_LG) { reason = 5; break; }
         int os = 0;
         while (os == cur) os++;
         const int lgn = lg_for(2 * n);
@@ -399,7 +634,7 @@ __global__ void __launch_bounds__(SPW_SMALL_THREADS) k_sp_walk_small(const __gri
         }
         if (jH && best != ~0ull) atomicMin(P.res + i, best);
         int64_t a_off = -1, h_off = -1;
-        if (f[SW_KEEP]) {
+        if (f[SW_KEEP] == 1 || (f[SW_KEEP] == 2 && nn <= SPW_KEEP_SMALL)) {
             const int lgk = lg_for(nn);
             const uint64_t ab = (8 * nn + 255) / 256 * 256, ib = 8ull << lgk;
             if (used + ab + ib > P.arena_bytes) { reason = 2; break; }
@@ -585,8 +820,18 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
         if (!e && b_cls) e = cuda_check(cudaMemcpyAsync(dbuf + b_spec + b_cls, weights, b_cls, cudaMemcpyHostToDevice, st), "walk rows");
         if (e) return e;
     }
+    static bool tiny_attr = false;
+    if (small_ok && !tiny_attr) {
+        e = cuda_check(cudaFuncSetAttribute(k_sp_walk_tiny, cudaFuncAttributeMaxDynamicSharedMemorySize, SPW_TINY_SMEM),
+                       "tiny walk shared memory");
+        if (e) return e;
+        tiny_attr = true;
+    }
     for (int i = 0; i < nsteps; i++) {
-        if (small_ok && 2 * n <= SPW_SMALL_MAX) {
+        // one-block walks while the tables are small: shared-memory tables first, then global ones;
+        // each stops when its tables outgrow it (the small walk also when they become tiny again)
+        while (small_ok && i < nsteps && 2 * n <= SPW_SMALL_MAX) {
+            const bool tiny = 2 * n <= SPW_TINY_N && lg <= SPW_TINY_LG;
             WalkSmall S;
             S.spec = reinterpret_cast<const int64_t *>(dbuf);
             S.masks = reinterpret_cast<const uint64_t *>(dbuf + b_spec);
@@ -609,7 +854,8 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
             S.res = res;
             unsigned long long *dstate = reinterpret_cast<unsigned long long *>(dbuf + b_spec + 2 * b_cls + b_out);
             S.state = dstate;
-            k_sp_walk_small<<<1, SPW_SMALL_THREADS, 0, st>>>(S);
+            if (tiny) k_sp_walk_tiny<<<1, SPW_TINY_THREADS, SPW_TINY_SMEM, st>>>(S);
+            else k_sp_walk_small<<<1, SPW_SMALL_THREADS, 0, st>>>(S);
             e = cuda_check(cudaGetLastError(), "small walk");
             if (!e) e = cuda_check(cudaMemcpyAsync(hb, dstate, 48, cudaMemcpyDeviceToHost, st), "small walk state");
             if (!e) e = cuda_check(cudaMemcpyAsync(out + 6 * (size_t)i, S.out + 6 * (size_t)i, 48 * (size_t)(nsteps - i),
@@ -628,9 +874,11 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
             }
             if (reason == 2) { need[1] = (int64_t)(2 * arena_bytes + (1 << 20)); return i1; }
             if (reason == 4) return set_error(TG_ERR_STATE, "walk table overflow");
-            if (i1 >= nsteps) break;
+            const bool progressed = i1 > i;
             i = i1;
+            if (!progressed && !tiny) break;    // the next step needs the per-step path
         }
+        if (i >= nsteps) break;
         const int64_t *f = spec + (size_t)SPW_FIELDS * i;
         int64_t *o = out + 6 * (size_t)i;
         if (2 * n > cap_n) { need[0] = (int64_t)(2 * n); return i; }
@@ -692,7 +940,7 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
         o[1] = (int64_t)nch;
         o[2] = o[3] = -1;
         o[4] = nlg;
-        if (f[SW_KEEP]) {
+        if (f[SW_KEEP] == 1 || (f[SW_KEEP] == 2 && nn <= SPW_KEEP_SMALL)) {
             // the kept copy gets an index of its own at load <= 1/2 (half the working index)
             const int lgk = lg_for(nn);
             const uint64_t ab = (8 * nn + 255) / 256 * 256, ib = 8ull << lgk;

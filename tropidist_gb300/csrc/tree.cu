@@ -120,18 +120,29 @@ __device__ __forceinline__ uint32_t gray_walk(uint32_t m, uint32_t li, uint32_t 
     uint32_t a[RI > 0 ? RI : 1], b[RI > 0 ? RI : 1];
 #pragma unroll
     for (int i = 0; i < RI; i++) { a[i] = gl[2 * i]; b[i] = gl[2 * i + 1]; }
-    m = min(m, __ldg(L + li) + __ldg(Rt + ri));
+    // batches of up to 8 pairs: all 16 gathers of a batch are issued before any is used, so a warp
+    // keeps many L2 requests in flight (the kernel is bound by gather latency, not bandwidth)
+    constexpr int NB = (1 << RI) < 8 ? (1 << RI) : 8;
 #pragma unroll
-    for (int k = 1; k < (1 << RI); k++) {
-        const int bit = __ffs(k) - 1;        // a constant once unrolled
-        li ^= a[bit];
-        ri ^= b[bit];
-        m = min(m, __ldg(L + li) + __ldg(Rt + ri));
+    for (int k0 = 0; k0 < (1 << RI); k0 += NB) {
+        uint32_t x[NB], y[NB];
+#pragma unroll
+        for (int k = k0; k < k0 + NB; k++) {
+            if (k) {
+                const int bit = __ffs(k) - 1;        // a constant once unrolled
+                li ^= a[bit];
+                ri ^= b[bit];
+            }
+            x[k - k0] = __ldg(L + li);
+            y[k - k0] = __ldg(Rt + ri);
+        }
+#pragma unroll
+        for (int k = 0; k < NB; k++) m = min(m, x[k] + y[k]);
     }
     return m;
 }
 
-__global__ void __launch_bounds__(TR_BS) k_tree_join(const TJoin *joins, int nj, const uint32_t *maps,
+__global__ void __launch_bounds__(TR_BS, 4) k_tree_join(const TJoin *joins, int nj, const uint32_t *maps,
                                                      uint32_t *arena, uint32_t inf) {
     __shared__ uint32_t sg[2 * TR_MAXJ];
     __shared__ int sj;

@@ -256,6 +256,29 @@ class _Tab:
     def __init__(self, arr, n, H, lg):
         self.arr, self.n, self.H, self.lg = arr, n, H, lg
 
+    def hptr(self):
+        return self.H.data_ptr()
+
+
+class _ArenaTab:
+    """A table kept by a device walk inside the walk's arena (states at int64 offset a0, index at h0);
+    the tensor views are made only when asked for."""
+    __slots__ = ("arena", "a0", "n", "h0", "lg")
+
+    def __init__(self, arena, a0, n, h0, lg):
+        self.arena, self.a0, self.n, self.h0, self.lg = arena, a0, n, h0, lg
+
+    @property
+    def arr(self):
+        return self.arena[self.a0:self.a0 + self.n]
+
+    @property
+    def H(self):
+        return self.arena[self.h0:self.h0 + (1 << self.lg)]
+
+    def hptr(self):
+        return self.arena.data_ptr() + 8 * self.h0
+
 
 class _Changed:
     __slots__ = ("arr", "n")
@@ -410,9 +433,9 @@ class GpuTables:
         bval = self.lookup(btab, bkey)
         return total, fkey, total - bval, bkey
 
-    def walk(self, tab, rows, masks, weights, K, max_states=None):
+    def walk(self, tab, rows, masks, weights, K, max_states=None, want_res=True):
         """Run the column steps of `rows` (int64 [m, 16] spec rows, csrc/sparse.cu tg_sp_walk) from
-        `tab` in one call: (out int64 [m, 6], {step: kept table}, join results uint64 [m])."""
+        `tab` in one call: (out int64 [m, 6], {step: kept table}, join results uint64 [m] or None)."""
         torch = self.torch
         m = len(rows)
         rows = np.ascontiguousarray(rows, dtype=np.int64)
@@ -423,7 +446,9 @@ class GpuTables:
         arena_bytes = max(getattr(self, "_arena_guess", 1 << 20), 1 << 16)
         out = np.zeros((max(1, m), 6), dtype=np.int64)
         need = np.zeros(2, dtype=np.int64)
-        res = torch.empty(max(1, m), dtype=torch.int64, device="cuda")
+        res = getattr(self, "_res", None)
+        if res is None or res.numel() < max(1, m):
+            res = self._res = torch.empty(max(1024, m), dtype=torch.int64, device="cuda")
         L = self.L
         while True:
             if max_states is not None and cap > 4 * max(max_states, 1) + 4 * tab.n:
@@ -435,7 +460,7 @@ class GpuTables:
             arena = None
             arena = torch.empty((arena_bytes + 7) // 8, dtype=torch.int64, device="cuda")
             r = L.tg_sp_walk(m, rows.ctypes.data, masks.ctypes.data, weights.ctypes.data, stride, int(K),
-                             tab.arr.data_ptr() if tab.n else None, tab.n, tab.H.data_ptr(), tab.lg,
+                             tab.arr.data_ptr() if tab.n else None, tab.n, tab.hptr(), tab.lg,
                              self._scratch.data_ptr(), cap, arena.data_ptr(), arena_bytes, out.ctypes.data,
                              res.data_ptr(), need.ctypes.data, self.counters.data_ptr(), device.stream_ptr())
             if r < 0:
@@ -449,14 +474,15 @@ class GpuTables:
                 arena_bytes = max(arena_bytes + (arena_bytes >> 1), int(need[1]) * m // max(1, r + 1) + (1 << 20))
         self._walk_cap = cap
         kept, used = {}, 0
-        for i in range(m):
-            if out[i, 2] >= 0:
-                n, lg = int(out[i, 0]), int(out[i, 4])
-                a0, h0 = int(out[i, 2]) // 8, int(out[i, 3]) // 8
-                kept[i] = _Tab(arena[a0:a0 + n], n, arena[h0:h0 + (1 << lg)], lg)
-                used = max(used, 8 * (h0 + (1 << lg)))
+        ks = np.nonzero(out[:m, 2] >= 0)[0]
+        if len(ks):
+            sub = out[ks]
+            for i, n, a, h, lg in zip(ks.tolist(), sub[:, 0].tolist(), sub[:, 2].tolist(), sub[:, 3].tolist(),
+                                      sub[:, 4].tolist()):
+                kept[i] = _ArenaTab(arena, a // 8, n, h // 8, lg)
+            used = int((sub[:, 3] + 8 * (np.int64(1) << sub[:, 4])).max())
         self._arena_guess = max(1 << 16, used + (used >> 2))
-        return out[:m], kept, res[:m].cpu().numpy().view(U64)
+        return out[:m], kept, (res[:m].cpu().numpy().view(U64) if want_res else None)
 
     def hist(self, tab):
         import torch
@@ -519,6 +545,13 @@ class Sweep:
         self.peak_bytes = 0
         self.steps_done = 0
         self._all = None
+        # device walks: tables of at most SMALL_KEEP states are kept at every cut (within a byte
+        # budget), so a meet in the middle reads them instead of recomputing segments
+        self.small_tabs = {}
+        self.small_bytes = 0
+
+    RUN_STEPS = 4096            # steps per device walk of a sweep that joins nothing
+    SMALL_KEEP_BYTES = 256 << 20
 
     def first(self):
         return (0 if self.direction > 0 else self.tr.N), self.be.start()
@@ -550,12 +583,11 @@ class Sweep:
         rows[:, 12] = np.asarray(keep, dtype=np.int64)
         if joins is not None:
             rows[:, 10] = 1
-            for k, j in enumerate(joins):
-                if j is not None:
-                    btab, jtm = j
-                    rows[k, 4] = btab.H.data_ptr()
-                    rows[k, 5] = int(jtm) & KEYMASK
-                    rows[k, 13] = btab.lg
+            ks = [k for k, j in enumerate(joins) if j is not None]
+            if ks:
+                rows[ks, 4] = [joins[k][0].hptr() for k in ks]
+                rows[ks, 5] = [int(joins[k][1]) & KEYMASK for k in ks]
+                rows[ks, 13] = [joins[k][0].lg for k in ks]
         return rows, masks0[pos], weights0[pos]
 
     def _all_rows(self):
@@ -621,23 +653,40 @@ class Sweep:
         c = c0
         while c != stop and not (best is not None and best[0] <= max(lower, 0)):
             c1 = self._next_ckpt(c, stop)
+            if join_with is None:           # no early stop possible: several intervals per walk
+                while c1 != stop and abs(c1 - c) < self.RUN_STEPS:
+                    c1 = self._next_ckpt(c1, stop)
             pos = self._positions(c, c1)
-            keep = [0] * (len(pos) - 1) + [1]
+            cuts = [p + 1 for p in pos] if self.direction > 0 else pos
+            small = 2 if self.small_bytes < self.SMALL_KEEP_BYTES else 0
+            keep = [1 if self.is_ckpt(cut) else small for cut in cuts]
+            keep[-1] = 1
             joins = None
             if join_with is not None:
-                joins = [(join_with.table(self._cut_of(p), cache), self.tr.tmask[self._cut_of(p)]) for p in pos]
+                joins = [(join_with.table(cut, cache), self.tr.tmask[cut]) for cut in cuts]
             rows, masks, weights = self._rows(pos, keep, joins)
-            out, kept, res = self.be.walk(tab, rows, masks, weights, self.K, self.max_states)
+            out, kept, res = self.be.walk(tab, rows, masks, weights, self.K, self.max_states,
+                                          want_res=join_with is not None)
             self.steps_done += len(pos)
-            for k, p in enumerate(pos):
-                cut = self._cut_of(p)
-                self.counts[cut] = int(out[k, 0])
-                self.changed_counts[cut] = int(out[k, 1])
-                self.peak = max(self.peak, int(out[k, 0]), int(out[k, 1]), int(out[k, 5]))
-                if join_with is not None and int(res[k]) != 0xFFFFFFFFFFFFFFFF:
+            for cut, a, b in zip(cuts, out[:, 0].tolist(), out[:, 1].tolist()):
+                self.counts[cut] = a
+                self.changed_counts[cut] = b
+            self.peak = max(self.peak, int(out[:, [0, 1, 5]].max()))
+            if join_with is not None:
+                ok = np.nonzero(res != U64(0xFFFFFFFFFFFFFFFF))[0]
+                if len(ok):
+                    k = int(ok[np.argmin(res[ok] >> U64(56))])      # the first least total
                     total = int(res[k]) >> 56
                     if best is None or total < best[0]:
-                        best = (total, cut, int(res[k]) & KEYMASK)
+                        best = (total, cuts[k], int(res[k]) & KEYMASK)
+            for k, t in kept.items():
+                if keep[k] == 1:
+                    if k != len(pos) - 1:
+                        self.ckpt[cuts[k]] = t
+                        ck_bytes += self.be.nbytes(t)
+                else:
+                    self.small_tabs[cuts[k]] = t
+                    self.small_bytes += 8 * (t.n + (1 << t.lg)) + 256
             tab = kept[len(pos) - 1]
             c = c1
             self.ckpt[c] = tab
@@ -727,7 +776,7 @@ class Sweep:
         if pos:
             keep = [1 if lo <= self._cut_of(p) <= hi else 0 for p in pos]
             rows, masks, weights = self._rows(pos, keep)
-            _, kept, _ = self.be.walk(tab, rows, masks, weights, self.K, self.max_states)
+            _, kept, _ = self.be.walk(tab, rows, masks, weights, self.K, self.max_states, want_res=False)
             for k, p in enumerate(pos):
                 if keep[k]:
                     out[self._cut_of(p)] = kept[k]
@@ -735,6 +784,9 @@ class Sweep:
 
     def table(self, c, cache):
         """Table at cut c for cuts requested against the sweep's direction (cache reused between calls)."""
+        t = self.small_tabs.get(c) or self.ckpt.get(c)
+        if t is not None:
+            return t
         if c not in cache:
             cache.clear()
             if self.direction < 0:
