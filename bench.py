@@ -302,7 +302,12 @@ def _finish_times(reqs):
     t0 = min(r.arrival for r in reqs)
     dense = [r.done - t0 for r in reqs if not isinstance(r, serve.SparseRequest)]
     sparse = [round(r.done - t0, 3) for r in reqs if isinstance(r, serve.SparseRequest)]
-    return {"dense_last": round(max(dense), 3), "sparse": sparse}
+    slow = sorted(reqs, key=lambda r: r.arrival - r.done)[:5]
+    return {"dense_last": round(max(dense), 3), "sparse": sparse,
+            "slowest": [[r.rid, "sparse" if isinstance(r, serve.SparseRequest) else
+                         "dense w%d x%d" % (max((pl.peak_bits for pl in r.plans if pl.feasible), default=0),
+                                            len(r.plans)),
+                         round(r.arrival - t0, 3), round((r.done - r.arrival) * 1e3, 1)] for r in slow]}
 
 
 def section_served(args):
