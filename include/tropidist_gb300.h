@@ -193,12 +193,16 @@ int tree_move(void *destination, const void *source, size_t bytes);
  * DEVICE arena.  leaves: rows (offset, size 1|2, column, nonzero); joins: rows (lo, ro, po, parent
  * rank, kernel generators, height >= 1, maps index, 0) in nondecreasing height; maps: uint32 (left,
  * right) state per generator.  info: heights, steps, launches per run, pairs, arena entries,
- * leaves, joins, single-block steps.  small_pairs (< 0: default): heights of at most that many pairs
- * run in one single-block launch; rbits (< 0: default): at most 2^rbits pairs per thread.  run:
- * target = HOST bit vector of a particular solution (ceil(ncols / 64) words); *value = root entry. */
+ * leaves, joins, single-block steps, block-product joins.  gemm: rows (join, F, mb, nb, kb, mapoff)
+ * of joins run as min-plus products of 2^mb left and 2^nb right rows of 2^F entries (2^kb of them),
+ * with their offset and parent vectors DL, DR, DT, PA, PB, PT (uint32) at gmaps[mapoff].
+ * small_pairs (< 0: default): heights of at most that many pairs run in one single-block launch;
+ * rbits (< 0: default): at most 2^rbits pairs per thread.  run: target = HOST bit vector of a
+ * particular solution (ceil(ncols / 64) words); *value = root entry. */
 void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins, int64_t njoins,
-                   const uint32_t *maps, int64_t nmaps, int64_t arena, int64_t root, int64_t ncols,
-                   int64_t small_pairs, int rbits, int *status);
+                   const uint32_t *maps, int64_t nmaps, const int64_t *gemm, int64_t ngemm, const uint32_t *gmaps,
+                   int64_t ngmaps, int64_t arena, int64_t root, int64_t ncols, int64_t small_pairs, int rbits,
+                   int *status);
 int tg_tree_plan_info(void *plan, int64_t *info, int n);
 int tg_tree_run(void *plan, void *arena, const uint64_t *target, uint32_t inf, uint32_t *value, void *stream);
 void tg_tree_plan_free(void *plan);

@@ -171,3 +171,30 @@ def test_tree_move_overlapping():
         assert L.tree_move(buf.data_ptr() + dst, buf.data_ptr() + src, nbytes) == 0
         torch.cuda.synchronize()
         assert np.array_equal(buf.cpu().numpy(), want), (src, dst, nbytes)
+
+
+def test_block_product_joins(td):
+    """Joins whose kernel generators are unit pairs and whose parents cover every pair of child
+    blocks run as min-plus block products (k_tree_gemm): against the oracle where it is affordable,
+    against the per-pair kernel elsewhere, on several targets each."""
+    from tropidist_gb300 import synth
+    rng = random.Random(12)
+    seen = 0
+    # chunks of 32 (F >= 5), 16 (F = 4), 8 (F = 3) and 4 (F = 2) entries per staging step: these
+    # trees run block products with F = 3 .. 9 and 2 (70 x 140, seeds 1 and 5)
+    for (m, n, win, seed), check in (((60, 120, 12, 3), "oracle"), ((80, 160, 10, 2), "oracle"),
+                                     ((80, 160, 12, 1), "oracle"), ((70, 140, 11, 1), "oracle"),
+                                     ((70, 140, 11, 5), "oracle"), ((120, 240, 12, 7), "device"),
+                                     ((90, 180, 11, 4), "device")):
+        p = synth.banded(m, n, win, 3, 1, seed=seed)
+        prog = td.CompiledTreeDP(p.h, balanced(list(range(n))))
+        info = prog.device_info()
+        assert info["block_product_joins"] >= 1
+        seen += info["block_product_joins"]
+        lim = dict(max_join_work=None, max_memory_bytes=None, max_seconds=None)
+        for t in [rng.randrange(1 << m) for _ in range(4)]:
+            got = prog.run(t, **lim)[0]
+            want = ot.run(prog, t) if check == "oracle" else prog.run(t, gemm=False, **lim)[0]
+            assert got == want, ((m, n, seed), t)
+        prog.free()
+    assert seen >= 14

@@ -33,7 +33,9 @@ namespace tg {
 struct TJoin {                 // one join of a tree plan (device)
     int64_t lo, ro, po;        // arena offsets (entries) of the left, right and parent tables
     int64_t block0;            // first block of this join in its launch (k_tree_join)
-    int32_t P, F, R, mapoff;   // parent rank, kernel generators, pair bits per thread, maps index
+    int32_t P, F, R, mapoff;   // parent rank, kernel generators, pair bits per thread (warp), maps index
+    int32_t W, pad;            // W = 1: the lanes of a warp take kernel generators 0..4 of one parent;
+                               // W = 2: a thread takes 2^R consecutive parents (F <= 4)
 };
 
 struct TFill { int64_t po, size, block0; };
@@ -142,7 +144,26 @@ __device__ __forceinline__ uint32_t gray_walk(uint32_t m, uint32_t li, uint32_t 
     return m;
 }
 
-__global__ void __launch_bounds__(TR_BS, 4) k_tree_join(const TJoin *joins, int nj, const uint32_t *maps,
+// 2^WW parents from base (bl, br): parent k (Gray order) toggles parent generator ctz(k); each
+// parent's 2^FF pairs from the inner generators gi; results stored in parent order
+template <int FF, int WW>
+__device__ __forceinline__ void parent_walk(uint32_t bl, uint32_t br, const uint32_t *sg, const uint32_t *gi,
+                                            const uint32_t *L, const uint32_t *Rt, uint32_t *out, uint32_t inf) {
+    uint32_t res[1 << WW];
+#pragma unroll
+    for (int k = 0; k < (1 << WW); k++) {
+        if (k) {
+            const int b = __ffs(k) - 1;                // a constant once unrolled
+            bl ^= sg[2 * b];
+            br ^= sg[2 * b + 1];
+        }
+        res[k ^ (k >> 1)] = min(gray_walk<FF>(inf, bl, br, gi, L, Rt), inf);
+    }
+#pragma unroll
+    for (int k = 0; k < (1 << WW); k++) out[k] = res[k];
+}
+
+__global__ void __launch_bounds__(TR_BS, 3) k_tree_join(const TJoin *joins, int nj, const uint32_t *maps,
                                                      uint32_t *arena, uint32_t inf) {
     __shared__ uint32_t sg[2 * TR_MAXJ];
     __shared__ int sj;
@@ -159,6 +180,78 @@ __global__ void __launch_bounds__(TR_BS, 4) k_tree_join(const TJoin *joins, int 
     const int J = d.P + d.F;
     for (int i = threadIdx.x; i < 2 * J; i += TR_BS) sg[i] = maps[2 * d.mapoff + i];
     __syncthreads();
+    if (d.W == 1) {
+        // warp mode (F >= 5): a warp takes 2^R pairs of one parent, lane l the pairs whose kernel
+        // generators 0..4 are the bits of l; with unit kernel generators the lanes read consecutive
+        // entries at every step
+        const int RW = d.R - 5, RI = min(RW, 6), RO = RW - RI;
+        const uint64_t nthr = 1ull << (J - d.R + 5);
+        const uint64_t u = ((uint64_t)blockIdx.x - (uint64_t)d.block0) * TR_BS + threadIdx.x;
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint64_t w = u >> 5, p = w & ((1ull << d.P) - 1ull);
+        uint32_t m = inf;
+        if (u < nthr) {
+            const uint64_t x0 = p | ((uint64_t)lane << d.P) | ((w >> d.P) << (d.P + d.R));
+            uint32_t bl = 0, br = 0;
+            for (uint64_t y = x0; y; y &= y - 1) {
+                const int b = __ffsll((long long)y) - 1;
+                bl ^= sg[2 * b];
+                br ^= sg[2 * b + 1];
+            }
+            const uint32_t *L = arena + d.lo, *Rt = arena + d.ro;
+            const uint32_t *gi = sg + 2 * (d.P + 5);
+            for (uint64_t q = 0; q < (1ull << RO); q++) {
+                if (q) {
+                    const int b = d.P + 5 + RI + __ffsll((long long)q) - 1;
+                    bl ^= sg[2 * b];
+                    br ^= sg[2 * b + 1];
+                }
+                switch (RI) {
+                    case 0: m = gray_walk<0>(m, bl, br, gi, L, Rt); break;
+                    case 1: m = gray_walk<1>(m, bl, br, gi, L, Rt); break;
+                    case 2: m = gray_walk<2>(m, bl, br, gi, L, Rt); break;
+                    case 3: m = gray_walk<3>(m, bl, br, gi, L, Rt); break;
+                    case 4: m = gray_walk<4>(m, bl, br, gi, L, Rt); break;
+                    case 5: m = gray_walk<5>(m, bl, br, gi, L, Rt); break;
+                    default: m = gray_walk<6>(m, bl, br, gi, L, Rt); break;
+                }
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, off));
+        if (lane == 0 && u < nthr) {
+            if (d.F == d.R) arena[d.po + p] = min(m, inf);
+            else if (m < inf) atomicMin(arena + d.po + p, m);
+        }
+        return;
+    }
+    if (d.W == 2) {
+        // small kernel (F <= 4, every parent's pairs in one thread): a thread walks 2^PW consecutive
+        // parents in Gray order (one parent generator toggled per parent), so the XOR of the first
+        // parent's generators is paid once per 2^PW parents; results go out as one vector
+        const int PW = d.R;                           // parent bits per thread
+        const uint64_t nthr = 1ull << (d.P - PW);
+        const uint64_t u = ((uint64_t)blockIdx.x - (uint64_t)d.block0) * TR_BS + threadIdx.x;
+        if (u >= nthr) return;
+        uint32_t bl = 0, br = 0;
+        for (uint64_t y = u << PW; y; y &= y - 1) {
+            const int b = __ffsll((long long)y) - 1;
+            bl ^= sg[2 * b];
+            br ^= sg[2 * b + 1];
+        }
+        const uint32_t *L = arena + d.lo, *Rt = arena + d.ro;
+        uint32_t *out = arena + d.po + (u << PW);
+        switch (d.F * 8 + PW) {
+#define TG_PW(FF, WW) case FF * 8 + WW: parent_walk<FF, WW>(bl, br, sg, sg + 2 * d.P, L, Rt, out, inf); break;
+            TG_PW(0, 0) TG_PW(0, 1) TG_PW(0, 2) TG_PW(0, 3) TG_PW(0, 4)
+            TG_PW(1, 0) TG_PW(1, 1) TG_PW(1, 2) TG_PW(1, 3) TG_PW(1, 4)
+            TG_PW(2, 0) TG_PW(2, 1) TG_PW(2, 2) TG_PW(2, 3) TG_PW(2, 4)
+            TG_PW(3, 0) TG_PW(3, 1) TG_PW(3, 2) TG_PW(3, 3) TG_PW(3, 4)
+            TG_PW(4, 0) TG_PW(4, 1) TG_PW(4, 2) TG_PW(4, 3) TG_PW(4, 4)
+#undef TG_PW
+            default: break;
+        }
+        return;
+    }
     const int R = d.R, RI = min(R, 6), RO = R - RI;
     const uint64_t nthr = 1ull << (J - R);
     const uint64_t u = ((uint64_t)blockIdx.x - (uint64_t)d.block0) * TR_BS + threadIdx.x;
@@ -174,6 +267,13 @@ __global__ void __launch_bounds__(TR_BS, 4) k_tree_join(const TJoin *joins, int 
             bl ^= sg[2 * b];
             br ^= sg[2 * b + 1];
         }
+        // start each lane at its own offset inside the inner walk (the same pairs in another order),
+        // so the lanes of a warp do not all touch the same offset of their blocks at once
+        for (uint32_t c = threadIdx.x & ((1u << RI) - 1u), b = 0; c; c >>= 1, b++)
+            if (c & 1u) {
+                bl ^= sg[2 * (d.P + b)];
+                br ^= sg[2 * (d.P + b) + 1];
+            }
         const uint32_t *L = arena + d.lo, *Rt = arena + d.ro;
         const uint32_t *gi = sg + 2 * d.P;             // the RI inner generators
         for (uint64_t q = 0; q < (1ull << RO); q++) {
@@ -202,6 +302,151 @@ __global__ void __launch_bounds__(TR_BS, 4) k_tree_join(const TJoin *joins, int 
         if ((threadIdx.x & 31) >= (1 << d.P)) return;
     }
     if (u < nthr && m < inf) atomicMin(arena + d.po + p, m);
+}
+
+// ---------------------------------------------------------------- joins as min-plus block products
+// When the kernel generators are the unit pairs (e_k, e_k) and every left block meets every right
+// block, parent p = PA a ^ PB b ^ PT t reads left row a and right row b (2^F entries each) with
+// XOR offsets DL a and DR b ^ DT t, and its value is min over f of L'[a][f] + R'[b][f]: a min-plus
+// matrix product, tiled through shared memory (a 64 x 64 tile of parents per block, 16 per thread,
+// K in chunks of 32 staged with the offsets applied), every parent written once.
+#define TG_T 64
+#define TG_KC 32
+#define TG_LD (TG_T + 4)
+
+struct TGemm {
+    int64_t lo, ro, po;                // arena offsets of the left, right and parent tables
+    int32_t F, mb, nb, kb;             // row length 2^F, 2^mb left rows, 2^nb right rows, 2^kb products
+    int32_t mapoff, pad;               // DL[mb] DR[nb] DT[kb] PA[mb] PB[nb] PT[kb] at gmaps[mapoff]
+};
+
+__device__ __forceinline__ uint32_t xor_bits(const uint32_t *v, int n, uint32_t x) {
+    uint32_t o = 0;
+    for (int i = 0; i < n; i++)
+        if ((x >> i) & 1u) o ^= v[i];
+    return o;
+}
+
+// PACK (INF < 2^15): right entries staged as 16-bit pairs, two parents per __viaddmin_u16x2 with
+// the left entry duplicated into both halves by an IMAD (FMA pipe); otherwise one per __viaddmin_u32.
+// KC = min(32, 2^F) entries of every row per chunk; the staging is double-buffered: chunk k + 1 is
+// loaded while chunk k is reduced.
+template <int N> struct Vec;
+template <> struct Vec<8> { using T = uint4; static constexpr int W = 2; };
+template <> struct Vec<4> { using T = uint4; static constexpr int W = 1; };
+template <> struct Vec<2> { using T = uint2; static constexpr int W = 1; };
+template <> struct Vec<1> { using T = uint32_t; static constexpr int W = 1; };
+
+template <int N>
+__device__ __forceinline__ void load_entries(const uint32_t *p, uint32_t (&v)[N]) {
+    if constexpr (N == 8) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(p)), b = __ldg(reinterpret_cast<const uint4 *>(p) + 1);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else if constexpr (N == 4) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(p));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    } else if constexpr (N == 2) {
+        const uint2 a = __ldg(reinterpret_cast<const uint2 *>(p));
+        v[0] = a.x; v[1] = a.y;
+    } else {
+        v[0] = __ldg(p);
+    }
+}
+
+template <bool PACK, int KC>
+__global__ void __launch_bounds__(256) k_tree_gemm(const __grid_constant__ TGemm G, const uint32_t *gmaps,
+                                                   uint32_t *arena, uint32_t inf) {
+    constexpr int NE = KC / 4;          // entries of a row staged by one thread per chunk
+    __shared__ __align__(16) uint32_t As[2][KC][TG_LD];
+    __shared__ __align__(16) uint32_t Bs[2][KC][PACK ? TG_LD / 2 : TG_LD];
+    __shared__ uint32_t dl[TG_T], dr[TG_T];
+    const uint32_t *DL = gmaps + G.mapoff, *DR = DL + G.mb, *DT = DR + G.nb;
+    const uint32_t *PA = DT + G.kb, *PB = PA + G.mb, *PT = PB + G.nb;
+    const uint32_t a0 = blockIdx.y * TG_T, b0 = blockIdx.x * TG_T, t = blockIdx.z;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (tid < TG_T) dl[tid] = xor_bits(DL, G.mb, a0 + tid);
+    else if (tid < 2 * TG_T) dr[tid - TG_T] = xor_bits(DR, G.nb, b0 + tid - TG_T) ^ xor_bits(DT, G.kb, t);
+    __syncthreads();
+    // staging: thread -> row r = tid / 4 of the tile, entries NE q .. NE q + NE - 1 of the chunk's
+    // aligned group; entry k0 + j of row a is L[a][(k0 + j) ^ dl] = group (k0 ^ (dl & ~(KC - 1))),
+    // element j ^ (dl & (KC - 1))
+    const int r = tid >> 2, q = tid & 3;
+    const uint32_t dla = dl[r], drb = dr[r];
+    const uint32_t *Lrow = arena + G.lo + ((uint64_t)(a0 + r) << G.F);
+    const uint32_t *Rrow = arena + G.ro + ((uint64_t)(b0 + r) << G.F);
+    const uint32_t nk = 1u << G.F, km = (uint32_t)KC - 1u;
+    uint32_t xa[NE], yb[NE];
+    auto fetch = [&](uint32_t k0) {
+        load_entries<NE>(Lrow + ((k0 ^ (dla & ~km)) + NE * q), xa);
+        load_entries<NE>(Rrow + ((k0 ^ (drb & ~km)) + NE * q), yb);
+    };
+    auto stage = [&](int buf) {
+#pragma unroll
+        for (int e = 0; e < NE; e++) {
+            As[buf][(NE * q + e) ^ (dla & km)][r] = xa[e];
+            if (PACK) reinterpret_cast<uint16_t *>(&Bs[buf][(NE * q + e) ^ (drb & km)][0])[r] = (uint16_t)yb[e];
+            else Bs[buf][(NE * q + e) ^ (drb & km)][r] = yb[e];
+        }
+    };
+    uint32_t acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = PACK ? (inf | (inf << 16)) : inf;
+    fetch(0);
+    stage(0);
+    __syncthreads();
+    int buf = 0;
+    for (uint32_t k0 = 0; k0 < nk; k0 += KC) {
+        const bool more = k0 + KC < nk;
+        if (more) fetch(k0 + KC);
+#pragma unroll 8
+        for (int kk = 0; kk < KC; kk++) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(&As[buf][kk][4 * ty]);
+            const uint32_t av[4] = {a.x, a.y, a.z, a.w};
+            if (PACK) {
+                const uint2 b = *reinterpret_cast<const uint2 *>(&Bs[buf][kk][2 * tx]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const uint32_t ad = av[i] * 0x10001u;
+                    acc[i][0] = __viaddmin_u16x2(ad, b.x, acc[i][0]);
+                    acc[i][1] = __viaddmin_u16x2(ad, b.y, acc[i][1]);
+                }
+            } else {
+                const uint4 b = *reinterpret_cast<const uint4 *>(&Bs[buf][kk][4 * tx]);
+                const uint32_t bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) acc[i][j] = __viaddmin_u32(av[i], bv[j], acc[i][j]);
+            }
+        }
+        if (more) stage(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
+    }
+    const uint32_t pt = xor_bits(PT, G.kb, t);
+    uint32_t pb[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) pb[j] = xor_bits(PB, G.nb, b0 + 4 * tx + j);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t pa = xor_bits(PA, G.mb, a0 + 4 * ty + i) ^ pt;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t v = PACK ? (acc[i][j >> 1] >> (16 * (j & 1))) & 0xFFFFu : acc[i][j];
+            arena[G.po + (pa ^ pb[j])] = min(v, inf);
+        }
+    }
+}
+
+template <bool PACK>
+static void launch_gemm(const TGemm &G, const uint32_t *gmaps, uint32_t *A, uint32_t inf, cudaStream_t s) {
+    const dim3 grid(1u << (G.nb - 6), 1u << (G.mb - 6), 1u << G.kb);
+    if (G.F >= 5) k_tree_gemm<PACK, 32><<<grid, 256, 0, s>>>(G, gmaps, A, inf);
+    else if (G.F == 4) k_tree_gemm<PACK, 16><<<grid, 256, 0, s>>>(G, gmaps, A, inf);
+    else if (G.F == 3) k_tree_gemm<PACK, 8><<<grid, 256, 0, s>>>(G, gmaps, A, inf);
+    else k_tree_gemm<PACK, 4><<<grid, 256, 0, s>>>(G, gmaps, A, inf);
 }
 
 // ---------------------------------------------------------------- reference per-call entry points
@@ -279,9 +524,10 @@ __global__ void k_tree_move(uint8_t *dst, const uint8_t *src, uint64_t bytes, ui
 
 // ---------------------------------------------------------------- plan
 struct TreeStep {
-    int kind;              // 0: k_tree_small over heights [h0, h1); 1: fill + join of height h0
+    int kind;              // 0: k_tree_small over heights [h0, h1); 1: fill + joins of height h0
     int h0, h1;
     int64_t j0, nj, blocks, f0, nf, fill_blocks;
+    std::vector<int64_t> gemms;   // block-product joins of this height (indexes into TreePlan::hg)
 };
 
 struct TreePlan {
@@ -293,6 +539,8 @@ struct TreePlan {
     uint32_t *d_maps = nullptr;
     uint64_t *d_target = nullptr;
     uint32_t *h_val = nullptr;      // pinned
+    uint32_t *d_gmaps = nullptr;
+    std::vector<TGemm> hg;
     std::vector<TreeStep> steps;
     int launches = 0;
 };
@@ -304,6 +552,7 @@ static void tree_plan_release(TreePlan *T) {
     cudaFree(T->d_joins);
     cudaFree(T->d_fills);
     cudaFree(T->d_maps);
+    cudaFree(T->d_gmaps);
     cudaFree(T->d_target);
     if (T->h_val) cudaFreeHost(T->h_val);
     delete T;
@@ -322,10 +571,18 @@ extern "C" {
 // ncols: column count (the target representative has ceil(ncols / 64) words).
 // small_pairs: heights of at most this many pairs run in the single-block kernel (< 0: 2^15);
 // rbits: pairs per thread 2^min(F, rbits) in the join kernel (< 0: enough threads for the GPU).
+// gemm: ngemm rows (join, F, mb, nb, kb, mapoff): joins run as min-plus block products, with their
+// DL, DR, DT, PA, PB, PT vectors (uint32) at gmaps[mapoff]; a row needs F >= 2, 6 <= mb, nb <= 21,
+// kb <= 16 and the join's F, parent rank and children's ranks to match.
 void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins, int64_t njoins,
-                   const uint32_t *maps, int64_t nmaps, int64_t arena, int64_t root, int64_t ncols,
-                   int64_t small_pairs, int rbits, int *status) {
+                   const uint32_t *maps, int64_t nmaps, const int64_t *gemm, int64_t ngemm, const uint32_t *gmaps,
+                   int64_t ngmaps, int64_t arena, int64_t root, int64_t ncols, int64_t small_pairs, int rbits,
+                   int *status) {
     if (small_pairs < 0) small_pairs = TR_SMALL_PAIRS;
+    if (ngemm < 0 || ngmaps < 0 || (ngemm && (!gemm || !gmaps))) {
+        if (status) *status = set_error(TG_ERR_ARG, "bad tree gemm rows");
+        return nullptr;
+    }
     int st = TG_OK;
     TreePlan *T = nullptr;
     if (nleaves < 0 || njoins < 0 || nmaps < 0 || arena < 1 || root < 0 || root >= arena || ncols < 0 ||
@@ -373,19 +630,58 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
             // pairs per thread: enough threads for the whole GPU, at most 2^11 pairs per thread
             const int J = P + F;
             hj[j].R = rbits >= 0 ? std::min(F, rbits) : std::min(F, std::max(std::min(F, 6), J - 19));
+            // F >= 5: warp mode, a warp per (parent, chunk of 2^R pairs); at least 5 + 1 bits, at most
+            // 2^11 pairs per lane, enough warps for the GPU
+            hj[j].W = F >= 5 ? 1 : 0;
+            hj[j].pad = 0;
+            if (hj[j].W)
+                hj[j].R = rbits >= 0 ? std::min(F, std::max(5, rbits))
+                                     : std::min(F, std::max(5 + std::min(F - 5, 6), std::min(J - 14, 16)));
+            else if (rbits < 0 && F <= 4 && P >= 18) {
+                // mode 2: R holds the parent bits per thread (up to 16 parents, >= 2^18 threads)
+                hj[j].W = 2;
+                hj[j].R = std::min(4, P - 18);
+            }
             T->pairs += 1ll << J;
         }
     }
     lvl.resize((size_t)hmax + 2, njoins);
     lvl[(size_t)hmax + 1] = njoins;
     T->nheights = hmax;
+    // block-product joins: checked against the join rows and the arena, then taken out of the
+    // join kernel's grid
+    std::vector<int> gemm_of((size_t)njoins, -1);
+    for (int64_t g = 0; g < ngemm && st == TG_OK; g++) {
+        const int64_t *r = gemm + 6 * g;
+        const int64_t j = r[0], F = r[1], mb = r[2], nb = r[3], kb = r[4], mo = r[5];
+        if (j < 0 || j >= njoins || gemm_of[j] >= 0 || F < 2 || F > 30 || mb < 6 || mb > 21 || nb < 6 || nb > 21 ||
+            kb < 0 || kb > 16 || mo < 0 || mo + 2 * (mb + nb + kb) > ngmaps || hj[j].F != F ||
+            hj[j].P != mb + nb + kb) {
+            st = set_error(TG_ERR_ARG, "bad tree gemm row");
+            break;
+        }
+        const int64_t lsz = 1ll << (mb + F), rsz = 1ll << (nb + F);
+        if (hj[j].lo + lsz > arena || hj[j].ro + rsz > arena || (hj[j].lo & 7) || (hj[j].ro & 7))
+            st = set_error(TG_ERR_ARG, "tree gemm reads outside the arena");
+        for (int64_t k = 0; k < mb + nb + kb && st == TG_OK; k++) {       // offsets below 2^F, parents below 2^P
+            if (gmaps[mo + k] >> F) st = set_error(TG_ERR_ARG, "tree gemm offset out of range");
+            if (hj[j].P < 32 && (gmaps[mo + mb + nb + kb + k] >> hj[j].P)) st = set_error(TG_ERR_ARG, "tree gemm parent out of range");
+        }
+        TGemm G;
+        G.lo = hj[j].lo; G.ro = hj[j].ro; G.po = hj[j].po;
+        G.F = (int32_t)F; G.mb = (int32_t)mb; G.nb = (int32_t)nb; G.kb = (int32_t)kb;
+        G.mapoff = (int32_t)mo; G.pad = 0;
+        gemm_of[j] = (int)T->hg.size();
+        T->hg.push_back(G);
+    }
     // steps: runs of small heights in one block, the others one launch each
     std::vector<TFill> fills;
     int64_t fill_block = 0;
     for (int h = 1; h <= hmax && st == TG_OK; h++) {
         int64_t pairs = 0;
         for (int64_t j = lvl[h]; j < lvl[h + 1]; j++) pairs += 1ll << (hj[j].P + hj[j].F);
-        if (pairs <= small_pairs) {
+        if (pairs <= small_pairs && lvl[h + 1] - lvl[h] <= 4) {     // a chain: one block, no launch per height
+            for (int64_t j = lvl[h]; j < lvl[h + 1]; j++) gemm_of[j] = -1;    // tiny: the single-block kernel
             if (!T->steps.empty() && T->steps.back().kind == 0 && T->steps.back().h1 == h) T->steps.back().h1 = h + 1;
             else { TreeStep s{}; s.kind = 0; s.h0 = h; s.h1 = h + 1; T->steps.push_back(s); }
             continue;
@@ -398,8 +694,10 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
         for (int64_t j = lvl[h]; j < lvl[h + 1]; j++) {
             TJoin &d = hj[j];
             d.block0 = blocks;
-            blocks += (int64_t)(((1ull << (d.P + d.F - d.R)) + TR_BS - 1) / TR_BS);
-            if (d.F > d.R) {
+            if (gemm_of[j] >= 0) { s.gemms.push_back(gemm_of[j]); continue; }   // no blocks in k_tree_join
+            const int tb = d.W == 2 ? d.P - d.R : d.P + d.F - d.R + (d.W ? 5 : 0);
+            blocks += (int64_t)(((1ull << tb) + TR_BS - 1) / TR_BS);
+            if (d.W != 2 && d.F > d.R) {
                 const int64_t size = 1ll << d.P;
                 fills.push_back(TFill{d.po, size, fill_block});
                 fill_block += (size + TR_BS * 8 - 1) / (TR_BS * 8);
@@ -426,6 +724,7 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
         alloc((void **)&T->d_fills, fills.size() * sizeof(TFill));
         alloc((void **)&T->d_maps, (size_t)nmaps * 8);
         alloc((void **)&T->d_target, (size_t)T->nwords * 8);
+        alloc((void **)&T->d_gmaps, (size_t)std::max<int64_t>(ngmaps, 1) * 4);
         if (!st && cudaMallocHost(&T->h_val, 64) != cudaSuccess) {
             cudaGetLastError();
             T->h_val = nullptr;
@@ -436,27 +735,30 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
         if (!st) st = cuda_check(cudaMemcpy(T->d_lvl, lvl.data(), lvl.size() * 8, cudaMemcpyHostToDevice), "heights");
         if (!st && !fills.empty()) st = cuda_check(cudaMemcpy(T->d_fills, fills.data(), fills.size() * sizeof(TFill), cudaMemcpyHostToDevice), "fills");
         if (!st && nmaps) st = cuda_check(cudaMemcpy(T->d_maps, maps, (size_t)nmaps * 8, cudaMemcpyHostToDevice), "maps");
+        if (!st && ngmaps) st = cuda_check(cudaMemcpy(T->d_gmaps, gmaps, (size_t)ngmaps * 4, cudaMemcpyHostToDevice), "gemm maps");
     }
     if (st) {
         tree_plan_release(T);
         T = nullptr;
     } else {
         T->launches = 1 + (nleaves ? 1 : 0);
-        for (const TreeStep &s : T->steps) T->launches += s.kind == 0 ? 1 : 1 + (s.nf ? 1 : 0);
+        for (const TreeStep &s : T->steps)
+            T->launches += s.kind == 0 ? 1 : (s.blocks ? 1 : 0) + (s.nf ? 1 : 0) + (int)s.gemms.size();
     }
     if (status) *status = st;
     return T;
 }
 
-// info: heights, steps, launches per run, pairs (join work), arena entries, nleaves, njoins, small steps
+// info: heights, steps, launches per run, pairs (join work), arena entries, nleaves, njoins, small steps,
+// block-product joins
 int tg_tree_plan_info(void *p, int64_t *info, int n) {
     TreePlan *T = static_cast<TreePlan *>(p);
     if (!T || !info) return set_error(TG_ERR_ARG, "null tree plan");
     int64_t small = 0;
     for (const TreeStep &s : T->steps) small += s.kind == 0;
-    const int64_t v[8] = {T->nheights, (int64_t)T->steps.size(), T->launches, T->pairs, T->arena, T->nleaves,
-                          T->njoins, small};
-    for (int i = 0; i < n && i < 8; i++) info[i] = v[i];
+    const int64_t v[9] = {T->nheights, (int64_t)T->steps.size(), T->launches, T->pairs, T->arena, T->nleaves,
+                          T->njoins, small, (int64_t)T->hg.size()};
+    for (int i = 0; i < n && i < 9; i++) info[i] = v[i];
     return TG_OK;
 }
 
@@ -478,7 +780,13 @@ int tg_tree_run(void *p, void *arena, const uint64_t *target, uint32_t inf, uint
             k_tree_small<<<1, 1024, 0, s>>>(T->d_joins, T->d_lvl, st.h0, st.h1, T->d_maps, A, inf);
         } else {
             if (st.nf) k_tree_fill<<<(unsigned)st.fill_blocks, TR_BS, 0, s>>>(T->d_fills + st.f0, (int)st.nf, A, inf);
-            k_tree_join<<<(unsigned)st.blocks, TR_BS, 0, s>>>(T->d_joins + st.j0, (int)st.nj, T->d_maps, A, inf);
+            if (st.blocks)
+                k_tree_join<<<(unsigned)st.blocks, TR_BS, 0, s>>>(T->d_joins + st.j0, (int)st.nj, T->d_maps, A, inf);
+            for (int64_t g : st.gemms) {
+                const TGemm &G = T->hg[(size_t)g];
+                if (inf < 32768u) launch_gemm<true>(G, T->d_gmaps, A, inf, s);
+                else launch_gemm<false>(G, T->d_gmaps, A, inf, s);
+            }
         }
     }
     e = cuda_check(cudaGetLastError(), "tree launches");

@@ -101,6 +101,17 @@ def _combine(vectors, bits):
     return out
 
 
+def _extend_basis(first, basis):
+    """A basis of span(basis) that starts with the independent vectors `first` (inside that span)."""
+    e = _Eliminator()
+    out = []
+    for v in tuple(first) + tuple(basis):
+        if e.add(v):
+            out.append(v)
+    assert len(out) == len(basis)
+    return tuple(out)
+
+
 def _intersect(a, b):
     """Basis of span(a) & span(b) for independent a and b: the a-part of every dependency of a + b."""
     e = _Eliminator(track=True)
@@ -316,6 +327,15 @@ class CompiledTreeDP:
             if nd.leaf is None:
                 outside[nd.left] = _span_basis(comp + space[nd.right])
                 outside[nd.right] = _span_basis(comp + space[nd.left])
+        # a child's table may be indexed in any basis of its interface; both children of a join take
+        # the basis of their common part first (in the same order), so the join's kernel generators
+        # become pairs of unit vectors (e_k, e_k): the pairs of one parent then read aligned blocks
+        # of 2^F entries of each child table
+        for i, nd in enumerate(self.nodes):
+            if nd.leaf is None:
+                common = _intersect(interfaces[nd.left], interfaces[nd.right])
+                interfaces[nd.left] = _extend_basis(common, interfaces[nd.left])
+                interfaces[nd.right] = _extend_basis(common, interfaces[nd.right])
         self.interfaces = tuple(interfaces)
 
         # generator maps of every join; the stack schedule of the reference's executor (its arena
@@ -332,9 +352,15 @@ class CompiledTreeDP:
             e = _Eliminator(track=True)
             for v in il + ir:
                 e.add(v)
-            pmaps = tuple(e.express(v) for v in interfaces[i])
+            pmaps = [e.express(v) for v in interfaces[i]]
             if any(m is None for m in pmaps):
                 raise AssertionError("parent interface must be contained in the child sum")
+            nf = len(e.dependencies)
+            if e.dependencies != [(1 << k) | (1 << (len(il) + k)) for k in range(nf)]:
+                raise AssertionError("kernel generators must be the common basis vectors")
+            # parent generators modulo the kernel: no left coordinate among the common ones
+            low = (1 << nf) - 1
+            pmaps = tuple(m ^ (m & low) ^ ((m & low) << len(il)) for m in pmaps)
             jn = TreeJoin(len(il), len(ir), prank, pmaps, tuple(e.dependencies))
             if jn.join_dimension != space_rank[nd.left] + space_rank[nd.right] + outside_rank[i] - self.matrix_rank:
                 raise AssertionError("compatible-pair dimension identity failed")
@@ -368,13 +394,11 @@ class CompiledTreeDP:
                   max_table_bits=None):
         """Table sizes and candidate-pair counts, with the reference's limits and accounting
         (cdist/tree_dp.py:371-406) plus the device figures of this executor."""
-        ranks = [len(v) for v in self.interfaces]
-        max_rank = max(ranks, default=0)
-        max_join = max((j.join_dimension for j in self.joins.values()), default=0)
-        work = sum(j.work for j in self.joins.values())
-        table_bytes = self.peak_live_entries * self.itemsize
-        scratch = 2 * max_join * 8
-        peak = table_bytes + scratch
+        base = self._device.get("profile")
+        if base is None:
+            base = self._device["profile"] = self._profile()
+        max_rank, max_join, work = base["max_interface_rank"], base["max_join_dimension"], base["join_work"]
+        table_bytes, peak = base["peak_live_table_bytes"], base["peak_dense_bytes"]
         why = []
         if max_rank >= 63 or max_join >= 63:
             why.append("table or join index requires at least 63 bits")
@@ -386,9 +410,19 @@ class CompiledTreeDP:
             why.append("dense workspace %d bytes exceeds max_memory_bytes=%d" % (peak, max_memory_bytes))
         if max_join_work is not None and work > max_join_work:
             why.append("join work %d exceeds max_join_work=%d" % (work, max_join_work))
-        dev = self._layout() if not why or max_rank < 63 else None
+        return dict(base, allowed=not why, rejection_reasons=why)
+
+    def _profile(self):
+        """The target- and limit-independent part of preflight (computed once)."""
+        ranks = [len(v) for v in self.interfaces]
+        max_rank = max(ranks, default=0)
+        max_join = max((j.join_dimension for j in self.joins.values()), default=0)
+        work = sum(j.work for j in self.joins.values())
+        table_bytes = self.peak_live_entries * self.itemsize
+        scratch = 2 * max_join * 8
+        peak = table_bytes + scratch
+        dev = self._layout() if max_rank < 63 else None
         return {
-            "allowed": not why, "rejection_reasons": why,
             "ncols": self.ncols, "matrix_rank": self.matrix_rank,
             "dtype": self.dtype, "dtype_bytes": self.itemsize, "infinity": self.infinity,
             "edge_state_dimensions": ranks, "max_interface_rank": max_rank,
@@ -441,26 +475,33 @@ class CompiledTreeDP:
                 A.release(off[nd.right], size[nd.right])
         leaves = np.array([[off[i], size[i], self.nodes[i].leaf, 1 if self.columns[self.nodes[i].leaf] else 0]
                            for i in by_h[0]], dtype=np.int64).reshape(-1, 4)
-        rows, maps = [], []
+        rows, maps, grows, gmaps = [], [], [], []
         for h in range(1, H + 1):
             for i in by_h[h]:
                 nd, jn = self.nodes[i], self.joins[i]
+                g = gemm_form(jn)
+                if g is not None and g["F"] >= 2 and 6 <= g["mb"] <= 21 and 6 <= g["nb"] <= 21 and g["kb"] <= 16:
+                    grows.append([len(rows), g["F"], g["mb"], g["nb"], g["kb"], len(gmaps)])
+                    for k in ("DL", "DR", "DT", "PA", "PB", "PT"):
+                        gmaps.extend(g[k])
                 rows.append([off[nd.left], off[nd.right], off[i], jn.parent_rank, len(jn.free_maps), h,
                              len(maps) // 2, 0])
                 lo = (1 << jn.left_rank) - 1
-                for g in jn.parent_maps + jn.free_maps:
-                    maps.append(g & lo)
-                    maps.append(g >> jn.left_rank)
+                for gen in jn.parent_maps + jn.free_maps:
+                    maps.append(gen & lo)
+                    maps.append(gen >> jn.left_rank)
         lay = {"heights": H, "arena": max(A.peak, 1), "peak_live": A.peak_live,
                "leaves": leaves, "joins": np.array(rows, dtype=np.int64).reshape(-1, 8),
-               "maps": np.array(maps, dtype=np.uint64), "root": off[self.root] if n else 0}
+               "maps": np.array(maps, dtype=np.uint64), "root": off[self.root] if n else 0,
+               "gemm": np.array(grows, dtype=np.int64).reshape(-1, 6), "gmaps": np.array(gmaps, dtype=np.uint32)}
         self._device["layout"] = lay
         return lay
 
-    def device_plan(self, small_pairs=-1, rbits=-1):
-        """The library's plan handle for this tree (built once per setting)."""
+    def device_plan(self, small_pairs=-1, rbits=-1, gemm=True):
+        """The library's plan handle for this tree (built once per setting); gemm: run the joins that
+        have the block-product form as min-plus block products."""
         from . import _lib
-        key = ("plan", small_pairs, rbits)
+        key = ("plan", small_pairs, rbits, gemm)
         if key in self._device:
             return self._device[key]
         lay = self._layout()
@@ -470,10 +511,14 @@ class CompiledTreeDP:
                                       % (max(ranks), DEVICE_INDEX_BITS))
         maps = np.ascontiguousarray(lay["maps"].astype(np.uint32))
         lv, jr = np.ascontiguousarray(lay["leaves"]), np.ascontiguousarray(lay["joins"])
+        gr = np.ascontiguousarray(lay["gemm"] if gemm else lay["gemm"][:0])
+        gm = np.ascontiguousarray(lay["gmaps"])
         st = ctypes.c_int(0)
         h = _lib.lib().tg_tree_plan(lv.ctypes.data if len(lv) else None, len(lv),
                                     jr.ctypes.data if len(jr) else None, len(jr),
                                     maps.ctypes.data if len(maps) else None, len(maps) // 2,
+                                    gr.ctypes.data if len(gr) else None, len(gr),
+                                    gm.ctypes.data if len(gm) else None, len(gm),
                                     int(lay["arena"]), int(lay["root"]), self.ncols, int(small_pairs), int(rbits),
                                     ctypes.byref(st))
         if not h:
@@ -481,11 +526,12 @@ class CompiledTreeDP:
         self._device[key] = h
         return h
 
-    def device_info(self, small_pairs=-1, rbits=-1):
+    def device_info(self, small_pairs=-1, rbits=-1, gemm=True):
         from . import _lib
-        info = np.zeros(8, dtype=np.int64)
-        _lib.check(_lib.lib().tg_tree_plan_info(self.device_plan(small_pairs, rbits), info.ctypes.data, 8))
-        keys = ("heights", "steps", "launches", "pairs", "arena_entries", "leaves", "joins", "single_block_steps")
+        info = np.zeros(9, dtype=np.int64)
+        _lib.check(_lib.lib().tg_tree_plan_info(self.device_plan(small_pairs, rbits, gemm), info.ctypes.data, 9))
+        keys = ("heights", "steps", "launches", "pairs", "arena_entries", "leaves", "joins", "single_block_steps",
+                "block_product_joins")
         return dict(zip(keys, (int(x) for x in info)))
 
     def free(self):
@@ -507,7 +553,7 @@ class CompiledTreeDP:
         return self.solver.express(target)
 
     def run(self, target=0, *, max_memory_bytes=DEFAULT_MEMORY_BYTES, max_join_work=DEFAULT_JOIN_WORK,
-            max_table_bits=None, max_seconds=60.0, backend="gpu", arena=None, small_pairs=-1, rbits=-1):
+            max_table_bits=None, max_seconds=60.0, backend="gpu", arena=None, small_pairs=-1, rbits=-1, gemm=True):
         """(exact minimum weight or None, stats), as cdist/tree_dp.py:409-501.  backend: "gpu" (or
         "c", the reference's name of its compiled executor); arena: an optional device buffer of at
         least device_arena_bytes, reused across calls."""
@@ -530,7 +576,7 @@ class CompiledTreeDP:
             raise TreeDPResourceError("tree DP exceeded max_seconds; no exact result returned", prof)
         from . import _lib, device
         device.require_gpu()
-        plan = self.device_plan(small_pairs, rbits)
+        plan = self.device_plan(small_pairs, rbits, gemm)
         need = prof["device_arena_bytes"]
         if arena is None or arena.numel() * arena.element_size() < need:
             try:
@@ -591,3 +637,38 @@ def preflight_tree_dp(h_cols, l_cols, mask, tree, *, max_compile_bytes=DEFAULT_M
     prog = CompiledTreeDP(cols, tree, max_compile_bytes=max_compile_bytes, max_compile_seconds=max_compile_seconds)
     return dict(prog.preflight(**limits), feasible=prog.representative(1 << nrows) is not None,
                 observable_mask=mask)
+
+
+def gemm_form(join):
+    """The block-product form of a join, or None.
+
+    With the kernel generators (e_k, e_k), parent p reads left entries (a(p) << F) | f and right
+    entries (b(p) << F) | (f ^ d(p)) for f < 2^F, where a, b, d are linear in p.  When p -> (a, b)
+    is onto (every left block meets every right block), p = PA a ^ PB b ^ PT t with t in the kernel of
+    that map, and d = DL a ^ DR b ^ DT t; with f' = f ^ DL a the parent's value is
+        min over f' of L[(a << F) | (f' ^ DL a)] + R[(b << F) | (f' ^ DR b ^ DT t)]
+    a min-plus product of 2^mb left rows and 2^nb right rows of length 2^F, once per t.
+    Returns dict(F, mb, nb, kb, DL, DR, DT, PA, PB, PT) (lists of ints, one per bit)."""
+    F = len(join.free_maps)
+    lr, rr, P = join.left_rank, join.right_rank, join.parent_rank
+    mb, nb = lr - F, rr - F
+    low = (1 << F) - 1
+    # per parent generator: its (a | b << mb) block coordinates and its d
+    ab, dd = [], []
+    for m in join.parent_maps:
+        left, right = m & ((1 << lr) - 1), m >> lr
+        if left & low:
+            return None
+        ab.append((left >> F) | ((right >> F) << mb))
+        dd.append(right & low)
+    e = _Eliminator(track=True)
+    for v in ab:
+        e.add(v)
+    if e.rank() != mb + nb:
+        return None
+    PA = [e.express(1 << i) for i in range(mb)]
+    PB = [e.express(1 << (mb + j)) for j in range(nb)]
+    PT = list(e.dependencies)
+    d_of = lambda comb: _combine(dd, comb)
+    return {"F": F, "mb": mb, "nb": nb, "kb": len(PT), "PA": PA, "PB": PB, "PT": PT,
+            "DL": [d_of(c) for c in PA], "DR": [d_of(c) for c in PB], "DT": [d_of(c) for c in PT]}
