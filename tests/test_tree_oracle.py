@@ -197,3 +197,12 @@ def test_deep_comb_compiles_without_recursion():
     prog = td.CompiledTreeDP([0] * 1300, comb(list(range(1300))))
     assert prog.preflight()["max_interface_rank"] == 0
     assert prog._layout()["heights"] == 1299
+
+
+def test_free_keeps_host_layout_and_profile():
+    prog = td.CompiledTreeDP([1, 2, 3, 1, 2, 3], ((0, (1, 2)), (3, (4, 5))))
+    a = prog.preflight()
+    prog._layout()
+    prog.free()
+    b = prog.preflight()
+    assert a == b and "layout" in prog._device and "profile" in prog._device

@@ -535,11 +535,13 @@ class CompiledTreeDP:
         return dict(zip(keys, (int(x) for x in info)))
 
     def free(self):
+        """Release the library's plan handles (the host layout and profile stay)."""
         from . import _lib
-        for k, v in list(self._device.items()):
-            if k != "layout" and v:
-                _lib.lib().tg_tree_plan_free(v)
-        self._device = {k: v for k, v in self._device.items() if k == "layout"}
+        plans = [k for k in self._device if isinstance(k, tuple) and k[0] == "plan"]
+        for k in plans:
+            if self._device[k]:
+                _lib.lib().tg_tree_plan_free(self._device[k])
+            del self._device[k]
 
     def __del__(self):
         try:
