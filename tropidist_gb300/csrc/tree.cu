@@ -35,7 +35,7 @@ struct TJoin {                 // one join of a tree plan (device)
     int64_t block0;            // first block of this join in its launch (k_tree_join)
     int32_t P, F, R, mapoff;   // parent rank, kernel generators, pair bits per thread (warp), maps index
     int32_t W, pad;            // W = 1: the lanes of a warp take kernel generators 0..4 of one parent;
-                               // W = 2: a thread takes 2^R consecutive parents (F <= 4)
+                               // W = 2 (F <= 4): 2^F lanes per parent, 2^R parents per lane
 };
 
 struct TFill { int64_t po, size, block0; };
@@ -144,23 +144,43 @@ __device__ __forceinline__ uint32_t gray_walk(uint32_t m, uint32_t li, uint32_t 
     return m;
 }
 
-// 2^WW parents from base (bl, br): parent k (Gray order) toggles parent generator ctz(k); each
-// parent's 2^FF pairs from the inner generators gi; results stored in parent order
-template <int FF, int WW>
-__device__ __forceinline__ void parent_walk(uint32_t bl, uint32_t br, const uint32_t *sg, const uint32_t *gi,
-                                            const uint32_t *L, const uint32_t *Rt, uint32_t *out, uint32_t inf) {
-    uint32_t res[1 << WW];
-#pragma unroll
-    for (int k = 0; k < (1 << WW); k++) {
-        if (k) {
-            const int b = __ffs(k) - 1;                // a constant once unrolled
+// The parents (pc << PW) | g, g < 2^PW, of one lane group (2^F lanes, lane f = pair f), pc = u >> F:
+// parent k of the walk (Gray order) toggles parent generator ctz(k); all lanes of the warp run the
+// same steps (the shuffles need them), lanes past nthr only compute dummies.
+template <int PW>
+__device__ __forceinline__ void group_walk(const TJoin &d, uint64_t u, uint64_t nthr, const uint32_t *sg,
+                                           const uint32_t *L, const uint32_t *Rt, uint32_t *arena, uint32_t inf) {
+    const int F = d.F;
+    const uint32_t f = threadIdx.x & ((1u << F) - 1u);
+    const bool active = u < nthr;
+    const uint64_t pc = u >> F;
+    uint32_t bl = 0, br = 0;
+    if (active)
+        for (uint64_t y = (pc << PW) | ((uint64_t)f << d.P); y; y &= y - 1) {
+            const int b = __ffsll((long long)y) - 1;
             bl ^= sg[2 * b];
             br ^= sg[2 * b + 1];
         }
-        res[k ^ (k >> 1)] = min(gray_walk<FF>(inf, bl, br, gi, L, Rt), inf);
-    }
+    uint32_t gl[PW > 0 ? PW : 1], gr[PW > 0 ? PW : 1];
 #pragma unroll
-    for (int k = 0; k < (1 << WW); k++) out[k] = res[k];
+    for (int b = 0; b < PW; b++) { gl[b] = sg[2 * b]; gr[b] = sg[2 * b + 1]; }
+    uint32_t res[1 << PW];
+#pragma unroll
+    for (int k = 0; k < (1 << PW); k++) {
+        if (k) {
+            const int b = __ffs(k) - 1;                // a constant once unrolled
+            bl ^= gl[b];
+            br ^= gr[b];
+        }
+        uint32_t v = active ? __ldg(L + bl) + __ldg(Rt + br) : inf;
+        for (int off = 1; off < (1 << F); off <<= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, off));
+        res[k ^ (k >> 1)] = min(v, inf);
+    }
+    if (active && f == 0) {
+        uint32_t *out = arena + d.po + (pc << PW);
+#pragma unroll
+        for (int k = 0; k < (1 << PW); k++) out[k] = res[k];
+    }
 }
 
 __global__ void __launch_bounds__(TR_BS, 3) k_tree_join(const TJoin *joins, int nj, const uint32_t *maps,
@@ -225,30 +245,20 @@ __global__ void __launch_bounds__(TR_BS, 3) k_tree_join(const TJoin *joins, int 
         return;
     }
     if (d.W == 2) {
-        // small kernel (F <= 4, every parent's pairs in one thread): a thread walks 2^PW consecutive
-        // parents in Gray order (one parent generator toggled per parent), so the XOR of the first
-        // parent's generators is paid once per 2^PW parents; results go out as one vector
-        const int PW = d.R;                           // parent bits per thread
-        const uint64_t nthr = 1ull << (d.P - PW);
+        // small kernel (F <= 4): a group of 2^F lanes takes one parent, lane f its pair f, so the
+        // group reads one aligned 2^F-entry block of each child (one sector); every thread walks 2^PW
+        // consecutive parents in Gray order (one parent generator toggled per parent, the XOR of the
+        // first parent's generators paid once), the group minimum comes from F shuffles, and the
+        // group's first lane writes its 2^PW parents as one vector
         const uint64_t u = ((uint64_t)blockIdx.x - (uint64_t)d.block0) * TR_BS + threadIdx.x;
-        if (u >= nthr) return;
-        uint32_t bl = 0, br = 0;
-        for (uint64_t y = u << PW; y; y &= y - 1) {
-            const int b = __ffsll((long long)y) - 1;
-            bl ^= sg[2 * b];
-            br ^= sg[2 * b + 1];
-        }
+        const uint64_t nthr = 1ull << (d.P - d.R + d.F);
         const uint32_t *L = arena + d.lo, *Rt = arena + d.ro;
-        uint32_t *out = arena + d.po + (u << PW);
-        switch (d.F * 8 + PW) {
-#define TG_PW(FF, WW) case FF * 8 + WW: parent_walk<FF, WW>(bl, br, sg, sg + 2 * d.P, L, Rt, out, inf); break;
-            TG_PW(0, 0) TG_PW(0, 1) TG_PW(0, 2) TG_PW(0, 3) TG_PW(0, 4)
-            TG_PW(1, 0) TG_PW(1, 1) TG_PW(1, 2) TG_PW(1, 3) TG_PW(1, 4)
-            TG_PW(2, 0) TG_PW(2, 1) TG_PW(2, 2) TG_PW(2, 3) TG_PW(2, 4)
-            TG_PW(3, 0) TG_PW(3, 1) TG_PW(3, 2) TG_PW(3, 3) TG_PW(3, 4)
-            TG_PW(4, 0) TG_PW(4, 1) TG_PW(4, 2) TG_PW(4, 3) TG_PW(4, 4)
-#undef TG_PW
-            default: break;
+        switch (d.R) {
+            case 0: group_walk<0>(d, u, nthr, sg, L, Rt, arena, inf); break;
+            case 1: group_walk<1>(d, u, nthr, sg, L, Rt, arena, inf); break;
+            case 2: group_walk<2>(d, u, nthr, sg, L, Rt, arena, inf); break;
+            case 3: group_walk<3>(d, u, nthr, sg, L, Rt, arena, inf); break;
+            default: group_walk<4>(d, u, nthr, sg, L, Rt, arena, inf); break;
         }
         return;
     }
@@ -637,10 +647,11 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
             if (hj[j].W)
                 hj[j].R = rbits >= 0 ? std::min(F, std::max(5, rbits))
                                      : std::min(F, std::max(5 + std::min(F - 5, 6), std::min(J - 14, 16)));
-            else if (rbits < 0 && F <= 4 && P >= 18) {
-                // mode 2: R holds the parent bits per thread (up to 16 parents, >= 2^18 threads)
+            else if (rbits < 0 && F <= 4 && P >= 14) {
+                // mode 2: lane groups of 2^F lanes; R holds the parents walked per thread (up to 16,
+                // keeping >= 2^14 groups)
                 hj[j].W = 2;
-                hj[j].R = std::min(4, P - 18);
+                hj[j].R = std::min(4, P - 14);
             }
             T->pairs += 1ll << J;
         }
@@ -695,7 +706,7 @@ void *tg_tree_plan(const int64_t *leaves, int64_t nleaves, const int64_t *joins,
             TJoin &d = hj[j];
             d.block0 = blocks;
             if (gemm_of[j] >= 0) { s.gemms.push_back(gemm_of[j]); continue; }   // no blocks in k_tree_join
-            const int tb = d.W == 2 ? d.P - d.R : d.P + d.F - d.R + (d.W ? 5 : 0);
+            const int tb = d.W == 2 ? d.P - d.R + d.F : d.P + d.F - d.R + (d.W ? 5 : 0);
             blocks += (int64_t)(((1ull << tb) + TR_BS - 1) / TR_BS);
             if (d.W != 2 && d.F > d.R) {
                 const int64_t size = 1ll << d.P;
