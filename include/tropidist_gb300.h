@@ -126,6 +126,13 @@ int64_t tg_sp_walk_scratch_bytes(uint64_t cap_n);
  * (cdist/trellis.py:20-36); columns as CSR lists of rows */
 int tg_rank_profile(int ncols, int nrows, const int64_t *col_ptr, const int32_t *col_rows, const int32_t *order,
                     int32_t *out);
+/* host planning (no GPU): the op stream of one dense query (the loop of cdist/trellis.py:147-182)
+ * from nrows bitset rows of `words` uint64 over column positions, the target row last; weights per
+ * position or NULL.  ops: int64 [cap][3] (expand 0,0,0 / update 1,mask,w / select 2,pos,target);
+ * widths: int32 [ncols]; columns: int32 [cap] (position of each update); out: ops, updates, peak.
+ * Returns 0, a negative status (-4: a mask beyond 63 rows), or the op count needed when > cap. */
+int tg_make_plan(int nrows, int ncols, int words, const uint64_t *rows, const int64_t *weights, int64_t *ops,
+                 int64_t cap, int32_t *widths, int32_t *columns, int64_t *out);
 /* host planning (no GPU): the lookahead classes of every cut (the per-cut loop of
  * cdist/sparse_dp.py:148-192), CSR inputs; see csrc/sparse.cu */
 int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,

@@ -72,3 +72,25 @@ def test_rank_profile_host_routine_matches_restatement():
     p = synth.circuit_dem(seed=2, rounds=6, checks=20, ncols=800)
     order = list(range(p.ncols))
     assert trellis.rank_profile(p.h, order) == trellis.rank_profile_py(p.h, order)
+
+
+def test_cpp_planner_matches_python_planner():
+    """tg_make_plan (C++) builds the op stream, widths and update positions of make_plan_py."""
+    import random
+    from tropidist_gb300 import trellis
+    rng = random.Random(3)
+    for t in range(200):
+        m, n = rng.randint(1, 12), rng.randint(1, 40)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(2) for _ in range(n)]
+        order = list(range(n))
+        rng.shuffle(order)
+        hrows = trellis.minimal_span_form(trellis.rows_from_columns(h, order, m))
+        lrow = trellis.reduce_target_row(trellis.target_row(l, 1, order), hrows)
+        w = [rng.randint(1, 3) for _ in range(n)] if t % 3 == 0 else None
+        a, b = trellis.make_plan(hrows, lrow, n, w), trellis.make_plan_py(hrows, lrow, n, w)
+        assert a.feasible == b.feasible
+        if a.feasible:
+            assert a.ops == b.ops and a.peak_bits == b.peak_bits and a.widths == b.widths
+            assert a.columns == b.columns and a.work() == b.work()
+            assert (a.encode() == b.encode()).all()

@@ -22,7 +22,6 @@ Weighted columns (the optional third field of an update) have no counterpart in 
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -164,23 +163,54 @@ def reduce_target_row(lrow, hrows):
     return lrow
 
 
-@dataclass
 class Plan:
-    ops: list                 # ("expand",) | ("update", mask[, w]) | ("select", pos, target)
-    peak_bits: int            # log2 of the largest table
-    widths: list              # active rows after each column
-    ncols: int
-    feasible: bool = True
-    columns: list = field(default_factory=list)   # position (in the order) of each update op
+    """Op stream of one query: ops ("expand",) | ("update", mask[, w]) | ("select", pos, target),
+    peak_bits (log2 of the largest table), widths (active rows after each column), columns (the
+    position in the order of each update op).  A plan built by the C++ planner holds the encoded
+    stream and makes the tuples only when `ops` is read."""
+
+    def __init__(self, ops, peak_bits, widths, ncols, feasible=True, columns=None, enc=None):
+        self._ops = ops
+        self._enc = enc
+        self.peak_bits = peak_bits
+        self.widths = widths
+        self.ncols = ncols
+        self.feasible = feasible
+        self.columns = [] if columns is None else columns
+
+    @property
+    def ops(self):
+        if self._ops is None:
+            self._ops = decode_ops(self._enc)
+        return self._ops
 
     def work(self):
         """Table entries touched by the update ops (the state-update count)."""
+        if self._enc is not None and self.peak_bits < 48:
+            code = self._enc[:, 0]
+            delta = (code == OP_EXPAND).astype(np.int64) - (code == OP_SELECT).astype(np.int64)
+            before = np.cumsum(delta) - delta
+            return int(np.sum(np.left_shift(np.int64(1), before[code == OP_UPDATE])))
         return plan_work(self.ops)
 
     def encode(self):
         """The op stream as an int64 array of (code, a, b) rows for the C-ABI:
         expand (0, 0, 0); update (1, mask, w); select (2, pos, target)."""
-        return encode_ops(self.ops)
+        if self._enc is None:
+            self._enc = encode_ops(self._ops)
+        return self._enc
+
+
+def decode_ops(enc):
+    out = []
+    for code, a, b in enc.tolist():
+        if code == OP_EXPAND:
+            out.append(("expand",))
+        elif code == OP_UPDATE:
+            out.append(("update", a) if b == 1 else ("update", a, b))
+        else:
+            out.append(("select", a, b))
+    return out
 
 
 def plan_work(ops):
@@ -213,7 +243,40 @@ def encode_ops(ops):
 
 def make_plan(hrows, lrow, ncols, weights=None):
     """Op stream of the sweep for constraint rows (target 0) and one target-1 row
-    (cdist/trellis.py:147-182).  weights: optional per-position column weight."""
+    (cdist/trellis.py:147-182), built by the library's C++ planner (tg_make_plan) from the rows as
+    bitsets.  weights: optional per-position column weight."""
+    if lrow == 0:
+        return Plan([], 0, [], ncols, feasible=False)
+    import ctypes
+    from . import _lib
+    rows = list(hrows) + [lrow]
+    words = max(1, (ncols + 63) // 64)
+    nb = 8 * words
+    buf = b"".join(r.to_bytes(nb, "little") for r in rows)
+    bits = np.frombuffer(buf, dtype=np.uint64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.int64)
+    widths = np.zeros(max(1, ncols), dtype=np.int32)
+    out = np.zeros(3, dtype=np.int64)
+    cap = 2 * len(rows) + ncols + 16
+    L = _lib.lib()
+    while True:
+        ops = np.zeros((cap, 3), dtype=np.int64)
+        cols = np.zeros(cap, dtype=np.int32)
+        r = L.tg_make_plan(len(rows), ncols, words, bits.ctypes.data, w.ctypes.data if w is not None else None,
+                           ops.ctypes.data, cap, widths.ctypes.data, cols.ctypes.data, out.ctypes.data)
+        if r == -4:
+            raise ValueError("update masks are limited to 63 bits")
+        if r < 0:
+            _lib.check(r)
+        if r == 0:
+            break
+        cap = r
+    n, nupd, peak = (int(x) for x in out)
+    return Plan(None, peak, widths[:ncols].tolist(), ncols, columns=cols[:nupd].tolist(), enc=ops[:n])
+
+
+def make_plan_py(hrows, lrow, ncols, weights=None):
+    """The same op stream built in Python (the cross-check of the C++ planner)."""
     if lrow == 0:
         return Plan([], 0, [], ncols, feasible=False)
     rows = list(hrows) + [lrow]
