@@ -131,3 +131,27 @@ def test_bound_data_host_routine_matches_restatement():
                 assert [int(v) for v in x[0]] == [int(v) for v in y[0]]
                 assert [int(v) for v in x[1]] == [int(v) for v in y[1]]
                 assert int(x[2]) == int(y[2])
+
+
+def test_trellis_cut_data_matches_plain_loops():
+    """The per-cut data of Trellis (built with array operations) against plain per-row loops:
+    active rows (start < c <= end), slot masks, widths, target masks, slot masks per position."""
+    from tropidist_gb300 import sparse_dp, synth
+    for p in (synth.circuit_dem(seed=2, rounds=10, checks=24, ncols=5000), synth.dense_small(1)):
+        order = sparse_dp.default_order(p)
+        tr = sparse_dp.Trellis.for_query(p, 0, order)
+        assert tr.feasible
+        N, nr = tr.N, len(tr.rows)
+        act = [[r for r in range(nr) if tr.start[r] < c <= tr.end[r]] for c in range(N + 1)]
+        assert tr.active_rows == act
+        assert tr.active == [sum(1 << tr.slot[r] for r in a) for a in act]
+        assert tr.width == [len(a) for a in act]
+        assert tr.tmask == [(1 << tr.slot[tr.L]) if tr.L in a else 0 for a in act]
+        col = [0] * N
+        for r, row in enumerate(tr.rows):
+            x = row
+            while x:
+                low = x & -x
+                col[low.bit_length() - 1] |= 1 << tr.slot[r]
+                x ^= low
+        assert tr.col == col

@@ -81,11 +81,14 @@ class Trellis:
         if nslots > 64:
             raise ValueError("trellis needs %d bits per state (at most 64 supported)" % nslots)
         self.slot, self.nslots = slot, nslots
-        col = [0] * N
-        for r, row in enumerate(rows):
-            for p in _bits(row):
-                col[p] |= 1 << slot[r]
-        self.col = col
+        nr = len(rows)
+        # positions of every row (CSR), and per position the slots of the rows through it
+        self.row_ptr, self.row_cols = trellis.bit_positions(rows, N)
+        entry_row = np.repeat(np.arange(nr, dtype=np.int64), np.diff(self.row_ptr))
+        sbit = np.left_shift(np.uint64(1), np.asarray(slot, dtype=np.uint64))
+        colm = np.zeros(max(1, N), dtype=U64)
+        np.bitwise_or.at(colm, self.row_cols, sbit[entry_row])
+        self.col = colm[:N].tolist()
         fsm, fsb, bsm, bsb = [0] * N, [0] * N, [0] * N, [0] * N
         starts_at, ends_at = [[] for _ in range(N)], [[] for _ in range(N)]
         for r in range(len(rows)):
@@ -99,22 +102,39 @@ class Trellis:
             ends_at[self.end[r]].append((slot[r], self.target[r]))
         self.fsel_mask, self.fsel_bits, self.bsel_mask, self.bsel_bits = fsm, fsb, bsm, bsb
         self.starts_at, self.ends_at = starts_at, ends_at
-        enter = [[] for _ in range(N + 2)]
-        leave = [[] for _ in range(N + 2)]
-        for r in range(len(rows)):
-            enter[self.start[r] + 1].append(r)
-            leave[self.end[r] + 1].append(r)
-        act, cur = [], set()
-        for c in range(N + 1):
-            cur.update(enter[c])
-            cur.difference_update(leave[c])
-            act.append(sorted(cur))
-        self.active_rows = act
-        self.active = [sum(1 << slot[r] for r in a) for a in act]
-        self.width = [len(a) for a in act]
-        ls = 1 << slot[self.L]
-        self.tmask = [ls if self.L in a else 0 for a in act]
+        # row r is active at the cuts start[r] < c <= end[r]: per cut the active rows (CSR, rows
+        # ascending), their slots as a mask (slots never overlap in time) and their number
+        st = np.asarray(self.start, dtype=np.int64)
+        en = np.asarray(self.end, dtype=np.int64)
+        ln = en - st
+        tot = int(ln.sum())
+        first = np.repeat(st + 1, ln)
+        off = np.arange(tot, dtype=np.int64) - np.repeat(np.cumsum(ln) - ln, ln)
+        cuts = first + off
+        rid = np.repeat(np.arange(nr, dtype=np.int64), ln)
+        o = np.lexsort((rid, cuts))
+        self.act_rows = rid[o].astype(np.int32)
+        self.act_ptr = np.zeros(N + 2, dtype=np.int64)
+        self.act_ptr[1:] = np.cumsum(np.bincount(cuts, minlength=N + 1))[:N + 1]
+        delta = np.zeros(N + 2, dtype=U64)
+        np.bitwise_xor.at(delta, st + 1, sbit)
+        np.bitwise_xor.at(delta, en + 1, sbit)
+        act_mask = np.bitwise_xor.accumulate(delta)[:N + 1]
+        self.active = act_mask.tolist()
+        self.width = np.diff(self.act_ptr).tolist()
+        lbit = int(sbit[self.L])         # the target row's own interval (its slot is shared over time)
+        sL, eL = self.start[self.L], self.end[self.L]
+        self.tmask = [lbit if sL < c <= eL else 0 for c in range(N + 1)]
         self._bd = {}
+
+    @property
+    def active_rows(self):
+        """The active rows of every cut (lists, rows ascending)."""
+        if getattr(self, "_active_rows", None) is None:
+            rows = self.act_rows.tolist()
+            ptr = self.act_ptr.tolist()
+            self._active_rows = [rows[ptr[c]:ptr[c + 1]] for c in range(self.N + 1)]
+        return self._active_rows
 
     @classmethod
     def for_query(cls, p, obs, order):
@@ -131,21 +151,14 @@ class Trellis:
         routine (tg_sp_bound_data; the same rule as _bound_data_py)."""
         N, rows = self.N, self.rows
         nr = len(rows)
-        rc = [_bits(row) for row in rows]
-        row_ptr = np.zeros(nr + 1, dtype=np.int64)
-        row_ptr[1:] = np.cumsum([len(x) for x in rc])
-        row_cols = np.array([j for x in rc for j in x], dtype=np.int32)
-        cr = [[] for _ in range(N)]
-        for r, x in enumerate(rc):
-            for j in x:
-                cr[j].append(r)
+        row_ptr, row_cols = self.row_ptr, self.row_cols
+        # the transpose: rows through every position, rows ascending
+        entry_row = np.repeat(np.arange(nr, dtype=np.int32), np.diff(row_ptr))
+        o = np.argsort(row_cols, kind="stable")
+        col_rows = entry_row[o]
         col_ptr = np.zeros(N + 1, dtype=np.int64)
-        col_ptr[1:] = np.cumsum([len(x) for x in cr])
-        col_rows = np.array([r for x in cr for r in x], dtype=np.int32)
-        act = [list(self.active_rows[c]) for c in range(N + 1)]
-        act_ptr = np.zeros(N + 2, dtype=np.int64)
-        act_ptr[1:] = np.cumsum([len(x) for x in act])
-        act_rows = np.array([r for x in act for r in x], dtype=np.int32)
+        col_ptr[1:] = np.cumsum(np.bincount(row_cols, minlength=N))[:N]
+        act_ptr, act_rows = self.act_ptr, self.act_rows
         start = np.array(self.start, dtype=np.int32)
         end = np.array(self.end, dtype=np.int32)
         slot = np.array(self.slot, dtype=np.int32)

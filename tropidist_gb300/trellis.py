@@ -33,17 +33,41 @@ def lowbit(x):
     return (x & -x).bit_length() - 1
 
 
+def bit_positions(values, nbits=None):
+    """Set-bit positions of many nonnegative ints at once: (ptr int64 [n + 1], pos int32), positions
+    ascending within each value (one byte scan instead of a big-int loop per bit)."""
+    n = len(values)
+    if nbits is None:
+        nbits = max((v.bit_length() for v in values), default=0)
+    nb = max(1, (nbits + 7) // 8)
+    B = np.frombuffer(b"".join(v.to_bytes(nb, "little") for v in values), dtype=np.uint8).reshape(n, nb)
+    r, k = np.nonzero(B)
+    U = np.unpackbits(B[r, k][:, None], axis=1, bitorder="little")
+    i, b = np.nonzero(U)
+    which = r[i]
+    pos = (k[i].astype(np.int64) * 8 + b).astype(np.int32)
+    ptr = np.zeros(n + 1, dtype=np.int64)
+    ptr[1:] = np.cumsum(np.bincount(which, minlength=n))
+    return ptr, pos
+
+
+_CSR = [None, None]     # key of the last column list given to rank_profile, its (nrows, col_ptr, col_rows)
+
+
+def _columns_csr(cols):
+    key = (len(cols), hash(tuple(cols)))
+    if _CSR[0] != key:
+        ptr, pos = bit_positions(cols)
+        nrows = int(pos.max()) + 1 if pos.size else 0
+        _CSR[0], _CSR[1] = key, (nrows, ptr, pos)
+    return _CSR[1]
+
+
 def rank_profile(cols, order):
     """r[i] = GF(2) rank of the first i columns of `order`, for i = 0..N (cdist/trellis.py:20-36),
     by the library's host routine (word-parallel bitsets; rank_profile_py restates it in Python)."""
-    import numpy as np
     from . import _lib
-    n = len(cols)
-    rows_of = [_set_bits(c) for c in cols]
-    nrows = max((r[-1] for r in rows_of if r), default=-1) + 1
-    col_ptr = np.zeros(n + 1, dtype=np.int64)
-    col_ptr[1:] = np.cumsum([len(r) for r in rows_of])
-    col_rows = np.array([x for r in rows_of for x in r], dtype=np.int32)
+    nrows, col_ptr, col_rows = _columns_csr(cols)
     order_a = np.ascontiguousarray(np.asarray(order, dtype=np.int32))
     out = np.zeros(len(order) + 1, dtype=np.int32)
     _lib.check(_lib.lib().tg_rank_profile(len(order), nrows, col_ptr.ctypes.data,
