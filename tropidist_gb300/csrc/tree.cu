@@ -7,14 +7,18 @@
 // x & (2^P - 1); the parent entry is the least left + right over its pairs (entries < INF =
 // ncols + 1; a finite sum never reaches INF, since the two subtrees' columns are disjoint).
 //
-// Device tables are uint32 in one arena.  A tree plan (host-built) lists the leaves and the joins
-// grouped by height: every join of one height runs in one launch, which is
+// Device tables are uint32 in one arena.  The host indexes both children of a join in bases that
+// start with their common part, so the kernel generators are unit pairs and a parent's pairs read
+// aligned 2^F-entry blocks of each child.  A tree plan (host-built) lists the leaves and the joins
+// grouped by height, all joins of one height in one launch of
 //   - k_tree_small: one block runs a whole run of consecutive small heights (a few thousand
 //     pairs each, e.g. the long spine of a comb tree) with a block barrier between heights;
-//   - k_tree_fill + k_tree_join: each thread walks 2^R pairs of one parent in Gray order (R <= F;
-//     inner 2^min(R,6) steps unrolled, so the generators sit in registers and all loads of a
-//     thread are independent), keeps the least sum and, when a parent's pairs span threads,
-//     reduces across the warp and commits with atomicMin into a table pre-filled with INF.
+//   - k_tree_gemm: a join whose parents cover every pair of child blocks, as a tiled min-plus
+//     matrix product of XOR-permuted child rows through shared memory;
+//   - k_tree_fill + k_tree_join for the other joins: lane groups of 2^F lanes per parent (F <= 4),
+//     a warp per parent (F >= 5), or per-thread Gray walks of 2^R pairs of one parent; when a
+//     parent's pairs span threads they are reduced across the warp and committed with atomicMin
+//     into a table pre-filled with INF.
 // The reference's per-call entry points (tree_join_u8/u16/u32/u64 over a pair range, tree_move)
 // are provided on device pointers with the reference's argument meaning.
 #include "tg_common.cuh"
@@ -341,12 +345,6 @@ __device__ __forceinline__ uint32_t xor_bits(const uint32_t *v, int n, uint32_t 
 // the left entry duplicated into both halves by an IMAD (FMA pipe); otherwise one per __viaddmin_u32.
 // KC = min(32, 2^F) entries of every row per chunk; the staging is double-buffered: chunk k + 1 is
 // loaded while chunk k is reduced.
-template <int N> struct Vec;
-template <> struct Vec<8> { using T = uint4; static constexpr int W = 2; };
-template <> struct Vec<4> { using T = uint4; static constexpr int W = 1; };
-template <> struct Vec<2> { using T = uint2; static constexpr int W = 1; };
-template <> struct Vec<1> { using T = uint32_t; static constexpr int W = 1; };
-
 template <int N>
 __device__ __forceinline__ void load_entries(const uint32_t *p, uint32_t (&v)[N]) {
     if constexpr (N == 8) {
