@@ -94,3 +94,23 @@ def test_cpp_planner_matches_python_planner():
             assert a.ops == b.ops and a.peak_bits == b.peak_bits and a.widths == b.widths
             assert a.columns == b.columns and a.work() == b.work()
             assert (a.encode() == b.encode()).all()
+
+
+def test_planner_edge_cases():
+    import pytest
+    from tropidist_gb300 import trellis
+    # 70 nested rows open at once: a mask on a row beyond position 63 is refused as by encode()
+    n = 160
+    hrows = [(1 << i) | (1 << (n - 1 - i)) for i in range(70)]
+    lrow = (1 << 70) | (1 << 89)
+    a = trellis.make_plan_py(hrows, lrow, n)
+    with pytest.raises(ValueError):
+        a.encode()
+    with pytest.raises(ValueError):
+        trellis.make_plan(hrows, lrow, n)
+    # an infeasible query and an empty problem
+    assert not trellis.make_plan([1], 0, 1).feasible
+    ptr, pos = trellis.bit_positions([])
+    assert ptr.tolist() == [0] and pos.size == 0
+    ptr, pos = trellis.bit_positions([0, 5, 0, 1 << 200])
+    assert ptr.tolist() == [0, 0, 2, 2, 3] and pos.tolist() == [0, 2, 200]
