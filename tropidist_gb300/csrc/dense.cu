@@ -753,6 +753,13 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
     for (auto c : P.ckpt_ops) is_ckpt[c] = 1;
     RowInfo RI;
     row_info(hops, RI, w_start);
+    // a segment record is several KB: reserve for about two updates per pass (passes fuse two or
+    // more updates; sweeps and relayouts are few) instead of growing by copies
+    {
+        int64_t nupd = 0;
+        for (const HostOp &o : hops) nupd += o.code == 1;
+        P.segs.reserve((size_t)std::min<int64_t>(nops + 8, nupd / 2 + 64 + 2 * nckpt));
+    }
 
     std::vector<int> canon;    // canonical order: position -> row (the positions the ops refer to)
     std::vector<int> phys;     // physical order of the table in memory
@@ -1085,6 +1092,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
         }
         P.segs.push_back(S);
     }
+    if (P.segs.capacity() > P.segs.size() + P.segs.size() / 4 + 16) P.segs.shrink_to_fit();
     P.final_buf = buf;
     return TG_OK;
 }
