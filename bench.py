@@ -54,7 +54,7 @@ def parse():
                     help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--tree-only", action="store_true",
                     help="run only the tree DP section (for profiling) and print its JSON")
-    ap.add_argument("--sections", default="batched,served,sparse,tree",
+    ap.add_argument("--sections", default="batched,served,sparse,tree,witness",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
 
@@ -441,7 +441,51 @@ def section_tree(args):
     return out
 
 
-SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse, "tree": section_tree}
+def section_witness(args):
+    """Witness traceback (cdist/auto.py:126-182): the columns of a minimum logical from device table
+    checkpoints and a bisection recomputation, on the banded m=1000 n=2000 window 30 problem (four
+    logical rows, natural order: 26-bit frontier), checked against H and L on the host.  The
+    reference keeps the table before every update (about 2000 tables of 64 MB here, beyond memory);
+    its traceback (restated in numpy, oracle/dense.py witness) is timed on the m=120 n=240 problem."""
+    import torch
+    from tropidist_gb300 import auto, synth, trellis
+    from tropidist_gb300.problem import verify_witness
+    p = synth.dense_scale(0, window=30)
+    order = list(range(p.ncols))
+    best, _ = auto.dp_distance(p, order)
+    auto.dp_witness(synth.dense_small(2), list(range(240)))       # warm-up (library, allocator)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = auto.dp_witness(p, order)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    cols = r["witness"]
+    out = {"workload": "banded m=1000 n=2000 col-weight 3 window 30 (seed 0), 4 logical rows, natural order",
+           "seconds": dt, "distance": r["distance"], "weight": len(cols), "observable": r["observable"],
+           "verified": bool(verify_witness(p, cols, r["observable"]) and len(cols) == r["distance"] == best),
+           "peak_bits": max(pl.peak_bits for _, pl in auto._plans(p, order) if pl.feasible)}
+    if not args.no_cpu_baseline:
+        from oracle import dense as od
+        q = synth.dense_small(1)
+        qo = list(range(q.ncols))
+        span = lambda h, o, m: trellis.minimal_span_form(trellis.rows_from_columns(h, o, m))
+        t0 = time.perf_counter()
+        w = od.witness(q.h, q.l, qo, q.nrows, 0, span, trellis.reduce_target_row, trellis.lowbit)
+        cpu = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = auto.dp_witness(q, qo, obs=0)
+        torch.cuda.synchronize()
+        out["small"] = {"workload": "banded m=120 n=240 window 16 (seed 1), logical row 0",
+                        "gpu_seconds": time.perf_counter() - t0, "cpu_seconds": cpu,
+                        "weights_equal": len(w) == len(g["witness"]),
+                        "cpu": "the reference's traceback (table before every update) restated in numpy, "
+                               "one core"}
+    return out
+
+
+SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse, "tree": section_tree,
+            "witness": section_witness}
 
 
 # ---------------------------------------------------------------------- GPU arm
