@@ -54,7 +54,7 @@ def parse():
                     help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--tree-only", action="store_true",
                     help="run only the tree DP section (for profiling) and print its JSON")
-    ap.add_argument("--sections", default="batched,served,sparse,tree,witness",
+    ap.add_argument("--sections", default="batched,served,sparse,tree,witness,search",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
 
@@ -484,8 +484,34 @@ def section_witness(args):
     return out
 
 
+def section_search(args):
+    """The weight-bounded search (cdist/search.py distance, completion table k = 2) with its probes
+    answered in waves by the device table, on the stim-free known-answer codes bb72 (Z, 12
+    observables, distance 6) and the rotated surface code d = 9 (Z)."""
+    import torch
+    from tropidist_gb300 import search
+    from tropidist_gb300.problem import Problem
+    codes = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "codes.json")))
+    out = {}
+    for name in ("bb72_Z", "surface_d9_Z"):
+        c = next(x for x in codes if x["name"] == name)
+        h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+        l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+        p = Problem(name, c["nrows"], c["nobs"], h, l, [(i, 0) for i in range(c["nrows"])])
+        search.distance(p, k_table=2, kmax=2)                     # warm-up (library, table kernels)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = search.distance(p, k_table=2, kmax=c["distance"])
+        dt = time.perf_counter() - t0
+        out[name] = {"distance": r["distance"], "known": c["distance"], "seconds": dt,
+                     "nodes": sum(sum(x["nodes"]) for x in r["runs"]), "lookups": sum(x["lookups"] for x in r["runs"]),
+                     "waves": sum(x["waves"] for x in r["runs"]), "false_hits": sum(x["false_hits"] for x in r["runs"]),
+                     "table_entries": r["table_entries"]}
+    return out
+
+
 SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse, "tree": section_tree,
-            "witness": section_witness}
+            "witness": section_witness, "search": section_search}
 
 
 # ---------------------------------------------------------------------- GPU arm

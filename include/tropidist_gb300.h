@@ -182,6 +182,21 @@ int tg_server_poll(void *server, int *slots, uint32_t *values, int max);
 int tg_server_stop(void *server);
 void tg_server_free(void *server);
 
+/* ---------------------------------------------------------------- weight-bounded search
+ * One threshold K of the search for a minimum logical (the DFS of cdist/gmitm.c:597-740 with the
+ * table probes collected into waves): columns as syndromes col[n][W], labels lg[n], table hashes
+ * zh/zl[n]; rows -> columns CSR (row_start[nrows + 1], row_cols), columns -> rows (col_start[n + 1],
+ * col_rows); rank[n] and the anchor columns in search order; kt the completion table's depth; probe
+ * answers a wave of m probes (least cost <= R[i] with hash (zh, zl)[i] and a label other than lg[i],
+ * or -1) and returns 0.  stats: nodes, lookups, hits, false hits, waves; sol / *nsol: the logical
+ * found.  Returns 1 found, 0 exhausted, 2 time limit (seconds > 0), or a negative status. */
+typedef int (*tg_probe_fn)(int64_t m, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, const int32_t *R,
+                           int32_t *out, void *ctx);
+int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint64_t *lg, const uint64_t *zh,
+              const uint64_t *zl, const int32_t *row_start, const int32_t *row_cols, const int32_t *col_start,
+              const int32_t *col_rows, const int32_t *rank, const int32_t *anchors, int nanchors, int K, int kt,
+              int64_t wave, tg_probe_fn probe, void *ctx, double seconds, int64_t *stats, int32_t *sol, int32_t *nsol);
+
 /* ---------------------------------------------------------------- tree DP (exact min-plus on a binary tree)
  * Per-call entry points with the reference's ctypes signatures (cdist/tree_dp.py:214-222), on DEVICE
  * tables: the pairs i in [start, stop) of a join in Gray order, out[parent] = min(out[parent], a + b)

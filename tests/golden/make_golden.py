@@ -18,6 +18,8 @@ next to this script; the test-suite reads only those files.
   tables.json         completion-table builds (count) and lookups of random syndromes
   tree_dp.json        the tree DP (cdist/tree_dp.py) on random matrices and trees, logical queries,
                       distances beyond 255, larger joins  (`make_golden.py tree` writes only this)
+  search.json         the weight-bounded search (cdist/search.py distance) on random problems
+                      (`make_golden.py search` writes only this)
 """
 from __future__ import annotations
 
@@ -371,9 +373,55 @@ def tree_main():
     shutil.rmtree(tmp, ignore_errors=True)
 
 
+def search_main():
+    """search.json: the reference's weight-bounded search (cdist/search.py distance, completion
+    table k = 2) on random problems, with brute-force truth where it is affordable."""
+    import itertools
+    tmp = tempfile.mkdtemp(prefix="tropi_ref_")
+    shutil.copytree(os.path.join(REF, "cdist"), os.path.join(tmp, "cdist"))
+    sys.path[:0] = [tmp]
+    from cdist import search
+    from cdist.problem import Problem
+
+    def brute(h, l):
+        n = len(h)
+        for w in range(1, n + 1):
+            for cols in itertools.combinations(range(n), w):
+                x = g = 0
+                for j in cols:
+                    x ^= h[j]
+                    g ^= l[j]
+                if x == 0 and g != 0:
+                    return w
+        return None
+
+    rng = random.Random(77)
+    cases = []
+    for t in range(60):
+        m = rng.randint(3, 14)
+        n = rng.randint(4, 30 if t % 2 else 14)
+        nobs = rng.randint(1, 3)
+        h = [sum(1 << r for r in rng.sample(range(m), rng.randint(1, min(3, m)))) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        p = Problem("rand%d" % t, m, nobs, h, l, [(i, 0) for i in range(m)])
+        r = search.distance(p, k_table=2, kmax=min(n, 12))
+        case = {"m": m, "n": n, "nobs": nobs, "h": h, "l": l, "k_table": 2, "kmax": min(n, 12),
+                "distance": r["distance"], "lower_bound": r["lower_bound"]}
+        if n <= 14:
+            case["brute"] = brute(h, l)
+        cases.append(case)
+    with open(os.path.join(HERE, "search.json"), "w") as f:
+        json.dump(cases, f, separators=(",", ":"))
+    print("wrote search.json", len(cases), "cases", os.path.getsize(os.path.join(HERE, "search.json")), "bytes")
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["tree"]:
         tree_main()
+    elif sys.argv[1:] == ["search"]:
+        search_main()
     else:
         main()
         tree_main()
+        search_main()

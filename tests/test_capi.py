@@ -8,6 +8,7 @@ from helpers import ROOT
 def declared_functions():
     text = open(os.path.join(ROOT, "include", "tropidist_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"typedef[^;]*;", "", text)            # function-pointer types are not exports
     names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text)
     return sorted({n for n in names if n not in ("if", "sizeof")})
 

@@ -1,0 +1,91 @@
+"""The weight-bounded search (tg_search) with its probes answered by the oracle's completion table:
+against the reference's own search (tests/golden/search.json, written by tests/golden/make_golden.py
+from cdist/search.py), brute force, and known code distances (tests/golden/codes.json)."""
+import itertools
+import json
+import os
+import random
+
+import numpy as np
+import pytest
+
+from helpers import ROOT
+from oracle import table as otab
+from tropidist_gb300 import search
+from tropidist_gb300.problem import Problem
+
+GOLD = json.load(open(os.path.join(ROOT, "tests", "golden", "search.json")))
+CODES = json.load(open(os.path.join(ROOT, "tests", "golden", "codes.json")))
+
+
+def oracle_probe(p, k, seed=12345):
+    zh, zl = search.column_hashes(p.h, search.row_hashes(p.nrows, seed))
+    wide = p.nobs > 16
+    tab = otab.entries(zh, zl, np.array(p.l, dtype=np.uint64), k, wide=wide)
+
+    def probe(pzh, pzl, plg, R):
+        return [otab.lookup(tab, a, b, c, wide=wide) for a, b, c in zip(pzl, plg, R)]
+    return probe
+
+
+def problem(m, n, nobs, h, l, name="p"):
+    return Problem(name, m, nobs, list(h), list(l), [(i, 0) for i in range(m)])
+
+
+def brute(h, l):
+    for w in range(1, len(h) + 1):
+        for cols in itertools.combinations(range(len(h)), w):
+            x = g = 0
+            for j in cols:
+                x ^= h[j]
+                g ^= l[j]
+            if x == 0 and g != 0:
+                return w
+    return None
+
+
+@pytest.mark.parametrize("case", range(len(GOLD)))
+def test_reference_search_distances(case):
+    c = GOLD[case]
+    p = problem(c["m"], c["n"], c["nobs"], c["h"], c["l"])
+    r = search.distance(p, k_table=c["k_table"], kmax=c["kmax"], probe=oracle_probe(p, c["k_table"]), wave=64)
+    assert r["distance"] == c["distance"]
+    assert r["lower_bound"] == c["lower_bound"]
+    for s in r["solutions"]:
+        syn, lg = p.check(list(s))
+        assert syn == 0 and lg != 0 and len(s) == r["distance"]
+
+
+def test_brute_force_every_table_depth_and_wave():
+    rng = random.Random(5)
+    for t in range(120):
+        m, n, nobs = rng.randint(1, 10), rng.randint(1, 13), rng.randint(1, 3)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        p = problem(m, n, nobs, h, l)
+        k = t % 3
+        r = search.distance(p, k_table=k, kmax=n, probe=oracle_probe(p, k), wave=1 + t % 9)
+        assert r["distance"] == brute(h, l), t
+        if r["distance"] is not None:
+            (s,) = r["solutions"]
+            syn, lg = p.check(list(s))
+            assert syn == 0 and lg != 0 and len(s) == r["distance"]
+
+
+@pytest.mark.parametrize("name", ["bb72_Z", "surface_d9_Z"])
+def test_known_code_distances(name):
+    c = next(x for x in CODES if x["name"] == name)
+    h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+    l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+    p = problem(c["nrows"], len(h), c["nobs"], h, l, name)
+    r = search.distance(p, k_table=2, kmax=c["distance"], probe=oracle_probe(p, 2))
+    assert r["distance"] == c["distance"]
+    assert [x["status"] for x in r["runs"]] == ["exhausted"] * (c["distance"] - 1) + ["found"]
+
+
+def test_unsupported_modes_raise():
+    p = problem(2, 3, 1, [1, 2, 3], [1, 0, 0])
+    with pytest.raises(NotImplementedError):
+        search.distance(p, enum_all=True, probe=oracle_probe(p, 2))
+    with pytest.raises(NotImplementedError):
+        search.distance(p, labelfree=True, probe=oracle_probe(p, 2))

@@ -3,6 +3,10 @@ import ctypes as c
 
 vp, u64, i64, ci = c.c_void_p, c.c_uint64, c.c_int64, c.c_int
 
+# the probe callback of tg_search: (m, zh, zl, lg, R, out, ctx) -> 0
+PROBE_FN = c.CFUNCTYPE(ci, i64, c.POINTER(c.c_uint64), c.POINTER(c.c_uint64), c.POINTER(c.c_uint64),
+                       c.POINTER(c.c_int32), c.POINTER(c.c_int32), vp)
+
 SIGNATURES = {
     "tg_sp_clear": (ci, [vp, u64, vp]),
     "tg_sp_step": (ci, [vp, u64, vp, ci, vp, ci, vp, u64, vp, u64, u64, u64, u64, ci, ci, ci, ci, ci, ci, ci,
@@ -32,6 +36,8 @@ SIGNATURES = {
     "tg_server_poll": (ci, [vp, vp, vp, ci]),
     "tg_server_stop": (ci, [vp]),
     "tg_server_free": (None, [vp]),
+    "tg_search": (ci, [ci, ci, ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, ci, ci, ci, i64, PROBE_FN, vp,
+                       c.c_double, vp, vp, vp]),
     "tree_join_u8": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),
     "tree_join_u16": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),
     "tree_join_u32": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),

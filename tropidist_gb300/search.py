@@ -120,3 +120,116 @@ class Table:
             self.free()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------- the search
+def _search_arrays(p: Problem):
+    """Columns as W-word syndromes, rows -> columns and columns -> rows (CSR), largest column weight."""
+    from .trellis import bit_positions
+    n, m = p.ncols, p.nrows
+    W = max(1, (m + 63) // 64)
+    col = np.frombuffer(b"".join(int(a).to_bytes(8 * W, "little") for a in p.h), dtype=np.uint64).reshape(n, W) \
+        if n else np.zeros((0, W), dtype=np.uint64)
+    col_start, col_rows = bit_positions(list(p.h), m)
+    entry_col = np.repeat(np.arange(n, dtype=np.int32), np.diff(col_start))
+    o = np.argsort(col_rows, kind="stable")
+    row_cols = entry_col[o].astype(np.int32)
+    row_start = np.zeros(m + 1, dtype=np.int64)
+    row_start[1:] = np.cumsum(np.bincount(col_rows, minlength=m))[:m]
+    wmax = int(np.diff(col_start).max()) if n else 1
+    return (W, np.ascontiguousarray(col), row_start.astype(np.int32), np.ascontiguousarray(row_cols),
+            col_start.astype(np.int32), np.ascontiguousarray(col_rows.astype(np.int32)), max(1, wmax))
+
+
+def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=None, enum_all=False, time_limit=0.0,
+             log=None, start=1, exclusions=True, on_run=None, table_load=0.5, kernel=None, cover=False,
+             labelfree=None, wave=1 << 16, probe=None, seed=12345):
+    """Exact distance by iterative deepening over the threshold K (cdist/search.py:387-441): per K a
+    depth-first search over column sets, the completion table of all subsets of at most k_table
+    columns answering the last levels (tg_search; the probes of many nodes go to the device table in
+    one wave of up to `wave` probes).  Returns the reference's record: k_table, table_entries,
+    table_seconds, runs (per K: status, best, nodes, lookups, hits, false_hits, seconds),
+    lower_bound, distance (None if none <= kmax), solutions, solutions_complete.
+
+    exclusions, cover and kernel are prunings of the reference's search: accepted, not applied (the
+    result does not depend on them).  enum_all, relaxed tables and label-free search (more than 64
+    observables) are not provided.  probe: a callable (zh, zl, lg, R) -> costs answering the probes
+    instead of the device table (the tests plug in the oracle's table)."""
+    import ctypes
+    from ._sigs_extra import PROBE_FN
+    if enum_all or relaxed:
+        raise NotImplementedError("enum_all and relaxed tables are not provided by this search")
+    if labelfree or p.nobs > 64:
+        raise NotImplementedError("label-free search (more than 64 observables) is not provided")
+    W, col, row_start, row_cols, col_start, col_rows, wmax = _search_arrays(p)
+    n = p.ncols
+    rank_a = np.ascontiguousarray(np.asarray(rank if rank is not None else range(n), dtype=np.int32))
+    anch = np.ascontiguousarray(np.asarray(anchors if anchors is not None else range(n), dtype=np.int32))
+    lg = np.ascontiguousarray(np.array([int(x) for x in p.l], dtype=np.uint64)) if n else np.zeros(1, np.uint64)
+    table = None
+    out = {"k_table": k_table, "table_entries": None, "table_seconds": 0.0, "exclusion_pairs": 0, "runs": [],
+           "lower_bound": start, "distance": None, "solutions": [], "solutions_complete": False}
+    if probe is None:
+        table = Table(p, k_table, seed=seed, load=table_load)
+        zh, zl = table.zh, table.zl
+        look = table.lookup
+        out["table_entries"], out["table_seconds"] = table.entries, table.build_seconds
+        if log:
+            log(f"  table k={k_table}: {table.entries} entries in 2^{table.log2slots} slots "
+                f"({table.build_seconds:.1f}s)")
+    else:
+        zh, zl = column_hashes(p.h, row_hashes(p.nrows, seed))
+        look = probe
+    zh, zl = np.ascontiguousarray(zh, dtype=np.uint64), np.ascontiguousarray(zl, dtype=np.uint64)
+
+    def answer(m, pzh, pzl, plg, pR, res, _ctx):
+        try:
+            a = [np.ctypeslib.as_array(x, shape=(m,)).copy() for x in (pzh, pzl, plg, pR)]
+            np.ctypeslib.as_array(res, shape=(m,))[:] = np.asarray(look(a[0], a[1], a[2], a[3]), dtype=np.int32)
+            return 0
+        except Exception:                 # reported to the search, which stops with an error
+            return 1
+
+    cb = PROBE_FN(answer)
+    L = _lib.lib()
+    stats = np.zeros(8, dtype=np.int64)
+    sol = np.zeros(64, dtype=np.int32)
+    nsol = np.zeros(1, dtype=np.int32)
+    ptr = lambda a: a.ctypes.data if a.size else None
+    try:
+        for K in range(start, kmax + 1):
+            check_threshold(K)
+            t0 = time.time()
+            r = L.tg_search(W, n, p.nrows, wmax, ptr(col), ptr(lg), ptr(zh), ptr(zl), ptr(row_start), ptr(row_cols),
+                            ptr(col_start), ptr(col_rows), ptr(rank_a), ptr(anch), len(anch), K, k_table, int(wave),
+                            cb, None, float(time_limit), stats.ctypes.data, sol.ctypes.data, nsol.ctypes.data)
+            if r < 0:
+                _lib.check(r)
+            status = {1: "found", 0: "exhausted", 2: "timeout"}[r]
+            s = sorted(int(x) for x in sol[:int(nsol[0])]) if r == 1 else []
+            best = len(s) if r == 1 else None
+            rec = {"K": K, "status": status, "best": best, "nodes": [int(stats[0])], "lookups": int(stats[1]),
+                   "hits": int(stats[2]), "false_hits": int(stats[3]), "waves": int(stats[4]),
+                   "seconds": time.time() - t0, "tasks": 0, "cover_pruned": 0,
+                   "nsol_recorded": 1 if r == 1 else 0, "nsol_found": 1 if r == 1 else 0,
+                   "solutions_complete": False}
+            out["runs"].append(rec)
+            if log:
+                log(f"  K={K}: {status} best={best} nodes={int(stats[0])} lookups={int(stats[1])} "
+                    f"false_hits={int(stats[3])} {rec['seconds']:.2f}s")
+            if on_run:
+                on_run(rec)
+            if r == 2:
+                break
+            if r == 1:
+                syn, lgx = p.check(s)
+                assert syn == 0 and lgx != 0 and len(set(s)) == len(s), "reported solution failed verification"
+                out["distance"] = best
+                out["solutions"] = [tuple(s)]
+                out["lower_bound"] = best
+                break
+            out["lower_bound"] = K + 1
+    finally:
+        if table is not None:
+            table.free()
+    return out
