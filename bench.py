@@ -487,13 +487,13 @@ def section_witness(args):
 def section_search(args):
     """The weight-bounded search (cdist/search.py distance, completion table k = 2) with its probes
     answered in waves by the device table, on the stim-free known-answer codes bb72 (Z, 12
-    observables, distance 6) and the rotated surface code d = 9 (Z)."""
+    observables, distance 6) and the rotated surface codes d = 9 and 15 (Z)."""
     import torch
     from tropidist_gb300 import search
     from tropidist_gb300.problem import Problem
     codes = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "codes.json")))
     out = {}
-    for name in ("bb72_Z", "surface_d9_Z"):
+    for name in ("bb72_Z", "surface_d9_Z", "surface_d15_Z"):
         c = next(x for x in codes if x["name"] == name)
         h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
         l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]

@@ -26,7 +26,7 @@ def test_reference_search_distances_on_device():
                 assert syn == 0 and lg != 0
 
 
-@pytest.mark.parametrize("name", ["bb72_Z", "surface_d9_Z"])
+@pytest.mark.parametrize("name", ["bb72_Z", "surface_d9_Z", "surface_d15_Z"])
 def test_known_code_distances_on_device(name):
     c = next(x for x in CODES if x["name"] == name)
     h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
