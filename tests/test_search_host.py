@@ -89,3 +89,25 @@ def test_unsupported_modes_raise():
         search.distance(p, enum_all=True, probe=oracle_probe(p, 2))
     with pytest.raises(NotImplementedError):
         search.distance(p, labelfree=True, probe=oracle_probe(p, 2))
+
+
+def test_time_limit_start_and_orders():
+    c = next(x for x in CODES if x["name"] == "bb72_Z")
+    h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+    l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+    p = problem(c["nrows"], len(h), c["nobs"], h, l, "bb72")
+    probe = oracle_probe(p, 2)
+    # a certified lower bound as the start skips the thresholds below it
+    r = search.distance(p, k_table=2, kmax=6, start=5, probe=probe)
+    assert r["distance"] == 6 and [x["K"] for x in r["runs"]] == [5, 6]
+    # any rank order and the anchors in any order give the same distance
+    rng = random.Random(3)
+    rank = list(range(p.ncols))
+    rng.shuffle(rank)
+    anchors = sorted(range(p.ncols), key=lambda j: rank[j])
+    r = search.distance(p, k_table=2, kmax=6, start=6, probe=probe, rank=rank, anchors=anchors)
+    assert r["distance"] == 6
+    # a time limit passed during a wave stops the threshold with status "timeout" and no distance
+    slow = lambda zh, zl, lg, R: (__import__("time").sleep(0.01), probe(zh, zl, lg, R))[1]
+    r = search.distance(p, k_table=1, kmax=6, start=6, probe=slow, wave=2, time_limit=1e-6)
+    assert r["runs"][-1]["status"] == "timeout" and r["distance"] is None and r["lower_bound"] == 6

@@ -115,6 +115,7 @@ struct Search {
         waves++;
         pout.assign((size_t)m, -1);
         if (probe(m, pzh.data(), pzl.data(), plg.data(), pR.data(), pout.data(), ctx) != 0) failed = true;
+        if (limited && std::chrono::steady_clock::now() > deadline) timeout = true;
         for (int64_t i = 0; i < m && !found && !failed; i++) {
             if (pout[(size_t)i] < 0) continue;
             hits++;
