@@ -76,15 +76,6 @@ def rank_profile(cols, order):
     return out.tolist()
 
 
-def _set_bits(x):
-    out = []
-    while x:
-        low = x & -x
-        out.append(low.bit_length() - 1)
-        x ^= low
-    return out
-
-
 def rank_profile_py(cols, order):
     """Python restatement of rank_profile (cdist/trellis.py:20-36)."""
     pivots = {}
