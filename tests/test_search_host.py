@@ -111,3 +111,24 @@ def test_time_limit_start_and_orders():
     slow = lambda zh, zl, lg, R: (__import__("time").sleep(0.01), probe(zh, zl, lg, R))[1]
     r = search.distance(p, k_table=1, kmax=6, start=6, probe=slow, wave=2, time_limit=1e-6)
     assert r["runs"][-1]["status"] == "timeout" and r["distance"] is None and r["lower_bound"] == 6
+
+
+def test_threads_share_anchors_with_the_same_results():
+    rng = random.Random(11)
+    for t in range(60):
+        m, n, nobs = rng.randint(1, 10), rng.randint(1, 13), rng.randint(1, 3)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        p = problem(m, n, nobs, h, l)
+        r = search.distance(p, k_table=t % 3, kmax=n, probe=oracle_probe(p, t % 3), wave=1 + t % 5, threads=4)
+        assert r["distance"] == brute(h, l), t
+        for s in r["solutions"]:
+            syn, lg = p.check(list(s))
+            assert syn == 0 and lg != 0 and len(s) == r["distance"]
+    for name in ("bb72_Z", "surface_d9_Z"):
+        c = next(x for x in CODES if x["name"] == name)
+        h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+        l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+        p = problem(c["nrows"], len(h), c["nobs"], h, l, name)
+        r = search.distance(p, k_table=2, kmax=c["distance"], probe=oracle_probe(p, 2), threads=8)
+        assert r["distance"] == c["distance"]

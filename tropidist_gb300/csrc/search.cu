@@ -12,8 +12,11 @@
 #include "tg_capi.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 namespace tg {
@@ -38,6 +41,9 @@ struct Search {
     tg_probe_fn probe;
     void *ctx;
     bool found = false, timeout = false, failed = false;
+    std::atomic<int> *stop = nullptr;     // shared by the threads of one search: set when one stops
+    std::mutex *mu = nullptr;             // one wave at a time through the probe
+    bool halted() const { return found || timeout || failed || (stop && stop->load(std::memory_order_relaxed)); }
     std::vector<int> sol;
     int64_t nodes = 0, lookups = 0, hits = 0, false_hits = 0, waves = 0;
     std::chrono::steady_clock::time_point deadline;
@@ -114,7 +120,11 @@ struct Search {
         if (!m) return;
         waves++;
         pout.assign((size_t)m, -1);
-        if (probe(m, pzh.data(), pzl.data(), plg.data(), pR.data(), pout.data(), ctx) != 0) failed = true;
+        {
+            std::unique_lock<std::mutex> lock;
+            if (mu) lock = std::unique_lock<std::mutex>(*mu);
+            if (probe(m, pzh.data(), pzl.data(), plg.data(), pR.data(), pout.data(), ctx) != 0) failed = true;
+        }
         if (limited && std::chrono::steady_clock::now() > deadline) timeout = true;
         for (int64_t i = 0; i < m && !found && !failed; i++) {
             if (pout[(size_t)i] < 0) continue;
@@ -149,7 +159,7 @@ struct Search {
         store.clear(); node_off.clear(); node_len.clear();
     }
     void dfs(int d) {
-        if (found || timeout || failed) return;
+        if (halted()) return;
         nodes++;
         if (limited && (nodes & 4095) == 0 && std::chrono::steady_clock::now() > deadline) { timeout = true; return; }
         const uint64_t *s = S(d);
@@ -209,7 +219,7 @@ struct Search {
                 forbid(f, stamp);
                 push(d, f);
                 dfs(d + 1);
-                if (found || timeout || failed) break;
+                if (halted()) break;
             }
         }
         for (int q = row_start[piv]; q < row_start[piv + 1]; q++)
@@ -230,50 +240,81 @@ extern "C" {
 // kt: the completion table holds every subset of at most kt columns; probe(m, zh, zl, lg, R, out,
 // ctx) answers a wave of probes (least cost <= R with the same hash and another label, or -1).
 // stats: nodes, lookups, hits, false hits, waves.  sol: the logical's columns (sorted), *nsol its
-// size.  Returns 1 found, 0 exhausted, 2 time limit, or a negative status (-6: the probe call failed).
+// size; threads: threads sharing out the anchors (the probe is entered by one at a time).  Returns 1
+// found, 0 exhausted, 2 time limit, or a negative status (-6: the probe call failed).
 int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint64_t *lg, const uint64_t *zh,
               const uint64_t *zl, const int32_t *row_start, const int32_t *row_cols, const int32_t *col_start,
               const int32_t *col_rows, const int32_t *rank, const int32_t *anchors, int nanchors, int K, int kt,
-              int64_t wave, tg_probe_fn probe, void *ctx, double seconds, int64_t *stats, int32_t *sol, int32_t *nsol) {
+              int64_t wave, tg_probe_fn probe, void *ctx, int threads, double seconds, int64_t *stats, int32_t *sol,
+              int32_t *nsol) {
     if (W < 1 || n < 0 || nrows < 0 || K < 1 || K > 64 || kt < 0 || !col || !lg || !zh || !zl || !row_start ||
         !col_start || !rank || (nanchors && !anchors) || !probe || !stats || !sol || !nsol || wave < 1)
         return set_error(TG_ERR_ARG, "bad search arguments");
-    Search X;
-    X.W = W; X.n = n; X.K = K; X.kt = kt; X.wmax = std::max(1, wmax);
-    X.col = col; X.lg = lg; X.zh = zh; X.zl = zl;
-    X.row_start = row_start; X.row_cols = row_cols; X.col_start = col_start; X.col_rows = col_rows;
-    X.forb.assign((size_t)n, 0);
-    X.avail.assign((size_t)nrows, 0);
-    X.syn.assign((size_t)(K + 2) * W, 0);
-    X.g.assign((size_t)K + 2, 0); X.hz.assign((size_t)K + 2, 0); X.lz.assign((size_t)K + 2, 0);
-    X.path.assign((size_t)K + 2, -1);
-    X.wave = wave; X.probe = probe; X.ctx = ctx;
-    if (seconds > 0) {
-        X.limited = true;
-        X.deadline = std::chrono::steady_clock::now() +
-                     std::chrono::microseconds((int64_t)(seconds * 1e6));
+    for (int a = 0; a < nanchors; a++)
+        if (anchors[a] < 0 || anchors[a] >= n) return set_error(TG_ERR_ARG, "anchor out of range");
+    const int T = std::max(1, std::min(threads, std::max(1, nanchors)));
+    std::atomic<int> stop(0), next(0);
+    std::mutex mu;
+    std::vector<Search> Xs((size_t)T);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::microseconds((int64_t)(seconds * 1e6));
+    for (Search &X : Xs) {
+        X.W = W; X.n = n; X.K = K; X.kt = kt; X.wmax = std::max(1, wmax);
+        X.col = col; X.lg = lg; X.zh = zh; X.zl = zl;
+        X.row_start = row_start; X.row_cols = row_cols; X.col_start = col_start; X.col_rows = col_rows;
+        X.forb.assign((size_t)n, 0);
+        X.avail.assign((size_t)nrows, 0);
+        X.syn.assign((size_t)(K + 2) * W, 0);
+        X.g.assign((size_t)K + 2, 0); X.hz.assign((size_t)K + 2, 0); X.lz.assign((size_t)K + 2, 0);
+        X.path.assign((size_t)K + 2, -1);
+        X.wave = wave; X.probe = probe; X.ctx = ctx;
+        X.limited = seconds > 0;
+        X.deadline = deadline;
+        X.stop = &stop;
+        X.mu = &mu;
     }
-    for (int a = 0; a < nanchors && !X.found && !X.timeout && !X.failed; a++) {
-        const int f0 = anchors[a];
-        if (f0 < 0 || f0 >= n) return set_error(TG_ERR_ARG, "anchor out of range");
-        for (int r = 0; r < nrows; r++) X.avail[(size_t)r] = row_start[r + 1] - row_start[r];
-        std::fill(X.forb.begin(), X.forb.end(), 0);
-        for (int f = 0; f < n; f++)
-            if (rank[f] < rank[f0]) X.forbid(f, 255);
-        X.forbid(f0, 254);
-        X.push(0, f0);
-        X.dfs(1);
+    // anchors are handed out one at a time; each thread searches below its anchors with its own
+    // forbidden set and wave
+    auto work = [&](Search &X) {
+        while (!X.halted()) {
+            const int a = next.fetch_add(1);
+            if (a >= nanchors) break;
+            const int f0 = anchors[a];
+            for (int r = 0; r < nrows; r++) X.avail[(size_t)r] = row_start[r + 1] - row_start[r];
+            std::fill(X.forb.begin(), X.forb.end(), 0);
+            for (int f = 0; f < n; f++)
+                if (rank[f] < rank[f0]) X.forbid(f, 255);
+            X.forbid(f0, 254);
+            X.push(0, f0);
+            X.dfs(1);
+        }
+        if (!X.halted()) X.flush();
+        if (X.found || X.timeout || X.failed) stop.store(1);
+    };
+    if (T == 1) {
+        work(Xs[0]);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; t++) pool.emplace_back(work, std::ref(Xs[(size_t)t]));
+        for (auto &th : pool) th.join();
     }
-    if (!X.found && !X.timeout && !X.failed) X.flush();
-    stats[0] = X.nodes; stats[1] = X.lookups; stats[2] = X.hits; stats[3] = X.false_hits; stats[4] = X.waves;
+    int64_t tot[5] = {0, 0, 0, 0, 0};
+    bool any_timeout = false, any_failed = false;
+    const Search *hit = nullptr;
+    for (const Search &X : Xs) {
+        tot[0] += X.nodes; tot[1] += X.lookups; tot[2] += X.hits; tot[3] += X.false_hits; tot[4] += X.waves;
+        any_timeout |= X.timeout;
+        any_failed |= X.failed;
+        if (X.found && !hit) hit = &X;
+    }
+    for (int i = 0; i < 5; i++) stats[i] = tot[i];
     *nsol = 0;
-    if (X.found) {
-        for (size_t i = 0; i < X.sol.size() && i < 64; i++) sol[i] = X.sol[i];
-        *nsol = (int32_t)X.sol.size();
+    if (hit) {
+        for (size_t i = 0; i < hit->sol.size() && i < 64; i++) sol[i] = hit->sol[i];
+        *nsol = (int32_t)hit->sol.size();
         return 1;
     }
-    if (X.failed) return set_error(TG_ERR_STATE, "the probe call failed");
-    return X.timeout ? 2 : 0;
+    if (any_failed) return set_error(TG_ERR_STATE, "the probe call failed");
+    return any_timeout ? 2 : 0;
 }
 
 }  // extern "C"

@@ -143,7 +143,7 @@ def _search_arrays(p: Problem):
 
 def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=None, enum_all=False, time_limit=0.0,
              log=None, start=1, exclusions=True, on_run=None, table_load=0.5, kernel=None, cover=False,
-             labelfree=None, wave=1 << 16, probe=None, seed=12345):
+             labelfree=None, wave=1 << 16, probe=None, seed=12345, threads=1):
     """Exact distance by iterative deepening over the threshold K (cdist/search.py:387-441): per K a
     depth-first search over column sets, the completion table of all subsets of at most k_table
     columns answering the last levels (tg_search; the probes of many nodes go to the device table in
@@ -154,7 +154,8 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
     exclusions, cover and kernel are prunings of the reference's search: accepted, not applied (the
     result does not depend on them).  enum_all, relaxed tables and label-free search (more than 64
     observables) are not provided.  probe: a callable (zh, zl, lg, R) -> costs answering the probes
-    instead of the device table (the tests plug in the oracle's table)."""
+    instead of the device table (the tests plug in the oracle's table).  threads: host threads that
+    share out the anchors of each threshold (the probes still go out one wave at a time)."""
     import ctypes
     from ._sigs_extra import PROBE_FN
     if enum_all or relaxed:
@@ -202,7 +203,8 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
             t0 = time.time()
             r = L.tg_search(W, n, p.nrows, wmax, ptr(col), ptr(lg), ptr(zh), ptr(zl), ptr(row_start), ptr(row_cols),
                             ptr(col_start), ptr(col_rows), ptr(rank_a), ptr(anch), len(anch), K, k_table, int(wave),
-                            cb, None, float(time_limit), stats.ctypes.data, sol.ctypes.data, nsol.ctypes.data)
+                            cb, None, int(threads), float(time_limit), stats.ctypes.data, sol.ctypes.data,
+                            nsol.ctypes.data)
             if r < 0:
                 _lib.check(r)
             status = {1: "found", 0: "exhausted", 2: "timeout"}[r]
