@@ -132,3 +132,34 @@ def test_threads_share_anchors_with_the_same_results():
         p = problem(c["nrows"], len(h), c["nobs"], h, l, name)
         r = search.distance(p, k_table=2, kmax=c["distance"], probe=oracle_probe(p, 2), threads=8)
         assert r["distance"] == c["distance"]
+
+
+def test_partner_exclusions_keep_the_distance():
+    """Columns that sum to another column (with the label) are partners; forbidding them below each
+    other changes no distance (a minimum logical never holds both) and prunes nodes."""
+    rng = random.Random(21)
+    pruned = 0
+    for t in range(60):
+        m, n, nobs = rng.randint(2, 8), rng.randint(3, 13), rng.randint(1, 2)
+        h = [rng.randrange(1, 1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        # plant sums: some columns are the XOR of two others (with their labels)
+        for _ in range(rng.randint(0, 3)):
+            a, b = rng.sample(range(len(h)), 2)
+            h.append(h[a] ^ h[b])
+            l.append(l[a] ^ l[b])
+        p = problem(m, len(h), nobs, h, l)
+        probe = oracle_probe(p, 1)
+        a = search.distance(p, k_table=1, kmax=len(h), probe=probe, exclusions=True)
+        b = search.distance(p, k_table=1, kmax=len(h), probe=probe, exclusions=False)
+        assert a["distance"] == b["distance"] == brute(h, l), t
+        na, nb = (sum(x["nodes"][0] for x in r["runs"]) for r in (a, b))
+        assert na <= nb
+        pruned += nb - na
+        if a["exclusion_pairs"]:
+            # partners lie on a zero-sum triple: a third column is their XOR, labels included
+            ex_start, ex_cols, _ = search.partners(p)
+            for f in range(p.ncols):
+                for y in ex_cols[ex_start[f]:ex_start[f + 1]].tolist():
+                    assert any(p.h[j] == p.h[f] ^ p.h[y] and p.l[j] == p.l[f] ^ p.l[y] for j in range(p.ncols))
+    assert pruned > 0

@@ -25,6 +25,7 @@ struct Search {
     int W, n, K, kt, wmax;
     const uint64_t *col, *lg, *zh, *zl;
     const int32_t *row_start, *row_cols, *col_start, *col_rows;
+    const int32_t *ex_start = nullptr, *ex_cols = nullptr;   // partners: f ^ y is a column with f's and y's label
     std::vector<uint8_t> forb;             // 0 free, else the stamp that forbade the column
     std::vector<int> avail;                // free columns per row
     std::vector<uint64_t> syn;             // per depth: W words
@@ -64,6 +65,15 @@ struct Search {
         if (!forb[f]) return;
         forb[f] = 0;
         for (int q = col_start[f]; q < col_start[f + 1]; q++) avail[col_rows[q]]++;
+    }
+    // a minimum logical holding f holds none of f's partners: forbid them below f (undone by the caller)
+    static constexpr uint8_t PARTNER = 253;
+    void exclude(int f, std::vector<int> &undo) {
+        if (!ex_start) return;
+        for (int q = ex_start[f]; q < ex_start[f + 1]; q++) {
+            const int y = ex_cols[q];
+            if (!forb[(size_t)y]) { forbid(y, PARTNER); undo.push_back(y); }
+        }
     }
     void push(int d, int f) {          // state d + 1 = state d with column f
         const uint64_t *a = S(d);
@@ -213,12 +223,16 @@ struct Search {
                 add_probe(hz[d] ^ zh[f], lz[d] ^ zl[f], g[d] ^ lg[f], R - 1, node, f);
             }
         } else {
+            std::vector<int> undo;
             for (int q = row_start[piv]; q < row_start[piv + 1]; q++) {
                 const int f = row_cols[q];
                 if (forb[f]) continue;
                 forbid(f, stamp);
                 push(d, f);
+                undo.clear();
+                exclude(f, undo);
                 dfs(d + 1);
+                for (int y : undo) unforbid(y);
                 if (halted()) break;
             }
         }
@@ -240,13 +254,15 @@ extern "C" {
 // kt: the completion table holds every subset of at most kt columns; probe(m, zh, zl, lg, R, out,
 // ctx) answers a wave of probes (least cost <= R with the same hash and another label, or -1).
 // stats: nodes, lookups, hits, false hits, waves.  sol: the logical's columns (sorted), *nsol its
-// size; threads: threads sharing out the anchors (the probe is entered by one at a time).  Returns 1
+// size; ex_start / ex_cols (or NULL): each column's partners (columns y with f ^ y equal to a column of
+// the same label: a minimum logical never holds both; cdist/search.py:207-231), forbidden below f;
+// threads: threads sharing out the anchors (the probe is entered by one at a time).  Returns 1
 // found, 0 exhausted, 2 time limit, or a negative status (-6: the probe call failed).
 int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint64_t *lg, const uint64_t *zh,
               const uint64_t *zl, const int32_t *row_start, const int32_t *row_cols, const int32_t *col_start,
               const int32_t *col_rows, const int32_t *rank, const int32_t *anchors, int nanchors, int K, int kt,
-              int64_t wave, tg_probe_fn probe, void *ctx, int threads, double seconds, int64_t *stats, int32_t *sol,
-              int32_t *nsol) {
+              int64_t wave, tg_probe_fn probe, void *ctx, const int32_t *ex_start, const int32_t *ex_cols, int threads,
+              double seconds, int64_t *stats, int32_t *sol, int32_t *nsol) {
     if (W < 1 || n < 0 || nrows < 0 || K < 1 || K > 64 || kt < 0 || !col || !lg || !zh || !zl || !row_start ||
         !col_start || !rank || (nanchors && !anchors) || !probe || !stats || !sol || !nsol || wave < 1)
         return set_error(TG_ERR_ARG, "bad search arguments");
@@ -271,6 +287,8 @@ int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint
         X.deadline = deadline;
         X.stop = &stop;
         X.mu = &mu;
+        X.ex_start = ex_start;
+        X.ex_cols = ex_cols;
     }
     // anchors are handed out one at a time; each thread searches below its anchors with its own
     // forbidden set and wave
@@ -285,6 +303,8 @@ int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint
                 if (rank[f] < rank[f0]) X.forbid(f, 255);
             X.forbid(f0, 254);
             X.push(0, f0);
+            std::vector<int> undo;
+            X.exclude(f0, undo);
             X.dfs(1);
         }
         if (!X.halted()) X.flush();

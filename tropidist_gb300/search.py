@@ -141,6 +141,33 @@ def _search_arrays(p: Problem):
             col_start.astype(np.int32), np.ascontiguousarray(col_rows.astype(np.int32)), max(1, wmax))
 
 
+def partners(p: Problem, row_start=None, row_cols=None):
+    """Each column's partners: the columns y sharing a row with f such that f ^ y is again a column
+    with the XOR of their labels (cdist/search.py:207-231; a minimum logical never holds both f and
+    y).  Returns (ex_start int32 [n + 1], ex_cols int32), and the number of pairs."""
+    if row_start is None:
+        _, _, row_start, row_cols, _, _, _ = _search_arrays(p)
+    index = {(int(a), int(b)): j for j, (a, b) in enumerate(zip(p.h, p.l))}
+    part = [set() for _ in range(p.ncols)]
+    seen = set()
+    for r in range(p.nrows):
+        cols = row_cols[row_start[r]:row_start[r + 1]].tolist()
+        for i, x in enumerate(cols):
+            for y in cols[i + 1:]:
+                if (x, y) in seen:
+                    continue
+                seen.add((x, y))
+                z = index.get((int(p.h[x]) ^ int(p.h[y]), int(p.l[x]) ^ int(p.l[y])))
+                if z is not None:
+                    part[x].update((y, z))
+                    part[y].update((x, z))
+                    part[z].update((x, y))
+    ex_start = np.zeros(p.ncols + 1, dtype=np.int32)
+    ex_start[1:] = np.cumsum([len(x) for x in part])
+    ex_cols = np.array([y for x in part for y in sorted(x)] or [0], dtype=np.int32)
+    return ex_start, ex_cols, int(ex_start[-1]) // 2
+
+
 def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=None, enum_all=False, time_limit=0.0,
              log=None, start=1, exclusions=True, on_run=None, table_load=0.5, kernel=None, cover=False,
              labelfree=None, wave=1 << 16, probe=None, seed=12345, threads=1):
@@ -151,8 +178,9 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
     table_seconds, runs (per K: status, best, nodes, lookups, hits, false_hits, seconds),
     lower_bound, distance (None if none <= kmax), solutions, solutions_complete.
 
-    exclusions, cover and kernel are prunings of the reference's search: accepted, not applied (the
-    result does not depend on them).  enum_all, relaxed tables and label-free search (more than 64
+    exclusions: forbid each taken column's partners below it (as the reference); cover and kernel
+    (the reference's other prunings) are accepted and not applied (the result does not depend on
+    them).  enum_all, relaxed tables and label-free search (more than 64
     observables) are not provided.  probe: a callable (zh, zl, lg, R) -> costs answering the probes
     instead of the device table (the tests plug in the oracle's table).  threads: host threads that
     share out the anchors of each threshold (the probes still go out one wave at a time)."""
@@ -164,11 +192,15 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
         raise NotImplementedError("label-free search (more than 64 observables) is not provided")
     W, col, row_start, row_cols, col_start, col_rows, wmax = _search_arrays(p)
     n = p.ncols
+    ex_start = ex_cols = None
+    n_excl = 0
+    if exclusions and n:
+        ex_start, ex_cols, n_excl = partners(p, row_start, row_cols)
     rank_a = np.ascontiguousarray(np.asarray(rank if rank is not None else range(n), dtype=np.int32))
     anch = np.ascontiguousarray(np.asarray(anchors if anchors is not None else range(n), dtype=np.int32))
     lg = np.ascontiguousarray(np.array([int(x) for x in p.l], dtype=np.uint64)) if n else np.zeros(1, np.uint64)
     table = None
-    out = {"k_table": k_table, "table_entries": None, "table_seconds": 0.0, "exclusion_pairs": 0, "runs": [],
+    out = {"k_table": k_table, "table_entries": None, "table_seconds": 0.0, "exclusion_pairs": n_excl, "runs": [],
            "lower_bound": start, "distance": None, "solutions": [], "solutions_complete": False}
     if probe is None:
         table = Table(p, k_table, seed=seed, load=table_load)
@@ -203,8 +235,9 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
             t0 = time.time()
             r = L.tg_search(W, n, p.nrows, wmax, ptr(col), ptr(lg), ptr(zh), ptr(zl), ptr(row_start), ptr(row_cols),
                             ptr(col_start), ptr(col_rows), ptr(rank_a), ptr(anch), len(anch), K, k_table, int(wave),
-                            cb, None, int(threads), float(time_limit), stats.ctypes.data, sol.ctypes.data,
-                            nsol.ctypes.data)
+                            cb, None, ptr(ex_start) if ex_start is not None else None,
+                            ptr(ex_cols) if ex_cols is not None else None, int(threads), float(time_limit),
+                            stats.ctypes.data, sol.ctypes.data, nsol.ctypes.data)
             if r < 0:
                 _lib.check(r)
             status = {1: "found", 0: "exhausted", 2: "timeout"}[r]
