@@ -507,7 +507,36 @@ def section_search(args):
                      "nodes": sum(sum(x["nodes"]) for x in r["runs"]), "lookups": sum(x["lookups"] for x in r["runs"]),
                      "waves": sum(x["waves"] for x in r["runs"]), "false_hits": sum(x["false_hits"] for x in r["runs"]),
                      "table_entries": r["table_entries"]}
+        if not args.no_cpu_baseline:
+            out[name]["cpu_baseline"] = _search_cpu(p, c["distance"])
     return out
+
+
+def _search_cpu(p, kmax):
+    """The same search with its probes answered by oracle/table_port.c (the reference's completion
+    table in C) on one host core: table build and search time."""
+    import ctypes
+    import math
+    from tropidist_gb300 import search
+    from tropidist_gb300._sigs_extra import PROBE_FN
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "table_port.so"))
+    lib.tp_create.restype = ctypes.c_void_p
+    lib.tp_create.argtypes = [ctypes.c_int]
+    lib.tp_build.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    lib.tp_free.argtypes = [ctypes.c_void_p]
+    t0 = time.perf_counter()
+    zh, zl = search.column_hashes(p.h, search.row_hashes(p.nrows, 12345))
+    import numpy as np
+    lg = np.array(p.l, dtype=np.uint64)
+    total = sum(math.comb(p.ncols, i) for i in range(3))
+    tab = lib.tp_create(max(10, math.ceil(math.log2(total / 0.5 + 1))))
+    lib.tp_build(tab, p.ncols, zh.ctypes.data, zl.ctypes.data, lg.ctypes.data, 2)
+    r = search.distance(p, k_table=2, kmax=kmax, probe_fn=PROBE_FN(("tp_probe", lib)), probe_ctx=tab)
+    dt = time.perf_counter() - t0
+    lib.tp_free(tab)
+    return {"seconds": dt, "distance": r["distance"], "cores": 1, "kind": "port",
+            "sample": "the whole deepening: the same host search, probes answered by a C port of the "
+                      "reference's completion table (cdist/gmitm.c tab_build / tab_lookup)"}
 
 
 SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse, "tree": section_tree,

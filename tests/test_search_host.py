@@ -163,3 +163,41 @@ def test_partner_exclusions_keep_the_distance():
                 for y in ex_cols[ex_start[f]:ex_start[f + 1]].tolist():
                     assert any(p.h[j] == p.h[f] ^ p.h[y] and p.l[j] == p.l[f] ^ p.l[y] for j in range(p.ncols))
     assert pruned > 0
+
+
+def port_table(p, k, seed=12345):
+    """oracle/table_port.c: the reference's completion table in C, and its native probe."""
+    import ctypes
+    import math
+    from tropidist_gb300._sigs_extra import PROBE_FN
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "table_port.so"))
+    lib.tp_create.restype = ctypes.c_void_p
+    lib.tp_create.argtypes = [ctypes.c_int]
+    lib.tp_build.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    lib.tp_free.argtypes = [ctypes.c_void_p]
+    zh, zl = search.column_hashes(p.h, search.row_hashes(p.nrows, seed))
+    lg = np.array(p.l, dtype=np.uint64)
+    total = sum(math.comb(p.ncols, i) for i in range(k + 1))
+    t = lib.tp_create(max(10, math.ceil(math.log2(total / 0.5 + 1))))
+    lib.tp_build(t, p.ncols, zh.ctypes.data, zl.ctypes.data, lg.ctypes.data, k)
+    return lib, t, PROBE_FN(("tp_probe", lib))
+
+
+def test_native_probe_with_the_c_table():
+    rng = random.Random(31)
+    for t in range(40):
+        m, n, nobs = rng.randint(1, 10), rng.randint(1, 13), rng.randint(1, 3)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        p = problem(m, n, nobs, h, l)
+        lib, tab, fn = port_table(p, 2)
+        r = search.distance(p, k_table=2, kmax=n, probe_fn=fn, probe_ctx=tab, wave=1 + t % 7)
+        lib.tp_free(tab)
+        assert r["distance"] == brute(h, l), t
+    c = next(x for x in CODES if x["name"] == "surface_d9_Z")
+    h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+    l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+    p = problem(c["nrows"], len(h), c["nobs"], h, l, "d9")
+    lib, tab, fn = port_table(p, 2)
+    assert search.distance(p, k_table=2, kmax=9, probe_fn=fn, probe_ctx=tab)["distance"] == 9
+    lib.tp_free(tab)

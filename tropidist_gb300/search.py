@@ -170,7 +170,7 @@ def partners(p: Problem, row_start=None, row_cols=None):
 
 def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=None, enum_all=False, time_limit=0.0,
              log=None, start=1, exclusions=True, on_run=None, table_load=0.5, kernel=None, cover=False,
-             labelfree=None, wave=1 << 16, probe=None, seed=12345, threads=1):
+             labelfree=None, wave=1 << 16, probe=None, seed=12345, threads=1, probe_fn=None, probe_ctx=None):
     """Exact distance by iterative deepening over the threshold K (cdist/search.py:387-441): per K a
     depth-first search over column sets, the completion table of all subsets of at most k_table
     columns answering the last levels (tg_search; the probes of many nodes go to the device table in
@@ -183,7 +183,9 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
     them).  enum_all, relaxed tables and label-free search (more than 64
     observables) are not provided.  probe: a callable (zh, zl, lg, R) -> costs answering the probes
     instead of the device table (the tests plug in the oracle's table).  threads: host threads that
-    share out the anchors of each threshold (the probes still go out one wave at a time)."""
+    share out the anchors of each threshold (the probes still go out one wave at a time).
+    probe_fn / probe_ctx: a native tg_probe_fn (a _sigs_extra.PROBE_FN) and its context answering the
+    probes instead (a host table: the timed CPU baseline)."""
     import ctypes
     from ._sigs_extra import PROBE_FN
     if enum_all or relaxed:
@@ -202,7 +204,10 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
     table = None
     out = {"k_table": k_table, "table_entries": None, "table_seconds": 0.0, "exclusion_pairs": n_excl, "runs": [],
            "lower_bound": start, "distance": None, "solutions": [], "solutions_complete": False}
-    if probe is None:
+    if probe_fn is not None:
+        zh, zl = column_hashes(p.h, row_hashes(p.nrows, seed))
+        look = None
+    elif probe is None:
         table = Table(p, k_table, seed=seed, load=table_load)
         zh, zl = table.zh, table.zl
         look = table.lookup
@@ -223,7 +228,8 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
         except Exception:                 # reported to the search, which stops with an error
             return 1
 
-    cb = PROBE_FN(answer)
+    cb = probe_fn if probe_fn is not None else PROBE_FN(answer)
+    ctx = probe_ctx if probe_fn is not None else None
     L = _lib.lib()
     stats = np.zeros(8, dtype=np.int64)
     sol = np.zeros(64, dtype=np.int32)
@@ -235,7 +241,7 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
             t0 = time.time()
             r = L.tg_search(W, n, p.nrows, wmax, ptr(col), ptr(lg), ptr(zh), ptr(zl), ptr(row_start), ptr(row_cols),
                             ptr(col_start), ptr(col_rows), ptr(rank_a), ptr(anch), len(anch), K, k_table, int(wave),
-                            cb, None, ptr(ex_start) if ex_start is not None else None,
+                            cb, ctx, ptr(ex_start) if ex_start is not None else None,
                             ptr(ex_cols) if ex_cols is not None else None, int(threads), float(time_limit),
                             stats.ctypes.data, sol.ctypes.data, nsol.ctypes.data)
             if r < 0:
