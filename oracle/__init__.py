@@ -11,8 +11,13 @@ the tropidist_gb300 package imports this directory; the product path runs on the
   sparse.py       numpy sparse tables (cdist/sparse_dp.py:300-455) and the lookahead bound
                   (cdist/sparse_dp.py:148-217)
   table.py        completion tables (cdist/gmitm.c:61-186, cdist/search.py:83-142)
-  Makefile        builds dense_port.so, and oracle/_ref/ from the reference C sources when the
-                  reference tree is present
+  table_port.c    the completion table in C with a native probe for the search: the timed CPU
+                  baseline of the weight-bounded search
+  tree.py         tree DP join over all pairs and the post-order executor (cdist/tree_dp.c:13-39,
+                  cdist/tree_dp.py:442-501), brute force; run_port drives tree_port.c
+  tree_port.c     the reference's Gray-code tree join in C: the timed CPU baseline of the tree DP
+  Makefile        builds dense_port.so, tree_port.so, table_port.so, and oracle/_ref/ from the
+                  reference C sources when the reference tree is present
 
 Parity is pinned against golden vectors produced by the reference itself (tests/golden/).
 """
