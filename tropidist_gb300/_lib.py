@@ -67,7 +67,7 @@ def build(force=False, verbose=False):
         with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             list(ex.map(run, jobs))
     if force or jobs or _stale(SO, objs):
-        run([_nvcc()] + ARCH + ["-shared", "-o", SO] + objs + ["-lcudart"])
+        run([_nvcc()] + ARCH + ["-shared", "-o", SO] + objs + ["-lcudart", "-lpthread"])
     return SO
 
 
