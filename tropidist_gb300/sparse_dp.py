@@ -1111,10 +1111,16 @@ def plan_trellises(p, order=None):
     data (no GPU; picklable, so it can run in a worker process)."""
     order = default_order(p) if order is None else order
     trs = [Trellis.for_query(p, i, order) for i in range(p.nobs)]
-    for t in trs:
-        if t.feasible:
-            t.bound_raw(True)
-            t.bound_raw(False)
+    # the lookahead data of both directions of every trellis: the library's routine releases the
+    # interpreter, so the directions run side by side
+    jobs = [(t, fwd) for t in trs if t.feasible for fwd in (True, False)]
+    if len(jobs) > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(min(len(jobs), 8)) as ex:
+            list(ex.map(lambda j: j[0].bound_raw(j[1]), jobs))
+    else:
+        for t, fwd in jobs:
+            t.bound_raw(fwd)
     return trs
 
 
