@@ -190,15 +190,16 @@ void tg_server_free(void *server);
  * answers a wave of m probes (least cost <= R[i] with hash (zh, zl)[i] and a label other than lg[i],
  * or -1) and returns 0.  stats: nodes, lookups, hits, false hits, waves; sol / *nsol: the logical
  * found; ex_start / ex_cols (or NULL): each column's partners (f ^ y a column with their label),
- * forbidden below f; threads share out the anchors (the probe is entered by one at a time).  Returns 1 found, 0
+ * forbidden below f; cover: the covering bound (0 off, 1 first dual, 2 with the ascent; stats[5] the
+ * nodes it pruned); threads share out the anchors (the probe is entered by one at a time).  Returns 1 found, 0
  * exhausted, 2 time limit (seconds > 0), or a negative status. */
 typedef int (*tg_probe_fn)(int64_t m, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, const int32_t *R,
                            int32_t *out, void *ctx);
 int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint64_t *lg, const uint64_t *zh,
               const uint64_t *zl, const int32_t *row_start, const int32_t *row_cols, const int32_t *col_start,
               const int32_t *col_rows, const int32_t *rank, const int32_t *anchors, int nanchors, int K, int kt,
-              int64_t wave, tg_probe_fn probe, void *ctx, const int32_t *ex_start, const int32_t *ex_cols, int threads,
-              double seconds, int64_t *stats, int32_t *sol, int32_t *nsol);
+              int64_t wave, tg_probe_fn probe, void *ctx, const int32_t *ex_start, const int32_t *ex_cols, int cover,
+              int threads, double seconds, int64_t *stats, int32_t *sol, int32_t *nsol);
 
 /* ---------------------------------------------------------------- tree DP (exact min-plus on a binary tree)
  * Per-call entry points with the reference's ctypes signatures (cdist/tree_dp.py:214-222), on DEVICE

@@ -201,3 +201,31 @@ def test_native_probe_with_the_c_table():
     lib, tab, fn = port_table(p, 2)
     assert search.distance(p, k_table=2, kmax=9, probe_fn=fn, probe_ctx=tab)["distance"] == 9
     lib.tp_free(tab)
+
+
+@pytest.mark.parametrize("cover", [True, "simple"])
+def test_covering_bound_keeps_the_distance(cover):
+    rng = random.Random(41)
+    pruned = 0
+    for t in range(80):
+        m, n, nobs = rng.randint(1, 10), rng.randint(1, 13), rng.randint(1, 3)
+        h = [rng.randrange(1 << m) for _ in range(n)]
+        l = [rng.randrange(1 << nobs) for _ in range(n)]
+        p = problem(m, n, nobs, h, l)
+        lib, tab, fn = port_table(p, t % 3)
+        r = search.distance(p, k_table=t % 3, kmax=n, probe_fn=fn, probe_ctx=tab, cover=cover)
+        lib.tp_free(tab)
+        assert r["distance"] == brute(h, l), t
+        pruned += sum(x["cover_pruned"] for x in r["runs"])
+    assert pruned > 0
+    for name, d in (("bb72_Z", 6), ("surface_d9_Z", 9)):
+        c = next(x for x in CODES if x["name"] == name)
+        h = [int(x, 16) if isinstance(x, str) else int(x) for x in c["h"]]
+        l = [int(x, 16) if isinstance(x, str) else int(x) for x in c["l"]]
+        p = problem(c["nrows"], len(h), c["nobs"], h, l, name)
+        lib, tab, fn = port_table(p, 2)
+        a = search.distance(p, k_table=2, kmax=d, probe_fn=fn, probe_ctx=tab, cover=cover)
+        b = search.distance(p, k_table=2, kmax=d, probe_fn=fn, probe_ctx=tab)
+        lib.tp_free(tab)
+        assert a["distance"] == b["distance"] == d
+        assert sum(x["nodes"][0] for x in a["runs"]) <= sum(x["nodes"][0] for x in b["runs"])

@@ -37,7 +37,7 @@ SIGNATURES = {
     "tg_server_stop": (ci, [vp]),
     "tg_server_free": (None, [vp]),
     "tg_search": (ci, [ci, ci, ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, ci, ci, ci, i64, PROBE_FN, vp,
-                       vp, vp, ci, c.c_double, vp, vp, vp]),
+                       vp, vp, ci, ci, c.c_double, vp, vp, vp]),
     "tree_join_u8": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),
     "tree_join_u16": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),
     "tree_join_u32": (ci, [vp, vp, vp, vp, vp, c.c_uint, c.c_uint, u64, u64, u64]),

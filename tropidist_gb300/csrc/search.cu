@@ -66,6 +66,68 @@ struct Search {
         forb[f] = 0;
         for (int q = col_start[f]; q < col_start[f + 1]; q++) avail[col_rows[q]]++;
     }
+    // covering bound (cdist/gmitm.c:496-596): each unsatisfied row needs a free column; the weights
+    // y_r = 1 / (most unsatisfied rows one free column of r clears) are a feasible dual of the covering
+    // LP, raised greedily (rows with the fewest free columns first) while every column's load stays
+    // <= 1; their sum bounds the columns still needed from below.  Returns true to prune.
+    int cover = 0;                                    // 0 off, 1 the first dual only, 2 with the ascent
+    std::vector<double> load;
+    std::vector<int> cv_rows;
+    std::vector<double> cv_y;
+    int64_t cover_pruned = 0;
+    bool cover_prune(const uint64_t *s, int R, int pc) {
+        const double lim = R + 1e-9, inv_wmax = 1.0 / wmax;
+        int left = pc;
+        if (left * inv_wmax > lim) return true;
+        double sum = 0.0;
+        cv_rows.clear();
+        cv_y.clear();
+        for (int w = 0; w < W; w++) {
+            uint64_t x = s[w];
+            while (x) {
+                const int r = w * 64 + __builtin_ctzll(x);
+                x &= x - 1;
+                left--;
+                int m = 0;
+                for (int q = row_start[r]; q < row_start[r + 1]; q++) {
+                    const int f = row_cols[q];
+                    if (forb[(size_t)f]) continue;
+                    int o = 0;
+                    for (int v = 0; v < W; v++) o += __builtin_popcountll(s[v] & col[(size_t)f * W + v]);
+                    m = std::max(m, o);
+                }
+                if (m == 0) return true;              // no free column reaches this row
+                sum += 1.0 / m;
+                if (sum + left * inv_wmax > lim) return true;
+                cv_rows.push_back(r);
+                cv_y.push_back(1.0 / m);
+            }
+        }
+        if (cover < 2) return false;
+        if (load.size() != (size_t)n) load.assign((size_t)n, 0.0);
+        for (size_t i = 0; i < cv_rows.size(); i++)
+            for (int q = row_start[cv_rows[i]]; q < row_start[cv_rows[i] + 1]; q++) load[(size_t)row_cols[q]] = 0.0;
+        for (size_t i = 0; i < cv_rows.size(); i++)
+            for (int q = row_start[cv_rows[i]]; q < row_start[cv_rows[i] + 1]; q++)
+                if (!forb[(size_t)row_cols[q]]) load[(size_t)row_cols[q]] += cv_y[i];
+        std::vector<int> ord(cv_rows.size());
+        for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return avail[(size_t)cv_rows[(size_t)a]] <
+                                                                           avail[(size_t)cv_rows[(size_t)b]]; });
+        for (int i : ord) {
+            const int r = cv_rows[(size_t)i];
+            double slack = 1.0;
+            for (int q = row_start[r]; q < row_start[r + 1]; q++)
+                if (!forb[(size_t)row_cols[q]]) slack = std::min(slack, 1.0 - load[(size_t)row_cols[q]]);
+            if (slack <= 1e-12) continue;
+            for (int q = row_start[r]; q < row_start[r + 1]; q++)
+                if (!forb[(size_t)row_cols[q]]) load[(size_t)row_cols[q]] += slack;
+            sum += slack;
+            if (sum > lim) return true;
+        }
+        return false;
+    }
+
     // a minimum logical holding f holds none of f's partners: forbid them below f (undone by the caller)
     static constexpr uint8_t PARTNER = 253;
     void exclude(int f, std::vector<int> &undo) {
@@ -186,6 +248,10 @@ struct Search {
             add_probe(hz[d], lz[d], g[d], R, node_here(d), -1);
             return;
         }
+        if (cover && pc > R && cover_prune(s, R, pc)) {
+            cover_pruned++;
+            return;
+        }
         int piv = -1, best = 1 << 30;
         for (int w = 0; w < W; w++) {
             uint64_t x = s[w];
@@ -256,13 +322,14 @@ extern "C" {
 // stats: nodes, lookups, hits, false hits, waves.  sol: the logical's columns (sorted), *nsol its
 // size; ex_start / ex_cols (or NULL): each column's partners (columns y with f ^ y equal to a column of
 // the same label: a minimum logical never holds both; cdist/search.py:207-231), forbidden below f;
+// cover: the covering bound (0 off, 1 its first dual, 2 with the ascent); stats[5]: nodes it pruned;
 // threads: threads sharing out the anchors (the probe is entered by one at a time).  Returns 1
 // found, 0 exhausted, 2 time limit, or a negative status (-6: the probe call failed).
 int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint64_t *lg, const uint64_t *zh,
               const uint64_t *zl, const int32_t *row_start, const int32_t *row_cols, const int32_t *col_start,
               const int32_t *col_rows, const int32_t *rank, const int32_t *anchors, int nanchors, int K, int kt,
-              int64_t wave, tg_probe_fn probe, void *ctx, const int32_t *ex_start, const int32_t *ex_cols, int threads,
-              double seconds, int64_t *stats, int32_t *sol, int32_t *nsol) {
+              int64_t wave, tg_probe_fn probe, void *ctx, const int32_t *ex_start, const int32_t *ex_cols, int cover,
+              int threads, double seconds, int64_t *stats, int32_t *sol, int32_t *nsol) {
     if (W < 1 || n < 0 || nrows < 0 || K < 1 || K > 64 || kt < 0 || !col || !lg || !zh || !zl || !row_start ||
         !col_start || !rank || (nanchors && !anchors) || !probe || !stats || !sol || !nsol || wave < 1)
         return set_error(TG_ERR_ARG, "bad search arguments");
@@ -289,6 +356,7 @@ int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint
         X.mu = &mu;
         X.ex_start = ex_start;
         X.ex_cols = ex_cols;
+        X.cover = std::max(0, std::min(cover, 2));
     }
     // anchors are handed out one at a time; each thread searches below its anchors with its own
     // forbidden set and wave
@@ -317,16 +385,17 @@ int tg_search(int W, int n, int nrows, int wmax, const uint64_t *col, const uint
         for (int t = 0; t < T; t++) pool.emplace_back(work, std::ref(Xs[(size_t)t]));
         for (auto &th : pool) th.join();
     }
-    int64_t tot[5] = {0, 0, 0, 0, 0};
+    int64_t tot[6] = {0, 0, 0, 0, 0, 0};
     bool any_timeout = false, any_failed = false;
     const Search *hit = nullptr;
     for (const Search &X : Xs) {
         tot[0] += X.nodes; tot[1] += X.lookups; tot[2] += X.hits; tot[3] += X.false_hits; tot[4] += X.waves;
+        tot[5] += X.cover_pruned;
         any_timeout |= X.timeout;
         any_failed |= X.failed;
         if (X.found && !hit) hit = &X;
     }
-    for (int i = 0; i < 5; i++) stats[i] = tot[i];
+    for (int i = 0; i < 6; i++) stats[i] = tot[i];
     *nsol = 0;
     if (hit) {
         for (size_t i = 0; i < hit->sol.size() && i < 64; i++) sol[i] = hit->sol[i];

@@ -178,9 +178,10 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
     table_seconds, runs (per K: status, best, nodes, lookups, hits, false_hits, seconds),
     lower_bound, distance (None if none <= kmax), solutions, solutions_complete.
 
-    exclusions: forbid each taken column's partners below it (as the reference); cover and kernel
-    (the reference's other prunings) are accepted and not applied (the result does not depend on
-    them).  enum_all, relaxed tables and label-free search (more than 64
+    exclusions: forbid each taken column's partners below it (as the reference); cover: the covering
+    bound (True / "ascent", or "simple" without the ascent; off by default, as the reference's);
+    kernel (the reference's kernel dominance) is accepted and not applied (the result does not
+    depend on it).  enum_all, relaxed tables and label-free search (more than 64
     observables) are not provided.  probe: a callable (zh, zl, lg, R) -> costs answering the probes
     instead of the device table (the tests plug in the oracle's table).  threads: host threads that
     share out the anchors of each threshold (the probes still go out one wave at a time).
@@ -194,6 +195,8 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
         raise NotImplementedError("label-free search (more than 64 observables) is not provided")
     W, col, row_start, row_cols, col_start, col_rows, wmax = _search_arrays(p)
     n = p.ncols
+    # cover: False, True / "ascent" (the covering bound with its dual ascent), "simple" (first dual)
+    cover_mode = 0 if not cover else (1 if cover == "simple" else 2)
     ex_start = ex_cols = None
     n_excl = 0
     if exclusions and n:
@@ -242,7 +245,7 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
             r = L.tg_search(W, n, p.nrows, wmax, ptr(col), ptr(lg), ptr(zh), ptr(zl), ptr(row_start), ptr(row_cols),
                             ptr(col_start), ptr(col_rows), ptr(rank_a), ptr(anch), len(anch), K, k_table, int(wave),
                             cb, ctx, ptr(ex_start) if ex_start is not None else None,
-                            ptr(ex_cols) if ex_cols is not None else None, int(threads), float(time_limit),
+                            ptr(ex_cols) if ex_cols is not None else None, cover_mode, int(threads), float(time_limit),
                             stats.ctypes.data, sol.ctypes.data, nsol.ctypes.data)
             if r < 0:
                 _lib.check(r)
@@ -251,7 +254,7 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
             best = len(s) if r == 1 else None
             rec = {"K": K, "status": status, "best": best, "nodes": [int(stats[0])], "lookups": int(stats[1]),
                    "hits": int(stats[2]), "false_hits": int(stats[3]), "waves": int(stats[4]),
-                   "seconds": time.time() - t0, "tasks": 0, "cover_pruned": 0,
+                   "seconds": time.time() - t0, "tasks": 0, "cover_pruned": int(stats[5]),
                    "nsol_recorded": 1 if r == 1 else 0, "nsol_found": 1 if r == 1 else 0,
                    "solutions_complete": False}
             out["runs"].append(rec)
