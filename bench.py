@@ -10,13 +10,16 @@ needed between steps.
 `value` is state-updates/s (Plan.work(), cdist/trellis.py:133-144) with the op stream already
 scheduled and the tables resident in HBM; `e2e` is the same metric through the public API
 (tropidist_gb300.auto.dp_distance: host planning, scheduling, launches and the result read back).
-`roofline` reports the fused tile pass (the dominant kernel): table bytes read + written per
-launch over its average CUDA-event launch time, against the measured HBM copy bandwidth.
-`cpu_baseline` times the C/OpenMP port of the reference's kernels (oracle/dense_port.c) on the
-host cores over a window of the same plan at full width.
+`roofline` reports the dominant kernel: table bytes read + written per launch over its average
+CUDA-event launch time, against the measured HBM copy bandwidth.  The four distances are compared
+with the ones the reference itself computed on this workload (tests/golden/headline.json); a
+mismatch fails the run.  `cpu_baseline` times the C/OpenMP port of the reference's kernels
+(oracle/dense_port.c) on observable 0's whole sweep with every host core, and on a window of it
+with one core.
 
---impl reference runs that CPU implementation alone (all host threads) on the same workload,
-each step a bounded window of ops of the first observable's plan.
+--impl reference runs that CPU implementation alone (every host core) on the same four plans,
+planned by the oracle's restatement of the reference's planner, each timed step one observable's
+whole sweep; it loads no library of the package.
 Multi-GPU (torchrun): replicas only; rank r sweeps its own instance (seed + r), no collective on
 the data path; the time is the maximum over ranks.
 """
@@ -47,7 +50,6 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--window", type=int, default=37)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sparse-query", type=int, default=0,
@@ -59,24 +61,53 @@ def parse():
     return ap.parse_args()
 
 
-def workload(args, rank=0):
-    from tropidist_gb300 import synth, trellis
+def problem(args, rank=0):
+    """The seeded banded problem of the headline (pure Python: no library is loaded)."""
+    from tropidist_gb300 import synth
     p = synth.dense_scale(args.seed + rank, window=args.window)
-    order = list(range(p.ncols))
+    return p, list(range(p.ncols))
+
+
+def workload(args, rank=0):
+    """The problem and its four plans from the package's planner (the GPU arm)."""
+    from tropidist_gb300 import trellis
+    p, order = problem(args, rank)
     plans = [trellis.build_plan(p.h, p.l, 1 << o, order, p.nrows) for o in range(p.nobs)]
     return p, order, plans
 
 
-def config(args, plans, extra=None):
-    c = {"workload": "dense Rank DP, banded m=1000 n=2000 col-weight 3 window %d, 4 logical rows one at a time"
-                     % args.window,
-         "m": 1000, "n": 2000, "window": args.window, "seed": args.seed, "observables": len(plans),
-         "peak_bits": max(pl.peak_bits for pl in plans), "table_bytes": 1 << max(pl.peak_bits for pl in plans),
-         "work_per_step": int(sum(pl.work() for pl in plans)), "entry": "uint8",
-         "l2": "inputs larger than L2 (2 GB tables), no flush"}
-    if extra:
-        c.update(extra)
-    return c
+def oracle_plans(p, order):
+    """The same plans from the oracle's restatement of the reference's planner (the CPU arm)."""
+    from oracle import plan as oplan
+    return [oplan.plan(p.h, p.l, 1 << o, order, p.nrows) for o in range(p.nobs)]
+
+
+def dist_string(dists):
+    return ",".join("none" if d is None else "overflow" if d == "overflow" else str(int(d)) for d in dists)
+
+
+def config(args, plans, dists):
+    """The workload, identical in both arms (both sweep the same plans to the same distances)."""
+    feas = [pl for pl in plans if pl.feasible]
+    peak = max(pl.peak_bits for pl in feas)
+    return {"workload": "dense Rank DP, banded m=1000 n=2000 col-weight 3 window %d seed %d, natural order, "
+                        "4 logical rows one at a time" % (args.window, args.seed),
+            "m": 1000, "n": 2000, "window": args.window, "seed": args.seed, "observables": len(plans),
+            "peak_bits": peak, "table_bytes": 1 << peak, "work_per_step": int(sum(pl.work() for pl in feas)),
+            "entry": "uint8", "l2": "inputs larger than L2 (2 GB tables), no flush",
+            "distances": dist_string(dists)}
+
+
+def golden_headline(args):
+    """Per observable the distance the reference itself computed on this workload (its planner and
+    C kernels, tests/golden/headline.json), or None for another seed / window."""
+    if args.seed != 0 or args.window != 37:
+        return None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "headline.json")) as f:
+            return [c["value"] for c in json.load(f)["cases"]]
+    except (OSError, ValueError, KeyError):
+        return None
 
 
 # ---------------------------------------------------------------------- CPU implementation (port)
@@ -89,30 +120,43 @@ def port_lib():
     L.port_run_plan.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_uint64]
     L.port_run_plan.restype = C.c_uint64
     L.port_num_threads.restype = C.c_int
+    L.port_set_threads.argtypes = [C.c_int]
     return L
 
 
-def cpu_window(plan, seconds, threads=None):
-    """Time the C port on a window of the plan's ops starting where the table first reaches
-    peak_bits - 1 (the prefix that gets there runs untimed).  Returns (rate, work, secs, desc)."""
-    import numpy as np
-    from tropidist_gb300 import trellis
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
-    L = port_lib()
-    enc = trellis.encode_ops(plan.ops)
-    w, start = 0, None
+def _full_width_start(plan):
+    """The first op after which the table is 2^(peak_bits - 1) entries wide."""
+    w = 0
     for i, op in enumerate(plan.ops):
         w += 1 if op[0] == "expand" else -1 if op[0] == "select" else 0
         if w >= plan.peak_bits - 1:
-            start = i + 1
-            break
-    buf = np.zeros(1 << plan.peak_bits, dtype=np.uint8)
+            return i + 1
+    return len(plan.ops)
+
+
+def port_sweep(L, plan, buf):
+    """One whole sweep of the plan by the C port: (distance or None / "overflow", seconds)."""
+    enc = plan.encoded()
+    buf[0] = 0
+    t0 = time.perf_counter()
+    n = L.port_run_plan(enc.ctypes.data, len(enc), buf.ctypes.data, 1)
+    dt = time.perf_counter() - t0
+    assert n == 1
+    v = int(buf[0])
+    return ("overflow" if v == 255 else v), dt
+
+
+def port_window(L, plan, buf, seconds):
+    """The C port on the ops after the table first reaches full width, for about `seconds`:
+    (state-updates/s, state-updates, seconds, first op, last op)."""
+    enc = plan.encoded()
+    start = _full_width_start(plan)
+    buf[0] = 0
     n = L.port_run_plan(enc.ctypes.data, start, buf.ctypes.data, 1)
-    i, work, t0 = start, 0, time.perf_counter()
     bits = int(n).bit_length() - 1
+    i, work, t0 = start, 0, time.perf_counter()
     while i < len(enc) and time.perf_counter() - t0 < seconds:
-        j = min(len(enc), i + 8)
+        j = min(len(enc), i + 4)
         for op in plan.ops[i:j]:
             if op[0] == "expand":
                 bits += 1
@@ -123,30 +167,72 @@ def cpu_window(plan, seconds, threads=None):
         n = L.port_run_plan(enc[i:j].ctypes.data, j - i, buf.ctypes.data, n)
         i = j
     secs = time.perf_counter() - t0
-    desc = "ops %d..%d of observable 0's plan (%.3g state-updates, table 2^%d..2^%d), C/OpenMP port" % (
-        start, i, work, plan.peak_bits - 1, plan.peak_bits)
-    return work / secs, work, secs, desc, L.port_num_threads()
+    return work / secs, work, secs, start, i
+
+
+def cpu_legs(p, order, seconds_one=8.0):
+    """The GPU arm's CPU baseline: observable 0's whole sweep by the C port on every host core, and
+    a window of the same plan at full width on one core."""
+    import numpy as np
+    plans = oracle_plans(p, order)
+    plan = plans[0]
+    L = port_lib()
+    buf = np.zeros(1 << plan.peak_bits, dtype=np.uint8)
+    buf.fill(0)
+    L.port_set_threads(os.cpu_count() or 1)
+    cores = L.port_num_threads()
+    v, dt = port_sweep(L, plan, buf)
+    out = {"value": plan.work() / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": "observable 0's whole sweep (%.3g state-updates, 2^%d-entry peak), oracle planner + C/OpenMP "
+                     "port of cdist/viterbi.c" % (plan.work(), plan.peak_bits), "seconds": dt, "distance": v}
+    L.port_set_threads(1)
+    rate, work, secs, a, b = port_window(L, plan, buf, seconds_one)
+    out["one_thread"] = {"value": rate, "cores": 1, "seconds": secs,
+                         "sample": "ops %d..%d of observable 0's plan at full width (%.3g state-updates)" % (a, b, work)}
+    L.port_set_threads(os.cpu_count() or 1)
+    return out
 
 
 def run_reference(args):
-    p, order, plans = workload(args)
-    plan = plans[0]
-    cores = None
-    rates = []
-    per_step = max(1.0, min(6.0, args.cpu_seconds / 3))
-    for k in range(args.warmup + args.steps):
-        rate, work, secs, desc, cores = cpu_window(plan, per_step)
-        if k >= args.warmup:
-            rates.append((work, secs))
-    work = sum(w for w, _ in rates)
-    secs = sum(s for _, s in rates)
+    """The CPU arm: the reference's dense algorithm (the C/OpenMP port of cdist/viterbi.c driven in
+    the executor order of cdist/kernel.py:94-138) on every host core, on the plans of the oracle's
+    restatement of cdist/trellis.py.  No library of the package is loaded.  Each timed step is one
+    observable's whole sweep (observables in turn, so the distances of all four are computed); the
+    warm-up steps run the first plan up to full width (thread pool and page faults)."""
+    import numpy as np
+    p, order = problem(args)
+    plans = oracle_plans(p, order)
+    feas = [(o, pl) for o, pl in enumerate(plans) if pl.feasible]
+    L = port_lib()
+    L.port_set_threads(os.cpu_count() or 1)
+    cores = L.port_num_threads()
+    peak = max(pl.peak_bits for _, pl in feas)
+    buf = np.zeros(1 << peak, dtype=np.uint8)
+    buf.fill(0)                                # the pages are touched before any timing
+    for _ in range(args.warmup):
+        enc = feas[0][1].encoded()
+        buf[0] = 0
+        L.port_run_plan(enc.ctypes.data, _full_width_start(feas[0][1]), buf.ctypes.data, 1)
+    dists = [None] * len(plans)
+    work = secs = 0.0
+    for k in range(args.steps):
+        o, pl = feas[k % len(feas)]
+        dists[o], dt = port_sweep(L, pl, buf)
+        work += pl.work()
+        secs += dt
+    for o, pl in feas[args.steps:]:            # fewer steps than observables: the rest untimed
+        dists[o], _ = port_sweep(L, pl, buf)
     value = work / secs
+    gold = golden_headline(args)
+    sample = "each step one observable's whole sweep (observables in turn), all host cores"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded banded problem)",
-            "impl": "reference",
-            "config": config(args, plans, {"sample": desc}),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "impl": "reference", "config": config(args, plans, dists),
+            "step": "one observable's whole sweep (the GPU arm's step sweeps all four)",
+            "parity": {"reference_fixture": dist_string(gold) if gold else None,
+                       "equal": (dists == gold) if gold else None},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -615,10 +701,16 @@ def main():
     value = total_work * args.steps / (ms / 1e3)
     launches = sum(cp.nsegs for cp in cps) * args.steps
     # distances of the four observables (checked for consistency with the e2e path below)
-    dists = []
-    for cp in cps:
+    dists, it = [], iter(cps)
+    for pl in plans:
+        if not pl.feasible:
+            dists.append(None)
+            continue
+        cp = next(it)
         cp.execute(a, b)
-        dists.append(cp.result(a, b))
+        v = cp.result(a, b)
+        dists.append("overflow" if v == 255 else v)
+    gold = golden_headline(args)
 
     # end to end through the public API (host problem in, distance out)
     e2e_ms = []
@@ -630,7 +722,7 @@ def main():
         torch.cuda.synchronize()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     if e2e_ms:
-        assert per == dists, (per, dists)
+        assert per == [d if d != "overflow" else None for d in dists], (per, dists)
         e2e_value = work / (statistics.median(e2e_ms) / 1e3) * (world if world > 1 else 1)
     else:
         e2e_value = None
@@ -656,19 +748,25 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded banded problem)",
-            "config": config(args, plans, {"parallelism": "replicas (one instance per rank)" if world > 1 else "1 GPU",
-                                           "distances": dists,
-                                           "fused_passes_per_step": int((acc[3] + acc[9]) / args.steps),
-                                           "streaming_passes_per_step": int(acc[9] / args.steps),
-                                           "segments_per_step": sum(cp.nsegs for cp in cps)}),
+            "config": config(args, plans, dists),
+            "parallelism": "replicas (one instance per rank)" if world > 1 else "1 GPU",
+            "schedule": {"fused_passes_per_step": int((acc[3] + acc[9]) / args.steps),
+                         "streaming_passes_per_step": int(acc[9] / args.steps),
+                         "segments_per_step": sum(cp.nsegs for cp in cps)},
+            "parity": {"reference_fixture": dist_string(gold) if gold else None,
+                       "equal": (dists == gold) if gold else None},
             "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": 4 * len(cps), "ms_per_step": statistics.median(e2e_ms) if e2e_ms else None,
                     "path": "tropidist_gb300.auto.dp_distance(problem, order)"}}
+    if gold is not None and dists != gold:
+        # the timed sweeps disagree with the reference's own distances: report and fail
+        print(json.dumps(line), flush=True)
+        raise SystemExit("distances %s differ from the reference's %s" % (dists, gold))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, cwork, secs, desc, cores = cpu_window(plans[0], args.cpu_seconds)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc,
-                                "seconds": secs}
+        line["cpu_baseline"] = cpu_legs(p, order)
+        if gold is not None and line["cpu_baseline"]["distance"] != gold[0]:
+            raise SystemExit("the CPU port's distance differs from the reference's")
     del a, b, cps
     torch.cuda.empty_cache()
     sections = [x for x in args.sections.split(",") if x] if rank == 0 and world == 1 else []

@@ -167,6 +167,15 @@ int port_num_threads(void) {
 #endif
 }
 
+/* Threads of the following parallel regions (the 1-thread leg of the CPU baseline). */
+void port_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 /* Runs ops[0..nops) on buf (room for the largest table); returns the final table size.  The
    first entry of buf must be initialised by the caller (0 for a fresh sweep). */
 uint64_t port_run_plan(const int64_t *ops, int64_t nops, uint8_t *buf, uint64_t n) {

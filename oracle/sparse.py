@@ -165,3 +165,137 @@ class NumpyTables:
         i = int(np.argmin(tot))
         fi = int(np.flatnonzero(hit)[i])
         return int(tot[i]), int(ck[fi]), int(cv[fi]), int(q[fi])
+
+
+# ---------------------------------------------------------------------- the C port as a backend
+_PORT = None
+
+
+def port_lib():
+    """oracle/sparse_port.so (built by oracle/Makefile), with its signatures declared."""
+    global _PORT
+    if _PORT is None:
+        import ctypes
+        import os
+        import subprocess
+        here = os.path.dirname(os.path.abspath(__file__))
+        so = os.path.join(here, "sparse_port.so")
+        if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(os.path.join(here, "sparse_port.c")):
+            subprocess.run(["make", "-s", "-C", here], check=True)
+        L = ctypes.CDLL(so)
+        vp, i64, u64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int
+        L.spp_candidates.argtypes = [vp, i64, u64, ci, u64, u64, ci, ci, vp, vp, i64, u64, ci, ci, vp, vp]
+        L.spp_candidates.restype = i64
+        L.spp_merge.argtypes = [vp, i64, vp, i64, u64, u64, ci, ci, ci, vp, vp, i64, u64, ci, ci, vp, vp,
+                                ctypes.POINTER(i64)]
+        L.spp_merge.restype = i64
+        L.spp_join.argtypes = [vp, i64, vp, i64, u64, ctypes.POINTER(u64), ctypes.POINTER(u64)]
+        L.spp_join.restype = ci
+        L.spp_hist.argtypes = [vp, i64, vp]
+        _PORT = L
+    return _PORT
+
+
+class CPortTables:
+    """The reference's C table backend (cdist/sparse_dp.py:506-605 over cdist/sparse_dp.c) restated
+    over oracle/sparse_port.c: a table is one sorted array of packed states key | value << 56.
+    step() returns arrays of two alternating buffers, so the table it returns is valid until the step
+    after next; persistent() copies.  One object per sweep."""
+    name = "c-port"
+    KEYMASK = (1 << 56) - 1
+
+    def __init__(self, tr=None):
+        if tr is not None and tr.nslots > 56:
+            raise ValueError("the C tables hold at most 56 row slots (this trellis needs %d)" % tr.nslots)
+        self.tr = tr
+        self.L = port_lib()
+        self.bufs = {}
+        self.flip = 0
+
+    def _buf(self, name, n):
+        b = self.bufs.get(name)
+        if b is None or b.size < n:
+            grow = int(1.25 * b.size) if b is not None else 0
+            b = self.bufs[name] = np.empty(max(n, grow, 1024), dtype=U64)
+        return b
+
+    @staticmethod
+    def start():
+        return np.zeros(1, dtype=U64)
+
+    @staticmethod
+    def size(tab):
+        return tab.size
+
+    @staticmethod
+    def nbytes(tab):
+        return tab.nbytes
+
+    @staticmethod
+    def persistent(tab):
+        return tab.copy()
+
+    @staticmethod
+    def truncate(tab, below):
+        return tab[(tab >> U64(56)) < U64(below)]
+
+    @classmethod
+    def arrays(cls, tab):
+        return tab & U64(cls.KEYMASK), (tab >> U64(56)).astype(np.uint8)
+
+    @classmethod
+    def from_arrays(cls, keys, vals):
+        o = np.argsort(keys)
+        return (np.asarray(keys, dtype=U64)[o] & U64(cls.KEYMASK)) | (np.asarray(vals).astype(U64)[o] << U64(56))
+
+    @classmethod
+    def lookup(cls, tab, s):
+        keys = tab & U64(cls.KEYMASK)
+        i = int(np.searchsorted(keys, U64(s)))
+        if i < keys.size and int(keys[i]) == s:
+            return int(tab[i] >> U64(56))
+        return INF
+
+    @staticmethod
+    def changed_size(ch):
+        return ch.size
+
+    def hist(self, tab):
+        h = np.zeros(256, dtype=np.int64)
+        self.L.spp_hist(tab.ctypes.data, tab.size, h.ctypes.data)
+        return h
+
+    def step(self, tab, upd, sel_mask, sel_bits, cap, K, tmask, hd, keep_below=None, want_changed=False, w=1):
+        import ctypes
+        n = tab.size
+        if hd is None:
+            ncls, mp, wp, extra, use_h = 0, None, None, 0, 0
+        else:
+            m_arr = np.ascontiguousarray(hd[0], dtype=U64)
+            w_arr = np.ascontiguousarray(hd[1], dtype=np.int64)
+            extra = int(hd[2])
+            ncls, use_h = m_arr.size, 1
+            mp = m_arr.ctypes.data if ncls else None
+            wp = w_arr.ctypes.data if ncls else None
+        cand, tmp = self._buf("cand", n), self._buf("tmp", n)
+        m = self.L.spp_candidates(tab.ctypes.data, n, int(upd), int(w), int(sel_mask), int(sel_bits), int(cap),
+                                  ncls, mp, wp, extra, int(tmask), int(K), use_h, cand.ctypes.data, tmp.ctypes.data)
+        self.flip ^= 1
+        out = self._buf("out%d" % self.flip, n + m)
+        ch = self._buf("changed", m) if want_changed else None
+        nch = ctypes.c_int64(0)
+        no = self.L.spp_merge(tab.ctypes.data, n, cand.ctypes.data, m, int(sel_mask), int(sel_bits), int(cap),
+                              int(keep_below or 0), ncls, mp, wp, extra, int(tmask), int(K), use_h, out.ctypes.data,
+                              ch.ctypes.data if ch is not None else None, ctypes.byref(nch))
+        return out[:no], (ch[:nch.value] if want_changed else None)
+
+    def join(self, ch, btab, tmask):
+        import ctypes
+        if not ch.size or not btab.size:
+            return None
+        fb, bb = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        tot = self.L.spp_join(ch.ctypes.data, ch.size, btab.ctypes.data, btab.size, int(tmask), ctypes.byref(fb),
+                              ctypes.byref(bb))
+        if tot < 0:
+            return None
+        return int(tot), fb.value & self.KEYMASK, fb.value >> 56, bb.value & self.KEYMASK

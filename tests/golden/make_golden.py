@@ -20,6 +20,10 @@ next to this script; the test-suite reads only those files.
                       distances beyond 255, larger joins  (`make_golden.py tree` writes only this)
   search.json         the weight-bounded search (cdist/search.py distance) on random problems
                       (`make_golden.py search` writes only this)
+  headline.json       the benchmark's dense workload (banded m=1000 n=2000 window 37, 31-bit
+                      frontier, four logical rows): op-stream digests, distances and two 2 GB
+                      tables per observable (sha256 + histogram) from the reference's planner and
+                      C kernels (`make_golden.py headline` writes only this; a few minutes)
 """
 from __future__ import annotations
 
@@ -416,11 +420,90 @@ def search_main():
     shutil.rmtree(tmp, ignore_errors=True)
 
 
+def headline_checkpoints(ops, peak_bits):
+    """Op counts at which the headline fixture records the table: the first op after half of the
+    plan and the first after three quarters at which the table is at least 2^(peak_bits - 1)
+    entries wide, each on a boundary of the reference's executor calls (not between an expand and
+    the update of its starting column)."""
+    out, w = [], 0
+    widths = []
+    for op in ops:
+        w += 1 if op[0] == "expand" else -1 if op[0] == "select" else 0
+        widths.append(w)
+    for frac in (2, 4 / 3):
+        k = next(i for i in range(int(len(ops) / frac), len(ops))
+                 if widths[i - 1] >= peak_bits - 1 and ops[i - 1][0] != "expand")
+        out.append(k)
+    return out
+
+
+def headline_main():
+    """headline.json: the benchmark's dense workload (tropidist_gb300.synth.dense_scale(0, window=37):
+    banded m=1000 n=2000, col-weight 3, natural order, 31-bit frontier, four logical rows one at a
+    time) planned by the reference's own cdist/trellis.py and swept by its own C kernels
+    (cdist/viterbi.c through its executor order): per observable the op-stream digest, work,
+    value, and the sha256 and value histogram of the table at two checkpoints near full width."""
+    import ctypes
+    import numpy as np
+    tmp = tempfile.mkdtemp(prefix="tropi_ref_")
+    shutil.copytree(os.path.join(REF, "cdist"), os.path.join(tmp, "cdist"))
+    sys.path[:0] = [tmp, REPO]
+    from cdist import kernel, trellis
+    from tropidist_gb300 import synth
+    p = synth.dense_scale(0, window=37)
+    order = list(range(p.ncols))
+    L = kernel.lib()
+    u8p = ctypes.POINTER(ctypes.c_uint8)
+    cases = []
+    for o in range(p.nobs):
+        plan = trellis.build_plan(p.h, p.l, 1 << o, order, p.nrows)
+        enc = np.array([[0, 0, 0] if op[0] == "expand" else [1, op[1], 1] if op[0] == "update"
+                        else [2, op[1], op[2]] for op in plan.ops], dtype=np.int64)
+        ks = headline_checkpoints(plan.ops, plan.peak_bits)
+        buf = np.zeros(1 << plan.peak_bits, dtype=np.uint8)
+        ptr = buf.ctypes.data_as(u8p)
+        n, i, ops, tabs = 1, 0, plan.ops, {}
+        while i < len(ops):                       # the executor order of cdist/kernel.py:112-135
+            op = ops[i]
+            if op[0] == "expand":
+                nxt = ops[i + 1]
+                if nxt[0] == "update" and (nxt[1] >> n.bit_length() - 1) == 1:
+                    L.dp_expand_update(ptr, n, nxt[1] ^ n)
+                    i += 2
+                else:
+                    L.dp_fill(ctypes.cast(ctypes.addressof(ptr.contents) + n, u8p), n, 255)
+                    i += 1
+                n <<= 1
+            elif op[0] == "update":
+                L.dp_update(ptr, n, op[1])
+                i += 1
+            else:
+                n = L.dp_select(ptr, n, op[1], op[2])
+                i += 1
+            if i in ks:
+                t = buf[:n]
+                tabs[str(i)] = {"sha": hashlib.sha256(memoryview(t)).hexdigest()[:16], "entries": int(n),
+                                "hist": np.bincount(t, minlength=256).tolist()}
+        assert n == 1
+        value = kernel.final_value(buf[0])
+        cases.append({"observable": o, "peak_bits": plan.peak_bits, "work": plan.work(), "nops": len(plan.ops),
+                      "ops_sha": sha(enc), "value": value, "tables": tabs,
+                      "threads": L.dp_num_threads()})
+        print("observable", o, "value", value, "peak", plan.peak_bits, "checkpoints", sorted(tabs), flush=True)
+    with open(os.path.join(HERE, "headline.json"), "w") as f:
+        json.dump({"workload": "synth.dense_scale(0, window=37), natural order, 4 logical rows", "cases": cases},
+                  f, separators=(",", ":"))
+    print("wrote headline.json", os.path.getsize(os.path.join(HERE, "headline.json")), "bytes")
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["tree"]:
         tree_main()
     elif sys.argv[1:] == ["search"]:
         search_main()
+    elif sys.argv[1:] == ["headline"]:
+        headline_main()
     else:
         main()
         tree_main()

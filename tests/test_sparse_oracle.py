@@ -155,3 +155,51 @@ def test_trellis_cut_data_matches_plain_loops():
                 col[low.bit_length() - 1] |= 1 << tr.slot[r]
                 x ^= low
         assert tr.col == col
+
+
+def test_c_port_tables_match_reference():
+    """oracle/sparse_port.c (the timed CPU baseline of the sparse sweep) behind the backend
+    interface: the reference's query values and peak states, and its tables at every cut."""
+    from oracle.sparse import CPortTables
+    checked = 0
+    for case in golden("sparse_random.json"):
+        if not case["feasible"]:
+            continue
+        p = _problem(case)
+        tr = sparse_dp.Trellis.for_query(p, case["obs"], case["order"])
+        for run in case["runs"]:
+            r = sparse_dp.query(tr, run["K"], mode=run["mode"], split=run["split"], use_h=run["use_h"],
+                                backend=CPortTables(tr))
+            assert r["value"] == run["value"], run
+            assert r["peak_states"] == run["peak_states"], run
+            if run["value"] is not None:
+                check_witness(p, r["witness"], run["value"], case["obs"])
+            checked += 1
+    assert checked > 1000
+    for case in golden("sparse_tables.json"):
+        p = Problem("t", case["nrows"], 1, unhex(case["h"]), unhex(case["l"]))
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        sw = sparse_dp.Sweep(tr, +1 if case["forward"] else -1, case["K"], case["K"], use_h=case["use_h"], every=1,
+                             backend=CPortTables(tr))
+        sw.run()
+        assert sw.counts == case["counts"]
+        for c, (n, hk, hv) in case["tables"].items():
+            keys, vals = CPortTables.arrays(sw.ckpt[int(c)])
+            assert keys.size == n and sha(keys) == hk and sha(vals) == hv, c
+
+
+def test_c_port_weighted_columns_match_numpy():
+    """With column weights (no reference caller) the C port's tables equal the numpy restatement's."""
+    import random
+    from oracle.sparse import CPortTables
+    rng = random.Random(5)
+    for t in range(30):
+        p = synth.banded(20, 40, 6, 3, 1, seed=t)
+        p.weights = [rng.randint(1, 3) for _ in range(p.ncols)]
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        if not tr.feasible:
+            continue
+        for K in (4, 7):
+            a = sparse_dp.query(tr, K, backend=NumpyTables(tr), witness=False)
+            b = sparse_dp.query(tr, K, backend=CPortTables(tr), witness=False)
+            assert a["value"] == b["value"] and a["peak_states"] == b["peak_states"]
