@@ -139,11 +139,45 @@ int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *ro
                      const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows, const int32_t *row_start,
                      const int32_t *row_end, const int32_t *slot, int L, int forward, int maxc, int32_t *ncls,
                      uint64_t *masks, int64_t *weights, int64_t *extra);
+/* the same for row slots beyond one word: masks uint64 [N + 1][maxc][words] (slot s in word s / 64) */
+int tg_sp_bound_data_wide(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
+                          const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows,
+                          const int32_t *row_start, const int32_t *row_end, const int32_t *slot, int L, int forward,
+                          int maxc, int words, int32_t *ncls, uint64_t *masks, int64_t *weights, int64_t *extra);
 int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int64_t *weights, int stride, int K,
                const void *A0, uint64_t n0, const void *H0, int lg0, void *scratch, uint64_t cap_n, void *arena,
                uint64_t arena_bytes, int64_t *out, void *join_results, int64_t *need, void *counters, void *stream);
 /* replaces sp_hist (cdist/sparse_dp.c:239-242): hist is a device uint64[256] */
 int tg_sp_hist(const void *A, uint64_t n, void *hist, void *stream);
+
+/* ---------------------------------------------------------------- sparse Rank DP, wide states
+ * States of W = 1..8 uint64 words (up to 512 row slots; the reference holds at most 56 in C and 64 in
+ * numpy, cdist/sparse_dp.c:3-4, cdist/sparse_dp.py:97-98, and refuses wider trellises).  A table:
+ * keys DEVICE uint64 [W][stride] (word w of state i at w * stride + i), vals DEVICE uint8 [stride],
+ * index DEVICE uint64 [2^lg] (value << 56 | state, empty = all ones).  Masks and states passed by
+ * the host are HOST uint64 [W]; lookahead masks HOST uint64 [ncls][W] (ncls <= 32).  counters:
+ * DEVICE uint64 [4] = states written, changed states, error flags (1 index full, 2 changed list
+ * full, 4 table full), unused.
+ * One column step, the rule of sp_candidates + sp_merge (cdist/sparse_dp.c:118-202) with a column
+ * weight w: staging keys/vals of 2n states (ecap >= 2n) and a staging index of 2^lgs >= 2n slots;
+ * the new table (ncap states) and its index (2^lgn slots); changed states (ccap) when asked. */
+int tg_spw_step(int W, const void *keys, const void *vals, uint64_t n, uint64_t stride, const void *Hold, int lg_old,
+                void *ekeys, void *evals, uint64_t ecap, void *Hs, int lgs, void *nkeys, void *nvals, uint64_t ncap,
+                void *Hn, int lgn, void *ckeys, void *cvals, uint64_t ccap, const uint64_t *upd,
+                const uint64_t *sel_mask, const uint64_t *sel_bits, int cap, int keep_below, int w, int want_changed,
+                int use_h, int K, int ncls, const uint64_t *masks, const int64_t *weights, int64_t extra,
+                const uint64_t *tmask, void *counters, void *stream);
+/* the states with value < below (all for below < 0) into a new table with its index (truncate,
+ * table from arrays); counters[0] = states written */
+int tg_spw_filter(int W, const void *keys, const void *vals, uint64_t n, uint64_t stride, int below, void *nkeys,
+                  void *nvals, uint64_t ncap, void *Hn, int lgn, void *counters, void *stream);
+/* replaces sp_join (cdist/sparse_dp.c:207-236) for wide states: result (DEVICE uint64) =
+ * min(total << 40 | changed state index), all ones when no pair meets */
+int tg_spw_join(int W, const void *fkeys, const void *fvals, uint64_t nf, uint64_t fstride, const void *Hb, int lgb,
+                const void *bkeys, uint64_t bstride, const uint64_t *tmask, void *result, void *stream);
+/* values of m query keys (DEVICE uint64 [W][m]) in a table (255 = absent) */
+int tg_spw_lookup(int W, const void *H, int lg, const void *keys, uint64_t stride, const void *q, uint64_t m,
+                  void *out, void *stream);
 
 /* ---------------------------------------------------------------- completion tables (search)
  * Same entry points as the reference's ctypes binding (cdist/search.py:58-67): */

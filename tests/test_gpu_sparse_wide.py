@@ -1,0 +1,108 @@
+"""Sparse Rank DP on device tables of multi-word states (more than 64 row slots, beyond the
+reference's limit), against the multi-word oracle restatement and the reference's own results."""
+import random
+
+import numpy as np
+import pytest
+
+from helpers import golden, unhex
+from oracle.sparse import NumpyTables
+from oracle.sparse_wide import WideTables
+from test_sparse_oracle import check_witness, interleaved
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+
+
+def _tables(be, tab):
+    keys, vals = be.arrays(tab)
+    return list(keys), np.asarray(vals).tolist()
+
+
+def test_wide_tables_at_every_cut_match_oracle():
+    from tropidist_gb300 import sparse_dp
+    from tropidist_gb300.sparse_tables import WideGpuTables
+    for copies, seed in ((8, 0), (10, 3)):
+        p, _ = interleaved(copies, seed)
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        assert tr.words >= 2
+        for direction, K, use_h in ((+1, 4, True), (-1, 4, True), (+1, 3, False)):
+            sweeps = {}
+            for name, be in (("gpu", WideGpuTables(tr)), ("oracle", WideTables(tr))):
+                sw = sparse_dp.Sweep(tr, direction, K, K, use_h=use_h, every=1, backend=be)
+                sw.run()
+                sweeps[name] = sw
+            g, o = sweeps["gpu"], sweeps["oracle"]
+            assert g.counts == o.counts and g.peak == o.peak
+            for c in range(0, tr.N + 1, 7):
+                assert _tables(g.be, g.ckpt[c]) == _tables(o.be, o.ckpt[c]), (copies, direction, c)
+
+
+def test_wide_frontier_sweeps_match_oracle_cut_by_cut():
+    """Forward frontier sweeps with falling caps: every table and changed set equal the oracle's."""
+    from tropidist_gb300 import sparse_dp
+    from tropidist_gb300.sparse_tables import WideGpuTables
+    rng = random.Random(9)
+    p, _ = interleaved(8, 5)
+    tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+    K = 5
+    caps = sorted((rng.randint(1, K) for _ in range(tr.N + 1)), reverse=True)
+    rec = {}
+    for name, be in (("gpu", WideGpuTables(tr)), ("oracle", WideTables(tr))):
+        sw = sparse_dp.Sweep(tr, +1, K, use_h=True, every=1, frontier=True, backend=be, caps=caps)
+        out = []
+
+        def on_cut(c, tab, ch, extra, sw=sw, out=out):
+            part = _tables(sw.be, ch) if ch is not None else None
+            out.append((c, _tables(sw.be, tab), part))
+            return False
+        sw.run(on_cut=on_cut)
+        rec[name] = out
+    assert rec["gpu"] == rec["oracle"]
+
+
+@pytest.mark.parametrize("words", [1, 2])
+def test_wide_tables_reproduce_reference_queries(words):
+    """One-word problems through the multi-word device tables: the reference's values and peaks."""
+    from tropidist_gb300 import sparse_dp
+    from tropidist_gb300.problem import Problem
+    from tropidist_gb300.sparse_tables import WideGpuTables
+    checked = 0
+    for case in golden("sparse_random.json")[::4]:
+        if not case["feasible"]:
+            continue
+        p = Problem("rand", case["m"], case["k"], case["h"], case["l"])
+        tr = sparse_dp.Trellis.for_query(p, case["obs"], case["order"])
+        for run in case["runs"][::5]:
+            r = sparse_dp.query(tr, run["K"], mode=run["mode"], split=run["split"], use_h=run["use_h"],
+                                backend=WideGpuTables(tr, words=words))
+            assert r["value"] == run["value"] and r["peak_states"] == run["peak_states"], run
+            if run["value"] is not None:
+                check_witness(p, r["witness"], run["value"], case["obs"])
+            checked += 1
+    assert checked > 50
+
+
+def test_wide_queries_and_distance():
+    """Trellises of more than 64 slots: the query value equals the first copy's own and the witness
+    is valid; distance() picks the wide tables by itself."""
+    from tropidist_gb300 import sparse_dp
+    for copies, seed in ((8, 1), (9, 2)):
+        p, first = interleaved(copies, seed)
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        t1 = sparse_dp.Trellis.for_query(first, 0, list(range(first.ncols)))
+        for K, mode in ((4, "mitm"), (6, "mitm"), (4, "forward")):
+            want = sparse_dp.query(t1, K, mode=mode, backend=NumpyTables(t1))
+            got = sparse_dp.query(tr, K, mode=mode)
+            assert got["backend"] == "gpu" and got["value"] == want["value"], (copies, K, mode)
+            if got["value"] is not None:
+                check_witness(p, got["witness"], got["value"], 0)
+        d = sparse_dp.distance(p, order=list(range(p.ncols)), kmax=12)
+        d1 = sparse_dp.distance(first, order=list(range(first.ncols)), kmax=12)
+        assert d["distance"] == d1["distance"]

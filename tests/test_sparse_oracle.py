@@ -203,3 +203,58 @@ def test_c_port_weighted_columns_match_numpy():
             a = sparse_dp.query(tr, K, backend=NumpyTables(tr), witness=False)
             b = sparse_dp.query(tr, K, backend=CPortTables(tr), witness=False)
             assert a["value"] == b["value"] and a["peak_states"] == b["peak_states"]
+
+
+def interleaved(copies, seed=0, m=60, n=120, window=12):
+    """`copies` independent banded problems with their columns interleaved and only the first one
+    carrying the logical row: a trellis as wide as all of them together (beyond one machine word
+    for 5 or more copies) whose distance is the first problem's."""
+    parts = [synth.banded(m, n, window, 3, 1, seed=seed + k) for k in range(copies)]
+    h, l = [], []
+    for j in range(n):
+        for k, q in enumerate(parts):
+            h.append(q.h[j] << (k * m))
+            l.append(q.l[j] if k == 0 else 0)
+    return Problem("interleaved x%d" % copies, m * copies, 1, h, l), parts[0]
+
+
+def test_wide_oracle_matches_numpy_tables():
+    """The multi-word restatement gives NumpyTables' tables at every cut and its query values on
+    one-word states (the reference's own golden tables included)."""
+    from oracle.sparse_wide import WideTables
+    for case in golden("sparse_tables.json"):
+        p = Problem("t", case["nrows"], 1, unhex(case["h"]), unhex(case["l"]))
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        be = WideTables(tr, words=2)
+        sw = sparse_dp.Sweep(tr, +1 if case["forward"] else -1, case["K"], case["K"], use_h=case["use_h"], every=1,
+                             backend=be)
+        sw.run()
+        assert sw.counts == case["counts"]
+        for c, (n, hk, hv) in case["tables"].items():
+            keys, vals = be.arrays(sw.ckpt[int(c)])
+            assert len(keys) == n and sha(np.array(keys, dtype=np.uint64)) == hk and sha(vals) == hv, c
+
+
+def test_wide_trellis_queries():
+    """Trellises of more than 64 row slots (interleaved copies): lookahead classes of every cut
+    against plain per-row loops, and the multi-word query's value equal to the first copy's own
+    (one-word) query, with a valid witness."""
+    from oracle.sparse_wide import WideTables
+    for copies, seed in ((8, 0), (10, 3)):
+        p, first = interleaved(copies, seed)
+        order = list(range(p.ncols))
+        tr = sparse_dp.Trellis.for_query(p, 0, order)
+        assert tr.nslots > 64 and tr.words >= 2
+        for fwd in (True, False):
+            ncls, masks, wts, extra = tr.bound_raw(fwd)
+            slow = tr._bound_data_py(fwd)
+            for c in range(tr.N + 1):
+                got = tuple(sum(int(masks[c, k, q]) << (64 * q) for q in range(tr.words)) for k in range(ncls[c]))
+                assert got == slow[c][0] and tuple(wts[c, :ncls[c]]) == slow[c][1] and extra[c] == slow[c][2]
+        t1 = sparse_dp.Trellis.for_query(first, 0, list(range(first.ncols)))
+        for K in (3, 5):
+            want = sparse_dp.query(t1, K, backend=NumpyTables(t1))
+            got = sparse_dp.query(tr, K, backend=WideTables(tr))
+            assert got["value"] == want["value"]
+            if got["value"] is not None:
+                check_witness(p, got["witness"], got["value"], 0)

@@ -977,15 +977,19 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
 // grouped into classes of equal weight (masks of slots, weights ascending), L's weight is `extra`.
 // Output per cut: ncls[c], masks / weights [c][maxc], extra[c].  Returns 0, or -4 if a cut has
 // more than maxc classes.
-int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
-                     const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows, const int32_t *row_start,
-                     const int32_t *row_end, const int32_t *slot, int L, int forward, int maxc, int32_t *ncls,
-                     uint64_t *masks, int64_t *weights, int64_t *extra) {
-    if (N < 0 || nrows <= 0 || !row_ptr || !col_ptr || !act_ptr || !ncls || !masks || !weights || !extra || maxc < 1)
+int tg_sp_bound_data_wide(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
+                          const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows,
+                          const int32_t *row_start, const int32_t *row_end, const int32_t *slot, int L, int forward,
+                          int maxc, int words, int32_t *ncls, uint64_t *masks, int64_t *weights, int64_t *extra) {
+    if (N < 0 || nrows <= 0 || !row_ptr || !col_ptr || !act_ptr || !ncls || !masks || !weights || !extra || maxc < 1 ||
+        words < 1)
         return set_error(TG_ERR_ARG, "bad bound data");
+    for (int r = 0; r < nrows; r++)
+        if (slot[r] < 0 || slot[r] >= 64 * words) return set_error(TG_ERR_ARG, "row slot beyond the mask words");
     std::vector<char> inrel(nrows, 0);
     std::vector<int> rel;
-    std::vector<std::pair<int64_t, uint64_t>> cls;
+    // weight classes: (weight in 1/Q units, first row of the class); a row joins its class's mask
+    std::vector<std::pair<int64_t, std::vector<uint64_t>>> cls;
     for (int c = 0; c <= N; c++) {
         rel.assign(act_rows + act_ptr[c], act_rows + act_ptr[c + 1]);
         const bool lone = forward ? row_start[L] >= c : row_end[L] < c;
@@ -1019,10 +1023,10 @@ int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *ro
             }
             const int64_t wr = SP_QW / worst;
             if (lone && r == L) { extra[c] = wr; continue; }
-            bool found = false;
-            for (auto &x : cls)
-                if (x.first == wr) { x.second |= 1ull << slot[r]; found = true; break; }
-            if (!found) cls.push_back({wr, 1ull << slot[r]});
+            size_t k = 0;
+            while (k < cls.size() && cls[k].first != wr) k++;
+            if (k == cls.size()) cls.push_back({wr, std::vector<uint64_t>(words, 0ull)});
+            cls[k].second[slot[r] >> 6] |= 1ull << (slot[r] & 63);
         }
         for (int r : rel) inrel[r] = 0;
         if ((int)cls.size() > maxc) return set_error(TG_ERR_TOO_BIG, "more lookahead classes than the output holds");
@@ -1030,10 +1034,18 @@ int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *ro
         ncls[c] = (int32_t)cls.size();
         for (size_t k = 0; k < cls.size(); k++) {
             weights[(size_t)c * maxc + k] = cls[k].first;
-            masks[(size_t)c * maxc + k] = cls[k].second;
+            for (int w = 0; w < words; w++) masks[((size_t)c * maxc + k) * words + w] = cls[k].second[w];
         }
     }
     return TG_OK;
+}
+
+int tg_sp_bound_data(int N, int nrows, const int64_t *row_ptr, const int32_t *row_cols, const int64_t *col_ptr,
+                     const int32_t *col_rows, const int64_t *act_ptr, const int32_t *act_rows, const int32_t *row_start,
+                     const int32_t *row_end, const int32_t *slot, int L, int forward, int maxc, int32_t *ncls,
+                     uint64_t *masks, int64_t *weights, int64_t *extra) {
+    return tg_sp_bound_data_wide(N, nrows, row_ptr, row_cols, col_ptr, col_rows, act_ptr, act_rows, row_start, row_end,
+                                 slot, L, forward, maxc, 1, ncls, masks, weights, extra);
 }
 
 // GF(2) rank of the first i columns of `order` for i = 0..ncols (host work, no GPU; the rank
