@@ -56,7 +56,7 @@ def parse():
                     help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--tree-only", action="store_true",
                     help="run only the tree DP section (for profiling) and print its JSON")
-    ap.add_argument("--sections", default="batched,served,sparse,tree,witness,search",
+    ap.add_argument("--sections", default="batched,served,sparse,sparse_full,tree,witness,search",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
 
@@ -418,37 +418,71 @@ def section_served(args):
     return res
 
 
-def section_sparse(args):
-    """The circuit-style detector error model scaled to 24 checks per round (40 rounds, n=20000,
-    weights {1,2,3}; 37 row slots: the as-written 150 checks need about 260 slots, beyond the
-    56-slot states of the reference's C tables and of these device tables) through the sparse DP
-    with meet in the middle at a weight threshold whose tables fit the device; the numpy
-    restatement of the reference's tables times the same query at a lower threshold on the host."""
+def _sparse_run(tr, K, backend="gpu", witness=False):
+    """One meet-in-the-middle query timed around the whole call: value, seconds, state-steps (the
+    states of every table stepped, both sweeps), peak states."""
     import torch
-    from tropidist_gb300 import sparse_dp, synth
-    from oracle import sparse as osp
-    p = synth.circuit_dem(seed=0, rounds=40, checks=24, ncols=20000)
-    order = sparse_dp.default_order(p)
-    tr = sparse_dp.Trellis.for_query(p, 0, order)
-    out = {"workload": "circuit DEM 40 rounds x 24 checks, n=20000, weights {1,2,3}, seed 0",
-           "slots": tr.nslots}
-    for K in (4, 8):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = sparse_dp.query(tr, K, mode="mitm", backend="gpu", witness=False)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        sm = sparse_dp.summary(r)
-        steps = sum(v for k, v in sm.items() if k.endswith("_states_total"))
-        out["K%d" % K] = {"value": r["value"], "seconds": dt, "state_steps": int(steps),
-                          "state_steps_per_s": steps / dt, "peak_states": sm.get("peak_states")}
+    from tropidist_gb300 import sparse_dp
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    r = sparse_dp.query(tr, 4, mode="mitm", backend=osp.NumpyTables(tr), witness=False)
+    r = sparse_dp.query(tr, K, mode="mitm", backend=backend, witness=witness)
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     sm = sparse_dp.summary(r)
     steps = sum(v for k, v in sm.items() if k.endswith("_states_total"))
-    out["cpu_baseline"] = {"K": 4, "value": r["value"], "seconds": dt, "state_steps_per_s": steps / dt,
-                           "kind": "port", "cores": 1, "sample": "the K=4 query, numpy restatement"}
+    return {"value": r["value"], "s": round(dt, 3), "state_steps": int(steps),
+            "steps_per_s": round(steps / dt), "peak": sm.get("peak_states")}
+
+
+def section_sparse(args):
+    """The circuit-style detector error model scaled to 24 checks per round (40 rounds, n=20000,
+    weights {1,2,3}, seed 0; 37 row slots: one-word states, the reference's C tables can hold it)
+    through the meet in the middle at K = 4, 8 and 10 on the device tables; the C port of the
+    reference's sparse kernels (oracle/sparse_port.c, one core, as the reference's
+    sparse_dp.c) behind the same host driver at K = 4 and 8."""
+    from tropidist_gb300 import sparse_dp, synth
+    from oracle.sparse import CPortTables
+    p = synth.circuit_dem(seed=0, rounds=40, checks=24, ncols=20000)
+    order = sparse_dp.default_order(p)
+    tr = sparse_dp.Trellis.for_query(p, 0, order)
+    _sparse_run(tr, 2)                                  # warm-up (library, allocator)
+    out = {"slots": tr.nslots}
+    for K in (4, 8, 10):
+        out["K%d" % K] = _sparse_run(tr, K)
+    if not args.no_cpu_baseline:
+        for K in (4, 8):
+            c = _sparse_run(tr, K, backend=CPortTables(tr))
+            c["equal"] = c["value"] == out["K%d" % K]["value"]
+            out["cpu_K%d" % K] = c
+    return out
+
+
+def section_sparse_full(args):
+    """The circuit-style detector error model as written: 40 rounds x 150 checks (m = 6000), n =
+    20000, weights {1,2,3}, seed 0, the package's column order: 153 row slots, so three-word
+    states on the device (the reference refuses more than 56).  Meet in the middle at K = 4, 8,
+    then 10, 12 and 14 while a query stays within 90 s; the multi-word numpy restatement of the
+    reference's table rules (oracle/sparse_wide.py) at K = 4 and 5 on one core."""
+    from tropidist_gb300 import sparse_dp, synth
+    from oracle.sparse_wide import WideTables
+    p = synth.circuit_dem(seed=0, rounds=40, checks=150, ncols=20000)
+    tr = sparse_dp.Trellis.for_query(p, 0, sparse_dp.default_order(p))
+    _sparse_run(tr, 2)
+    out = {"slots": tr.nslots, "words": tr.words}
+    for K in (4, 8, 10, 12, 14):
+        try:
+            r = _sparse_run(tr, K)
+        except (MemoryError, RuntimeError) as e:
+            out["K%d" % K] = {"error": type(e).__name__}
+            break
+        out["K%d" % K] = r
+        if r["s"] > 90:
+            break
+    if not args.no_cpu_baseline:
+        for K in (4, 5):
+            c = _sparse_run(tr, K, backend=WideTables(tr))
+            c["equal"] = c["value"] == out.get("K%d" % K, {}).get("value", c["value"])
+            out["cpu_K%d" % K] = c
     return out
 
 
@@ -625,8 +659,9 @@ def _search_cpu(p, kmax):
                       "reference's completion table (cdist/gmitm.c tab_build / tab_lookup)"}
 
 
-SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse, "tree": section_tree,
-            "witness": section_witness, "search": section_search}
+SECTIONS = {"batched": section_batched, "served": section_served, "sparse": section_sparse,
+            "sparse_full": section_sparse_full, "tree": section_tree, "witness": section_witness,
+            "search": section_search}
 
 
 # ---------------------------------------------------------------------- GPU arm

@@ -191,6 +191,13 @@ int tg_tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const u
  * R (int32[m]) -> out (int32[m]): least cost <= R[q] with the same fingerprint and another label, or -1 */
 int tg_tab_lookup_dev(void *t, uint64_t m, const void *zh, const void *zl, const void *lg, const void *R,
                       void *out, void *stream);
+/* The reference's exact names and signatures, bound by cdist/search.py:58-67 (ctypes) and
+ * defined at cdist/gmitm.c:61 (tab_create), :78 (tab_free), :84 (tab_count), :176 (tab_build):
+ * thin forms of the tg_tab_* functions above (tab_create returns NULL on allocation failure). */
+void *tab_create(int log2slots, int wide);
+void tab_free(void *t);
+int64_t tab_count(void *t);
+void tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, int k);
 
 /* ---------------------------------------------------------------- batched dense Rank DP
  * Many plans (op streams ops[offsets[i]..offsets[i+1]), uint8) in one persistent launch fed from a
@@ -201,6 +208,9 @@ int tg_batch_info(void *batch, int64_t *info, int ninfo);
 /* window: plans in progress at once (0: all), admitted widest first */
 int tg_batch_run(void *batch, void *arena, int blocks, int window, uint32_t *values, void *stream);
 void tg_batch_free(void *batch);
+/* polls of one device wait for work before a block gives up and the run returns TG_ERR_TIMEOUT
+ * (-5) with the context still usable; 0 restores the default (about 2.5 s of polling) */
+int tg_batch_set_spin_limit(uint64_t polls);
 
 /* ---------------------------------------------------------------- continuous serving
  * A long-lived persistent launch that takes new plans while it runs (no counterpart in the

@@ -50,3 +50,22 @@ def test_batched_distances_of_instances():
     got = batched_dp_distances(ps)
     for p, g in zip(ps, got):
         assert g == auto.dp_distance(p, list(range(p.ncols)))
+
+
+def test_bounded_wait_runs_out_and_returns_timeout():
+    """A device wait for work bounded at one poll: the blocks that find no unit at once give up, the
+    run returns TG_ERR_TIMEOUT (TimeoutError here) instead of waiting on, and the context stays
+    usable: the same batch then gives the right value under the default bound."""
+    from tropidist_gb300 import _lib, kernel, synth, trellis
+    from tropidist_gb300.batch import DenseBatch
+    p = synth.banded(200, 400, 20, 3, 1, seed=4)
+    plan = trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows)
+    b = DenseBatch([plan])
+    L = _lib.lib()
+    try:
+        assert L.tg_batch_set_spin_limit(1) == 0
+        with pytest.raises(TimeoutError):
+            b.run()
+    finally:
+        L.tg_batch_set_spin_limit(0)
+    assert b.run() == [kernel.run_plan(plan)[0]]

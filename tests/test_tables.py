@@ -80,3 +80,24 @@ def test_wide_and_labelfree_tables():
         want = [ot.lookup(ent, zl[i], lab[i], 2, wide=T.wide) for i in range(len(syn))]
         assert got.tolist() == want
         T.free()
+
+
+@pytest.mark.gpu
+def test_reference_named_table_entry_points():
+    """tab_create / tab_build / tab_count / tab_free with the reference's own names and arity
+    (cdist/search.py:58-67), called as its ctypes binding calls them: the reference's entry counts."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from tropidist_gb300 import _lib
+    L = _lib.lib()
+    for case in golden("tables.json"):
+        zh = np.array(unhex(case["zh"]), dtype=np.uint64)
+        zl = np.array(unhex(case["zl"]), dtype=np.uint64)
+        lg = np.array(case["l"], dtype=np.uint64)
+        t = L.tab_create(case["log2slots"], 0)
+        assert t
+        L.tab_build(t, len(zh), zh.ctypes.data, zl.ctypes.data, lg.ctypes.data, case["k"])
+        assert L.tab_count(t) == case["entries"]
+        L.tab_free(t)

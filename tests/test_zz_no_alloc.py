@@ -26,6 +26,8 @@ def _plans():
         out.append(trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows))
     p = synth.banded(300, 600, 22, 3, 1, seed=5)          # fused passes, peak about 19 bits
     out.append(trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows))
+    p = synth.banded(300, 600, 24, 3, 1, seed=2)          # peak exactly 22 bits: the whole scratch
+    out.append(trellis.build_plan(p.h, p.l, 1, list(range(p.ncols)), p.nrows))
     return [pl for pl in out if pl.feasible]
 
 
@@ -37,6 +39,8 @@ def test_noalloc_matches_allocating_entry_point_twice():
     stream = torch.cuda.current_stream().cuda_stream
     plans = _plans()
     assert any(pl.peak_bits > 16 for pl in plans)
+    assert any(pl.peak_bits == 22 for pl in plans)          # the largest plan the scratch holds
+    wants = []
     for plan in plans:
         ops = np.ascontiguousarray(plan.encode())
         n = 1 << plan.peak_bits
@@ -44,12 +48,22 @@ def test_noalloc_matches_allocating_entry_point_twice():
         b = torch.empty(n, dtype=torch.uint8, device="cuda")
         want = ctypes.c_uint32(0)
         assert L.tg_dense_run(ops.ctypes.data, len(ops), 1, a.data_ptr(), b.data_ptr(), ctypes.byref(want), stream) == 0
+        wants.append(want.value)
         table = torch.full((n,), 77, dtype=torch.uint8, device="cuda")
         for _ in range(2):
             got = ctypes.c_uint32(12345)
             st = L.tg_dense_run_noalloc(ops.ctypes.data, len(ops), table.data_ptr(), n, ctypes.byref(got), stream)
             assert st == 0, L.tg_last_error()
             assert got.value == want.value, (plan.peak_bits, got.value, want.value)
+    # the scratch keeps the last call's contents: calls alternating between plans of different
+    # widths still agree with the allocating entry point
+    for plan, want in list(zip(plans, wants))[::-1] + list(zip(plans, wants)):
+        ops = np.ascontiguousarray(plan.encode())
+        n = 1 << plan.peak_bits
+        table = torch.full((n,), 200, dtype=torch.uint8, device="cuda")
+        got = ctypes.c_uint32(12345)
+        assert L.tg_dense_run_noalloc(ops.ctypes.data, len(ops), table.data_ptr(), n, ctypes.byref(got), stream) == 0
+        assert got.value == want
 
 
 def test_noalloc_refuses_plans_beyond_its_scratch():

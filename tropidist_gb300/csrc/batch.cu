@@ -545,6 +545,14 @@ __global__ void k_batch_values(const uint8_t *arena, const uint64_t *offs, int n
 // progress at once (0: all); waiting plans are admitted widest first as running ones finish, which
 // keeps the tables of the plans in progress within L2 when the window is small.  Returns
 // TG_ERR_TIMEOUT if a block waited longer than its bound for work (the launch still returns).
+// polls of one wait for work before a block gives up (0: the default, about 2.5 s)
+static unsigned long long g_batch_spin = 0;
+
+int tg_batch_set_spin_limit(uint64_t polls) {
+    g_batch_spin = polls;
+    return TG_OK;
+}
+
 int tg_batch_run(void *p, void *arena, int blocks, int window, uint32_t *values, void *stream) {
     if (!p || !arena || !values) return set_error(TG_ERR_ARG, "null argument");
     BatchPlan &B = *static_cast<BatchPlan *>(p);
@@ -604,7 +612,7 @@ int tg_batch_run(void *p, void *arena, int blocks, int window, uint32_t *values,
     A.admit = dc + 4 * nj + 8;
     A.nadmit = nadmit;
     A.nplans = (unsigned)B.nplans;
-    A.spin_limit = 20000000ull;          // about 2.5 s of polling at the sleep lengths used
+    A.spin_limit = g_batch_spin ? g_batch_spin : 20000000ull;   // about 2.5 s of polling by default
     int grid = blocks > 0 ? blocks : sm_count();
     if (finished < (unsigned)B.nplans) {
         k_batch<<<grid, BT_THREADS, BT_TILE_SMEM + 4096, st>>>(A);

@@ -24,6 +24,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 namespace tg {
@@ -1498,22 +1500,30 @@ static void emulate_plan(const DensePlan &P, E *a, E *b, void **ckpt) {
 #define TG_NOALLOC_MAX_BITS 22
 static __device__ __align__(256) uint8_t g_noalloc_scratch[1u << TG_NOALLOC_MAX_BITS];
 #define TG_NOALLOC_MAX_DEVICES 64
-static uint8_t *g_noalloc_ptr[TG_NOALLOC_MAX_DEVICES];
+static std::atomic<uint8_t *> g_noalloc_ptr[TG_NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
 
-// device address of the scratch array on the current device (looked up once per device; the
-// array's name in host code is only a stand-in, not an address a kernel may use)
+// device address of the scratch array on the current device (looked up once per device, under a
+// lock so that two host threads making their first call at once agree; the array's name in host
+// code is only a stand-in, not an address a kernel may use)
 static int noalloc_scratch(uint8_t **out) {
     int dev = 0;
     int e = cuda_check(cudaGetDevice(&dev), "get device");
     if (e) return e;
     if (dev < 0 || dev >= TG_NOALLOC_MAX_DEVICES) return set_error(TG_ERR_TOO_BIG, "device index beyond the table");
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        e = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch), "scratch symbol address");
-        if (e) return e;
-        g_noalloc_ptr[dev] = static_cast<uint8_t *>(p);
+    uint8_t *p = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        p = g_noalloc_ptr[dev].load(std::memory_order_relaxed);
+        if (!p) {
+            void *q = nullptr;
+            e = cuda_check(cudaGetSymbolAddress(&q, g_noalloc_scratch), "scratch symbol address");
+            if (e) return e;
+            p = static_cast<uint8_t *>(q);
+            g_noalloc_ptr[dev].store(p, std::memory_order_release);
+        }
     }
-    *out = g_noalloc_ptr[dev];
+    *out = p;
     return TG_OK;
 }
 

@@ -262,4 +262,21 @@ int tg_tab_lookup_dev(void *p, uint64_t m, const void *zh, const void *zl, const
     return cuda_check(cudaGetLastError(), "table lookup");
 }
 
+// The reference's own names and signatures (cdist/search.py:58-67 binds them with ctypes), so a
+// binding written for cdist's libgmitm can load this library unchanged: NULL from tab_create when
+// the table cannot be allocated (the reference's binding raises MemoryError on NULL), tab_build on
+// HOST arrays zh, zl, lg of n columns.
+void *tab_create(int log2slots, int wide) {
+    int status = 0;
+    return tg_tab_create(log2slots, wide, &status);
+}
+
+void tab_free(void *t) { tg_tab_free(t); }
+
+int64_t tab_count(void *t) { return tg_tab_count(t); }
+
+void tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, int k) {
+    tg_tab_build(t, n, zh, zl, lg, k);
+}
+
 }  // extern "C"
