@@ -928,6 +928,8 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             if (eb == 1) {
                 build_groups(pp, selmask);
                 if (g_cosets) build_stream(pp, local, d_in, out, sel_rows, sel_tg, w_in, (int)cout_.size());
+                // tables that fit L2 together (in + out <= 64 MB) keep their stores cached for the next pass
+                pp.s_l2 = ((1ull << w_in) + (1ull << cout_.size())) <= (64ull << 20) ? 1 : 0;
             }
             phys = out;
             canon = cout_;

@@ -165,6 +165,7 @@ struct PassParams {
     // registers with __shfl_xor (code s_lcode: register xor | lane swap << 6, weight s_lw)
     int s_lane, nkt;                   // nkt = nk + s_lane: coset-number bits of a tile
     int s_lgen;                        // 1: the lane update has an in-chunk part (general path)
+    int s_l2;                          // 1: input and output fit L2 together (stores stay cached)
     uint32_t s_lvec, s_lin, s_lout;
     uint8_t s_lcode, s_lw;
     uint8_t s_cw[4];
@@ -422,55 +423,52 @@ static __device__ __forceinline__ void lane_dispatch(uint32_t code, uint32_t (&R
     }
 }
 
-// mode-1 output chunks of a coset: the member pairs (x, x ^ PB) that differ in chunk bit 0, without
-// in-chunk bit s_bit
-template <int PB>
-static __device__ __forceinline__ void u8_stream_pairs(const PassParams &P, const uint32_t (&W)[32], uint32_t keep,
-                                                      uint8_t *dst, uint32_t outc, uint32_t c0b) {
-#pragma unroll
-    for (int x = 0; x < 8; x++) {
-        if (x & PB) continue;
-        if (!((keep >> x) & 1u)) continue;
-        const uint4 M0 = make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]);
-        const uint4 M1 = make_uint4(W[4 * (x | PB)], W[4 * (x | PB) + 1], W[4 * (x | PB) + 2], W[4 * (x | PB) + 3]);
-        const bool sw = (P.sxoff[x] ^ c0b) & 1u;   // member x has chunk bit 0 set: it is the upper one
-        const uint4 A = sw ? M1 : M0, B = sw ? M0 : M1;
-        uint8_t *const o = dst + (outc ^ P.xout[x]);
-        if (P.s_both) {
-            __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, 0u));
-            __stcs(reinterpret_cast<uint4 *>(o + P.s_w), gather_one_select(A, B, P.s_bit, 1u));
-        } else {
-            __stcs(reinterpret_cast<uint4 *>(o), gather_one_select(A, B, P.s_bit, P.s_tgt));
-        }
+// ---- the coset of one thread in one step (straight-line code, no per-member switches)
+// member x's 16 entries widened into R[8x .. 8x + 7] (u16 lanes) in the canonical permuted form: the
+// unpack selectors realise the in-chunk XOR on entry bits 0-1, and for word-permuted members (WS)
+// the entry word k is read from storage word k ^ wsw (bits 2-3) by its shared-memory address
+template <bool WS>
+static __device__ __forceinline__ void u8_unpack_member(const PassParams &P, const uint8_t *src, int x, bool is_inf,
+                                                        uint32_t *R) {
+    uint32_t w0, w1, w2, w3;
+    if (WS) {
+        const uint32_t ws4 = 4u * P.s_wsw[x];
+        const uint8_t *m = src + x * 512;
+        w0 = *reinterpret_cast<const uint32_t *>(m + (0u ^ ws4));
+        w1 = *reinterpret_cast<const uint32_t *>(m + (4u ^ ws4));
+        w2 = *reinterpret_cast<const uint32_t *>(m + (8u ^ ws4));
+        w3 = *reinterpret_cast<const uint32_t *>(m + (12u ^ ws4));
+    } else {
+        const uint4 v = *reinterpret_cast<const uint4 *>(src + x * 512);
+        w0 = v.x; w1 = v.y; w2 = v.z; w3 = v.w;
     }
+    if (is_inf) w0 = w1 = w2 = w3 = 0xFFFFFFFFu;
+    const uint32_t se = P.s_selu[x][0], so = P.s_selu[x][1];
+    R[0] = __byte_perm(w0, 0u, se); R[1] = __byte_perm(w0, 0u, so);
+    R[2] = __byte_perm(w1, 0u, se); R[3] = __byte_perm(w1, 0u, so);
+    R[4] = __byte_perm(w2, 0u, se); R[5] = __byte_perm(w2, 0u, so);
+    R[6] = __byte_perm(w3, 0u, se); R[7] = __byte_perm(w3, 0u, so);
 }
 
-// One coset of a streaming pass: its 8 staged chunks (INF where `inf`) into registers in the
-// canonical permuted form, the residual updates, the NC canonical updates (straight-line code:
-// member x with member x ^ 2^j), back to entry order and out to the output chunks (`keep`).
-template <int NC, bool WS, bool GEN = false>
-static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, const uint8_t *src, uint32_t inf,
-                                                      uint32_t keep, uint8_t *dst, uint32_t outc, uint32_t c0b) {
-    uint32_t R[64];
-#pragma unroll
-    for (int x = 0; x < 8; x++) {
-        uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
-        if (!((inf >> x) & 1u)) v = *reinterpret_cast<const uint4 *>(src + x * 512);
-        const uint32_t se = P.s_selu[x][0], so = P.s_selu[x][1];
-        uint32_t w0 = v.x, w1 = v.y, w2 = v.z, w3 = v.w;
-        if (WS) switch (P.s_wsw[x]) {  // storage word k holds entry word k ^ wsw (uniform branch)
-            case 1: w0 = v.y; w1 = v.x; w2 = v.w; w3 = v.z; break;
-            case 2: w0 = v.z; w1 = v.w; w2 = v.x; w3 = v.y; break;
-            case 3: w0 = v.w; w1 = v.z; w2 = v.y; w3 = v.x; break;
-            default: break;
-        }
-        R[8 * x + 0] = __byte_perm(w0, 0u, se); R[8 * x + 1] = __byte_perm(w0, 0u, so);
-        R[8 * x + 2] = __byte_perm(w1, 0u, se); R[8 * x + 3] = __byte_perm(w1, 0u, so);
-        R[8 * x + 4] = __byte_perm(w2, 0u, se); R[8 * x + 5] = __byte_perm(w2, 0u, so);
-        R[8 * x + 6] = __byte_perm(w3, 0u, se); R[8 * x + 7] = __byte_perm(w3, 0u, so);
-    }
+// member x back to its 16 bytes in storage order
+template <bool WS>
+static __device__ __forceinline__ uint4 u8_pack_member(const PassParams &P, int x, const uint32_t *R) {
+    const uint32_t sp = P.s_selp[x];
+    const uint32_t q0 = __byte_perm(R[0], R[1], sp), q1 = __byte_perm(R[2], R[3], sp);
+    const uint32_t q2 = __byte_perm(R[4], R[5], sp), q3 = __byte_perm(R[6], R[7], sp);
+    if (!WS) return make_uint4(q0, q1, q2, q3);
+    // storage word k holds entry word k ^ wsw
+    const uint32_t ws = P.s_wsw[x];
+    const bool b0 = ws & 1u, b1 = ws & 2u;
+    const uint32_t t0 = b0 ? q1 : q0, t1 = b0 ? q0 : q1, t2 = b0 ? q3 : q2, t3 = b0 ? q2 : q3;
+    return b1 ? make_uint4(t2, t3, t0, t1) : make_uint4(t0, t1, t2, t3);
+}
+
+// the coset's updates on its registers: NC canonical member pairings, the lane update, or (GEN) every
+// update through its code
+template <int NC, bool GEN>
+static __device__ __forceinline__ void u8_stream_updates(const PassParams &P, uint32_t (&R)[64]) {
     if constexpr (GEN) {
-        // general form (residual updates present): every update through the code switch
         for (int u = 0; u < P.s_nc; u++) {
             const uint32_t w = P.s_cw[u];
             reg_dispatch(8u << u, R, w | (w << 16));
@@ -488,32 +486,33 @@ static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, cons
         if (GEN) lane_dispatch(P.s_lcode, R, w | (w << 16));
         else LanePairs<0, 0, 0>::run(R, w | (w << 16));
     }
-    uint32_t W[32];
+}
+
+// an output chunk: kept in L2 when the next pass reads it from there, else streamed out
+static __device__ __forceinline__ void u8_store(const PassParams &P, uint8_t *p, const uint4 &v) {
+    if (P.s_l2) __stcg(reinterpret_cast<uint4 *>(p), v);
+    else __stcs(reinterpret_cast<uint4 *>(p), v);
+}
+
+// mode-1 output chunks: the member pairs (x, x ^ PB) that differ in chunk bit 0, without in-chunk
+// bit s_bit (one or both halves stored)
+template <int PB, bool WS>
+static __device__ __forceinline__ void u8_stream_store_pairs(const PassParams &P, const uint32_t (&R)[64],
+                                                            uint32_t keep, uint8_t *dst, uint32_t outc, uint32_t c0b) {
 #pragma unroll
     for (int x = 0; x < 8; x++) {
-        const uint32_t sp = P.s_selp[x];
-        const uint32_t q0 = __byte_perm(R[8 * x + 0], R[8 * x + 1], sp), q1 = __byte_perm(R[8 * x + 2], R[8 * x + 3], sp);
-        const uint32_t q2 = __byte_perm(R[8 * x + 4], R[8 * x + 5], sp), q3 = __byte_perm(R[8 * x + 6], R[8 * x + 7], sp);
-        // entry word k is storage word k ^ wsw
-        switch (WS ? P.s_wsw[x] : 0) {
-            case 1: W[4 * x] = q1; W[4 * x + 1] = q0; W[4 * x + 2] = q3; W[4 * x + 3] = q2; break;
-            case 2: W[4 * x] = q2; W[4 * x + 1] = q3; W[4 * x + 2] = q0; W[4 * x + 3] = q1; break;
-            case 3: W[4 * x] = q3; W[4 * x + 1] = q2; W[4 * x + 2] = q1; W[4 * x + 3] = q0; break;
-            default: W[4 * x] = q0; W[4 * x + 1] = q1; W[4 * x + 2] = q2; W[4 * x + 3] = q3; break;
+        if (x & PB) continue;
+        if (!((keep >> x) & 1u)) continue;
+        const uint4 M0 = u8_pack_member<WS>(P, x, R + 8 * x), M1 = u8_pack_member<WS>(P, x | PB, R + 8 * (x | PB));
+        const bool sw = (P.sxoff[x] ^ c0b) & 1u;   // member x has chunk bit 0 set: it is the upper one
+        const uint4 A = sw ? M1 : M0, B = sw ? M0 : M1;
+        uint8_t *const o = dst + (outc ^ P.xout[x]);
+        if (P.s_both) {
+            u8_store(P, o, gather_one_select(A, B, P.s_bit, 0u));
+            u8_store(P, o + P.s_w, gather_one_select(A, B, P.s_bit, 1u));
+        } else {
+            u8_store(P, o, gather_one_select(A, B, P.s_bit, P.s_tgt));
         }
-    }
-    if (P.s_mode == 0) {
-#pragma unroll
-        for (int x = 0; x < 8; x++)
-            if ((keep >> x) & 1u)
-                __stcs(reinterpret_cast<uint4 *>(dst + (outc ^ P.xout[x])),
-                       make_uint4(W[4 * x], W[4 * x + 1], W[4 * x + 2], W[4 * x + 3]));
-    } else if (P.s_pb == 0) {
-        u8_stream_pairs<1>(P, W, keep, dst, outc, c0b);
-    } else if (P.s_pb == 1) {
-        u8_stream_pairs<2>(P, W, keep, dst, outc, c0b);
-    } else {
-        u8_stream_pairs<4>(P, W, keep, dst, outc, c0b);
     }
 }
 
@@ -521,9 +520,75 @@ static __device__ __forceinline__ void u8_stream_coset(const PassParams &P, cons
 // the tile's chunks (c0 fixed per thread for the whole launch), stages its 8 input chunks in its
 // own shared-memory slots with cp.async three tiles ahead (no barriers: a thread reads back only
 // its own copies), applies the group's updates in registers and stores the output chunks straight
-// to global memory.  A block covers 512 >> nk tiles per step; steps [s0, s1) in order.
+// to global memory, member by member.  A block covers 512 >> nk tiles per step; steps [s0, s1) in
+// order.  The variant (canonical updates, word permutation, general codes) is chosen once per range.
 #define FS_STAGES 3
 #define FS_WARP_BYTES (FS_STAGES * 8 * 512)      // staging bytes of one warp
+
+template <int NC, bool WS, bool GEN>
+static __device__ __forceinline__ void u8_stream_loop(const PassParams &P, uint64_t s0, uint64_t s1,
+                                                      const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
+                                                      uint8_t *stage0, const int64_t *s_cin, const int64_t *s_cout,
+                                                      int g, int ng, uint32_t j, uint32_t keep, uint32_t inf,
+                                                      uint32_t c0b, uint32_t inc, uint32_t outc, uint64_t ib,
+                                                      uint64_t ob) {
+    const uint64_t ntiles = P.ntiles;
+    auto issue = [&](uint64_t s, uint64_t b, int st) {
+        if ((((s << g) | j) < ntiles)) {
+            uint8_t *dst = stage0 + st * 4096;
+            const uint8_t *base = in + b;
+#pragma unroll
+            for (int x = 0; x < 8; x++)
+                if (!((inf >> x) & 1u)) cp_async16(dst + x * 512, base + (inc ^ P.xin[x]));
+        }
+        cp_async_commit();
+    };
+    auto advance = [&](uint64_t s, uint64_t &bi, uint64_t &bo) {   // bases of step s + 1 from step s
+        const int q = __ffsll((long long)~s) - 1 + ng;
+        if (q < P.n_outer) { bi += s_cin[q]; bo += s_cout[q]; }
+    };
+    uint64_t ibn = ib, dummy = 0;
+    // prologue: steps s0 and s0 + 1 in flight
+    issue(s0, ibn, 0);
+    if (s0 + 1 < s1) {
+        advance(s0, ibn, dummy);
+        issue(s0 + 1, ibn, 1);
+    } else {
+        cp_async_commit();
+    }
+    int st = 0;
+    for (uint64_t s = s0; s < s1; s++) {
+        if (s + 2 < s1) {
+            advance(s + 1, ibn, dummy);
+            issue(s + 2, ibn, st == 0 ? 2 : st - 1);
+        } else {
+            cp_async_commit();
+        }
+        cp_async_wait_group<2>();
+        if (((s << g) | j) < ntiles) {
+            const uint8_t *src = stage0 + st * 4096;
+            uint32_t R[64];
+#pragma unroll
+            for (int x = 0; x < 8; x++) u8_unpack_member<WS>(P, src, x, (inf >> x) & 1u, R + 8 * x);
+            u8_stream_updates<NC, GEN>(P, R);
+            uint8_t *const dst = out + ob;
+            if (P.s_mode == 0) {
+#pragma unroll
+                for (int x = 0; x < 8; x++)
+                    if ((keep >> x) & 1u) u8_store(P, dst + (outc ^ P.xout[x]), u8_pack_member<WS>(P, x, R + 8 * x));
+            } else if (P.s_pb == 0) {
+                u8_stream_store_pairs<1, WS>(P, R, keep, dst, outc, c0b);
+            } else if (P.s_pb == 1) {
+                u8_stream_store_pairs<2, WS>(P, R, keep, dst, outc, c0b);
+            } else {
+                u8_stream_store_pairs<4, WS>(P, R, keep, dst, outc, c0b);
+            }
+        }
+        st = st == FS_STAGES - 1 ? 0 : st + 1;
+        if (s + 1 < s1) advance(s, dummy, ob);
+    }
+    cp_async_wait_group<0>();
+}
 
 static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint64_t s0, uint64_t s1,
                                                    const uint8_t *__restrict__ in, uint8_t *__restrict__ out,
@@ -560,62 +625,30 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
     uint64_t ib = jin, ob = jout;                      // bases of step s0
     for (int q = ng; q < P.n_outer; q++)
         if ((s0 >> (q - ng)) & 1ull) { ib += P.outer_in[q]; ob += P.outer_out[q]; }
-    const uint64_t ntiles = P.ntiles;
     __syncthreads();
     // programmatic dependent launch: everything above overlapped the previous pass; its writes (our
     // input) and reads (our output buffer) are complete past this point
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
     uint8_t *const stage0 = reinterpret_cast<uint8_t *>(smem_raw) + (size_t)warp * FS_WARP_BYTES + lane * 16u;
-    auto issue = [&](uint64_t s, uint64_t b, int st) {
-        if ((((s << g) | j) < ntiles)) {
-            uint8_t *dst = stage0 + st * 4096;
-#pragma unroll
-            for (int x = 0; x < 8; x++)
-                if (!((inf >> x) & 1u)) cp_async16(dst + x * 512, in + b + (inc ^ P.xin[x]));
-        }
-        cp_async_commit();
-    };
-    auto advance = [&](uint64_t s, uint64_t &bi, uint64_t &bo) {   // bases of step s + 1 from step s
-        const int q = __ffsll((long long)~s) - 1 + ng;
-        if (q < P.n_outer) { bi += s_cin[q]; bo += s_cout[q]; }
-    };
-    uint64_t ibn = ib, dummy = 0;
-    // prologue: steps s0 and s0 + 1 in flight
-    issue(s0, ibn, 0);
-    if (s0 + 1 < s1) {
-        advance(s0, ibn, dummy);
-        issue(s0 + 1, ibn, 1);
+    const uint32_t c0b = c0 & 1u;
+#define TG_SLOOP(NC, WS, GEN) \
+    u8_stream_loop<NC, WS, GEN>(P, s0, s1, in, out, stage0, s_cin, s_cout, g, ng, j, keep, inf, c0b, inc, outc, ib, ob)
+    if (P.s_nres || P.s_lgen) {
+        TG_SLOOP(0, true, true);
     } else {
-        cp_async_commit();
-    }
-    int st = 0;
-    for (uint64_t s = s0; s < s1; s++) {
-        if (s + 2 < s1) {
-            advance(s + 1, ibn, dummy);
-            issue(s + 2, ibn, st == 0 ? 2 : st - 1);
-        } else {
-            cp_async_commit();
+        switch (P.s_nc + 4 * P.s_ws) {
+            case 0: TG_SLOOP(0, false, false); break;
+            case 1: TG_SLOOP(1, false, false); break;
+            case 2: TG_SLOOP(2, false, false); break;
+            case 3: TG_SLOOP(3, false, false); break;
+            case 4: TG_SLOOP(0, true, false); break;
+            case 5: TG_SLOOP(1, true, false); break;
+            case 6: TG_SLOOP(2, true, false); break;
+            default: TG_SLOOP(3, true, false); break;
         }
-        cp_async_wait_group<2>();
-        if (((s << g) | j) < ntiles) {
-            const uint8_t *src = stage0 + st * 4096;
-            if (P.s_nres || P.s_lgen) u8_stream_coset<0, true, true>(P, src, inf, keep, out + ob, outc, c0 & 1u);
-            else switch (P.s_nc + 4 * P.s_ws) {
-                case 0: u8_stream_coset<0, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 1: u8_stream_coset<1, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 2: u8_stream_coset<2, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 3: u8_stream_coset<3, false>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 4: u8_stream_coset<0, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 5: u8_stream_coset<1, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                case 6: u8_stream_coset<2, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-                default: u8_stream_coset<3, true>(P, src, inf, keep, out + ob, outc, c0 & 1u); break;
-            }
-        }
-        st = st == FS_STAGES - 1 ? 0 : st + 1;
-        if (s + 1 < s1) advance(s, dummy, ob);
     }
-    cp_async_wait_group<0>();
+#undef TG_SLOOP
 }
 
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P,
