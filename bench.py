@@ -56,7 +56,9 @@ def parse():
                     help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--tree-only", action="store_true",
                     help="run only the tree DP section (for profiling) and print its JSON")
-    ap.add_argument("--sections", default="batched,served,sparse,sparse_full,tree,witness,search",
+    ap.add_argument("--wide-bits", type=int, default=26,
+                    help="served: dense requests with tables of 2^wide_bits entries or more take the wide lane (0: none)")
+    ap.add_argument("--sections", default="search,tree,witness,sparse,sparse_full,batched,served",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
     return ap.parse_args()
 
@@ -356,11 +358,9 @@ def section_batched(args):
     for cp in cps:
         if cp is not None:
             cp.free()
-    return {"workload": "256 banded instances, widths 12-26, n = 8 w U(4,12), m = n/2, 1-12 logical rows, "
-                        "unit weights (seed 0)", "plans": len(plans), "solves_per_s": len(ps) / tb,
-            "plain_solves_per_s": len(ps) / ts, "speedup": ts / tb, "seconds": tb, "plain_seconds": ts,
-            "distances_equal": per == seq, "autotuned": tuner.report(),
-            "plain": "one instance at a time: its plans' schedules (autotuned per width) then its result"}
+    knobs = {w: "%d/%d/%d" % (r["dmax"], r["span"], r["span_sel"]) for w, r in tuner.report().items()}
+    return {"plans": len(plans), "solves_s": round(len(ps) / tb, 1), "plain_solves_s": round(len(ps) / ts, 1),
+            "speedup": round(ts / tb, 3), "equal": per == seq, "knobs_dmax_span_sel": knobs}
 
 
 def _serve_requests(seed=11):
@@ -382,39 +382,27 @@ def _serve_requests(seed=11):
     return out + sparse[si:]
 
 
-def _finish_times(reqs):
-    """Seconds from the first arrival to the last dense completion and to each sparse completion."""
-    from tropidist_gb300 import serve
-    t0 = min(r.arrival for r in reqs)
-    dense = [r.done - t0 for r in reqs if not isinstance(r, serve.SparseRequest)]
-    sparse = [round(r.done - t0, 3) for r in reqs if isinstance(r, serve.SparseRequest)]
-    slow = sorted(reqs, key=lambda r: r.arrival - r.done)[:5]
-    return {"dense_last": round(max(dense), 3), "sparse": sparse,
-            "slowest": [[r.rid, "sparse" if isinstance(r, serve.SparseRequest) else
-                         "dense w%d x%d" % (max((pl.peak_bits for pl in r.plans if pl.feasible), default=0),
-                                            len(r.plans)),
-                         round(r.arrival - t0, 3), round((r.done - r.arrival) * 1e3, 1)] for r in slow]}
-
-
 def section_served(args):
-    """Poisson request streams mixing banded instances (widths 10-28) and circuit-style sparse
-    problems (n = 2000-20000, 24 checks per round), served by the persistent-kernel request loop
-    with continuous batching, against the plain path (one request at a time), same distances."""
+    """Poisson request streams (rates 10 to 2000 req/s) of 96 banded instances (widths 10-28, 1-12
+    logical rows, seed 11) and 4 circuit-style sparse problems (n = 2000-20000, 24 checks per
+    round), served by the persistent-kernel request loop with continuous batching (dense tables in
+    an arena of 60 % of the free HBM, sparse against 20 %; requests with tables of 2^26 entries or
+    more on the wide lane), against the plain path (one request at a time); per rate p50 / p99
+    latency in ms and solves/s of both, and whether every distance is the same."""
     from tropidist_gb300 import serve
-    res = {"workload": "96 banded instances (widths 10-28, 1-12 logical rows, seed 11) + 4 circuit-style "
-                       "sparse problems (n 2000-20000, 24 checks per round), Poisson arrivals",
-           "admission": "dense tables in a persistent-kernel arena of 60 % of free HBM, sparse tables "
-                        "against 20 % (80 % in all)", "rates": {}}
-    for rate in (20, 2000):
+    res = {}
+    for rate in (10, 50, 200, 1000, 2000):
         arr = serve.poisson_arrivals(100, rate, seed=rate)
         r1, w1, peak = serve.serve_persistent(_serve_requests(), arr, budget_frac=0.8, sparse_frac=0.2,
-                                              sparse_sms=24, jobs=1 << 21, param_bytes=2 << 30, plans=4096)
+                                              sparse_sms=24, jobs=1 << 21, param_bytes=2 << 30, plans=4096,
+                                              wide_bits=args.wide_bits if args.wide_bits > 0 else None)
         r2, w2 = serve.serve_plain(_serve_requests(), arr)
-        same = [a.distance for a in r1] == [b.distance for b in r2]
         s1, s2 = serve.summarize(r1, w1), serve.summarize(r2, w2)
-        res["rates"][str(rate)] = {"served": s1, "plain": s2, "solves_ratio": s1["solves_per_s"] / s2["solves_per_s"],
-                                   "peak_plans_in_flight": peak, "distances_equal": same,
-                                   "finish_s": {"served": _finish_times(r1), "plain": _finish_times(r2)}}
+        res[str(rate)] = {"p50": round(s1["p50_ms"], 1), "p99": round(s1["p99_ms"], 1),
+                          "solves_s": round(s1["solves_per_s"], 1), "plain_p50": round(s2["p50_ms"], 1),
+                          "plain_p99": round(s2["p99_ms"], 1), "plain_solves_s": round(s2["solves_per_s"], 1),
+                          "ratio": round(s1["solves_per_s"] / s2["solves_per_s"], 3),
+                          "equal": [a.distance for a in r1] == [b.distance for b in r2]}
     return res
 
 
@@ -539,24 +527,15 @@ def section_tree(args):
     e1.record(st)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / reps
-    info = prog.device_info()
     work = pf["join_work"]
-    out = {"workload": "banded m=120 n=240 window 16 (seed 1), first logical row, balanced tree over the "
-                       "natural column order", "distance": v, "join_pairs": work,
-           "max_join_dimension": pf["max_join_dimension"], "max_interface_rank": pf["max_interface_rank"],
-           "device_arena_bytes": pf["device_arena_bytes"], "launches_per_run": info["launches"],
-           "seconds": sec, "pairs_per_s": work / sec,
-           "l2": "tables stay L2-resident (arena below the 129 MB L2)",
-           "timing": "CUDA events around 5 whole runs (target copied in, root entry read back each run)"}
+    out = {"distance": v, "pairs": work, "ms": round(sec * 1e3, 3), "pairs_s": round(work / sec)}
     if not args.no_cpu_baseline:
         from oracle import tree as ot
         t0 = time.perf_counter()
         vc = ot.run_port(prog, target)
         cpu = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": work / cpu, "unit": "pairs/s", "seconds": cpu, "cores": 1, "kind": "port",
-                               "sample": "the whole query: the reference's executor loop over a C port of "
-                                         "cdist/tree_dp.c tree_join (single-threaded, as the reference)"}
-        out["distances_equal"] = vc == v
+        out["cpu_pairs_s"] = round(work / cpu)      # the reference's executor loop over the C port, one core
+        out["equal"] = vc == v
     prog.free()
     return out
 
@@ -580,8 +559,7 @@ def section_witness(args):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     cols = r["witness"]
-    out = {"workload": "banded m=1000 n=2000 col-weight 3 window 30 (seed 0), 4 logical rows, natural order",
-           "seconds": dt, "distance": r["distance"], "weight": len(cols), "observable": r["observable"],
+    out = {"s": round(dt, 3), "distance": r["distance"],
            "verified": bool(verify_witness(p, cols, r["observable"]) and len(cols) == r["distance"] == best),
            "peak_bits": max(pl.peak_bits for _, pl in auto._plans(p, order) if pl.feasible)}
     if not args.no_cpu_baseline:
@@ -596,11 +574,9 @@ def section_witness(args):
         t0 = time.perf_counter()
         g = auto.dp_witness(q, qo, obs=0)
         torch.cuda.synchronize()
-        out["small"] = {"workload": "banded m=120 n=240 window 16 (seed 1), logical row 0",
-                        "gpu_seconds": time.perf_counter() - t0, "cpu_seconds": cpu,
-                        "weights_equal": len(w) == len(g["witness"]),
-                        "cpu": "the reference's traceback (table before every update) restated in numpy, "
-                               "one core"}
+        out["small_s"] = round(time.perf_counter() - t0, 4)
+        out["small_cpu_s"] = round(cpu, 4)            # the reference's store-every-table traceback, numpy
+        out["small_equal"] = len(w) == len(g["witness"])
     return out
 
 
@@ -623,12 +599,10 @@ def section_search(args):
         t0 = time.perf_counter()
         r = search.distance(p, k_table=2, kmax=c["distance"])
         dt = time.perf_counter() - t0
-        out[name] = {"distance": r["distance"], "known": c["distance"], "seconds": dt,
-                     "nodes": sum(sum(x["nodes"]) for x in r["runs"]), "lookups": sum(x["lookups"] for x in r["runs"]),
-                     "waves": sum(x["waves"] for x in r["runs"]), "false_hits": sum(x["false_hits"] for x in r["runs"]),
-                     "table_entries": r["table_entries"]}
+        out[name] = {"d": r["distance"], "known": c["distance"], "s": round(dt, 4),
+                     "nodes": sum(sum(x["nodes"]) for x in r["runs"])}
         if not args.no_cpu_baseline:
-            out[name]["cpu_baseline"] = _search_cpu(p, c["distance"])
+            out[name]["cpu_s"] = round(_search_cpu(p, c["distance"])["seconds"], 4)
     return out
 
 
@@ -772,14 +746,14 @@ def main():
     tr = traffic_per_launch(kname)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak_gbs,
                 "unit": "GB/s", "frac": achieved / peak_gbs if achieved else None,
-                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "peak_source": "measured hbm_gbs" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes_per_launch": bytes_fp / n_fp if n_fp else None,
                 "avg_launch_us": 1e3 * ms_fp / n_fp if n_fp else None, "launches": int(n_fp),
                 "share_of_gpu_time": ms_fp / sum(acc[1::3]) if sum(acc[1::3]) else None,
                 "traffic": (tr["ratio"] * bytes_fp / n_fp) if (tr and n_fp) else None,
                 "whole_step_gbs": (sum(acc[2::3]) / args.steps) / (ms / args.steps / 1e3) / 1e9 if ms else None,
-                "traffic_source": ("ncu DRAM bytes / algorithmic bytes = %.3f on %s, scaled to the average launch"
-                                   % (tr["ratio"], tr["source"])) if tr else None}
+                "traffic_source": ("ncu DRAM/algorithmic bytes %.3f (profiles/), scaled to the average launch"
+                                   % tr["ratio"]) if tr else None}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded banded problem)",

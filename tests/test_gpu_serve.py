@@ -96,3 +96,22 @@ def test_persistent_server_mixes_sparse_requests():
     assert got_dense == alone_dense
     assert got_sparse == alone_sparse
     assert all(getattr(r, "error", None) is None for r in done)
+
+
+def test_persistent_server_wide_lane():
+    """Wide dense requests on their own lane (plain streaming launches) beside the persistent kernel
+    and the sparse workers: every distance is the one computed alone."""
+    from tropidist_gb300 import auto, sparse_dp, synth
+    from tropidist_gb300.serve import SparseRequest, poisson_arrivals, serve_persistent
+    ps, reqs = _requests(6, 10)
+    widths = sorted(max((pl.peak_bits for pl in r.plans if pl.feasible), default=0) for r in reqs)
+    cut = widths[len(widths) // 2]                       # about half of them take the wide lane
+    sp = synth.circuit_dem(seed=40, rounds=4, checks=12, ncols=400)
+    alone_dense = [auto.dp_distance(p, list(range(p.ncols)))[0] for p in ps]
+    alone_sparse = sparse_dp.distance(sp, kmax=30, witness=False)["distance"]
+    mixed = reqs[:5] + [SparseRequest(100, sp)] + reqs[5:]
+    done, wall, peak = serve_persistent(mixed, poisson_arrivals(len(mixed), 300.0, seed=5), budget_frac=0.5,
+                                        sparse_frac=0.1, sparse_sms=16, jobs=1 << 16, param_bytes=64 << 20,
+                                        plans=512, wide_bits=cut)
+    assert [r.distance for r in done if getattr(r, "kind", None) != "sparse"] == alone_dense
+    assert [r.distance for r in done if getattr(r, "kind", None) == "sparse"] == [alone_sparse]

@@ -13,7 +13,10 @@ PersistentServer   the same interface on one long-lived persistent kernel (csrc/
                    granularity, with no kernel launches per pass.  Sparse requests (SparseRequest:
                    circuit-style problems for the sparse Rank DP) run beside it on worker threads
                    with their own streams and SMs, each worker admitting one request at a time
-                   against its share of the memory budget.
+                   against its share of the memory budget; with `wide_bits`, dense requests with
+                   a table of 2^wide_bits entries or more run on a lane of their own with the
+                   plain streaming launches (their passes are bandwidth-bound: batching them gains
+                   nothing and the persistent kernel's share of the SMs would slow them down).
 serve_plain        the same requests one at a time on one stream (the plain GPU path).
 poisson_arrivals   seeded exponential inter-arrival times.
 Latency = completion time - arrival time; p50 / p99 and solves/s are computed by `summarize`.
@@ -288,7 +291,7 @@ class PersistentServer:
     polling, and a request completes when all of its plans have."""
 
     def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192,
-                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2, sparse_planners=4):
+                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2, sparse_planners=4, wide_bits=None):
         import ctypes
         import torch
         from . import _lib
@@ -328,6 +331,16 @@ class PersistentServer:
         self.sparse_threads = [threading.Thread(target=self._sparse_loop, daemon=True) for _ in range(sparse_workers)]
         for t in self.sparse_threads:
             t.start()
+        # wide dense requests (a table of 2^wide_bits entries or more: bandwidth-bound passes) run on
+        # a lane of their own with the plain streaming launches, one request at a time, beside the
+        # persistent kernel; their tables come from the same memory budget, checked at submit
+        self.wide_bits = wide_bits
+        self.wide_q = collections.deque()
+        self.wide_wake = threading.Event()
+        self.wide_thread = None
+        if wide_bits is not None:
+            self.wide_thread = threading.Thread(target=self._wide_loop, daemon=True)
+            self.wide_thread.start()
 
     def submit(self, req, arrival=None):
         req.arrival = time.perf_counter() if arrival is None else arrival
@@ -342,9 +355,29 @@ class PersistentServer:
                     req.plan = self.planner.submit(_plan_sparse, req.problem)
                 self.sparse_q.append(req)
                 self.sparse_wake.set()
+            elif self.wide_bits is not None and req.cps is not None and \
+                    max((pl.peak_bits for pl in req.plans if pl.feasible), default=0) >= self.wide_bits:
+                self.wide_q.append(req)
+                self.wide_wake.set()
             else:
                 self.pending.append(req)
         return req
+
+    def _wide_loop(self):
+        stream = self.torch.cuda.Stream()
+        while not self.stop_flag:
+            with self.lock:
+                req = self.wide_q.popleft() if self.wide_q else None
+            if req is None:
+                self.wide_wake.wait(0.001)
+                self.wide_wake.clear()
+                continue
+            req.admitted = time.perf_counter()
+            _launch(req, stream)
+            req.event.synchronize()
+            req.done = time.perf_counter()
+            _finish(req)
+            self.finished.append(req)
 
     def _sparse_loop(self):
         stream = self.torch.cuda.Stream()
@@ -451,6 +484,9 @@ class PersistentServer:
         self.sparse_wake.set()
         for t in self.sparse_threads:
             t.join(timeout=60)
+        self.wide_wake.set()
+        if self.wide_thread is not None:
+            self.wide_thread.join(timeout=60)
         if self.handle:
             self.L.tg_server_free(self.handle)
             self.handle = None
