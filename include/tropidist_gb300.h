@@ -191,6 +191,13 @@ int tg_tab_build(void *t, int n, const uint64_t *zh, const uint64_t *zl, const u
  * R (int32[m]) -> out (int32[m]): least cost <= R[q] with the same fingerprint and another label, or -1 */
 int tg_tab_lookup_dev(void *t, uint64_t m, const void *zh, const void *zl, const void *lg, const void *R,
                       void *out, void *stream);
+/* A native probe for tg_search (no counterpart in the reference, whose DFS looks its table up in
+ * the same process, cdist/gmitm.c:138-163): create it on a device table with room for `cap`
+ * probes per round trip, pass tg_tab_probe as the probe and the handle as its context. */
+void *tg_tab_probe_create(void *table, int64_t cap, int *status);
+int tg_tab_probe(int64_t m, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, const int32_t *R,
+                 int32_t *out, void *ctx);
+void tg_tab_probe_free(void *ctx);
 /* The reference's exact names and signatures, bound by cdist/search.py:58-67 (ctypes) and
  * defined at cdist/gmitm.c:61 (tab_create), :78 (tab_free), :84 (tab_count), :176 (tab_build):
  * thin forms of the tg_tab_* functions above (tab_create returns NULL on allocation failure). */

@@ -262,10 +262,80 @@ int tg_tab_lookup_dev(void *p, uint64_t m, const void *zh, const void *zl, const
     return cuda_check(cudaGetLastError(), "table lookup");
 }
 
+// A native answer to the search's probe waves (tg_probe_fn): a wave's probes go through pinned
+// staging to the device table and back on a stream of its own, with no interpreter in the loop.
+struct NativeProbe {
+    TableHandle *T;
+    int64_t cap;                   // probes per round trip
+    uint8_t *h_in, *d_in;          // zh, zl, lg (8 bytes each) and R (4 bytes): 28 bytes per probe
+    int32_t *h_out, *d_out;
+    cudaStream_t st;
+};
+
+static void probe_release(NativeProbe *P) {
+    if (!P) return;
+    if (P->h_in) cudaFreeHost(P->h_in);
+    if (P->h_out) cudaFreeHost(P->h_out);
+    if (P->d_in) cudaFree(P->d_in);
+    if (P->d_out) cudaFree(P->d_out);
+    if (P->st) cudaStreamDestroy(P->st);
+    delete P;
+}
+
 // The reference's own names and signatures (cdist/search.py:58-67 binds them with ctypes), so a
 // binding written for cdist's libgmitm can load this library unchanged: NULL from tab_create when
 // the table cannot be allocated (the reference's binding raises MemoryError on NULL), tab_build on
 // HOST arrays zh, zl, lg of n columns.
+void *tg_tab_probe_create(void *table, int64_t cap, int *status) {
+    int st = TG_OK;
+    NativeProbe *P = nullptr;
+    if (!table || cap < 1 || cap > (1ll << 28)) {
+        st = set_error(TG_ERR_ARG, "bad table or probe capacity");
+    } else {
+        P = new NativeProbe();
+        memset(P, 0, sizeof(*P));
+        P->T = static_cast<TableHandle *>(table);
+        P->cap = cap;
+        st = cuda_check(cudaMallocHost((void **)&P->h_in, 28 * (size_t)cap), "probe staging");
+        if (!st) st = cuda_check(cudaMallocHost((void **)&P->h_out, 4 * (size_t)cap), "probe staging");
+        if (!st) st = cuda_check(cudaMalloc((void **)&P->d_in, 28 * (size_t)cap), "probe buffers");
+        if (!st) st = cuda_check(cudaMalloc((void **)&P->d_out, 4 * (size_t)cap), "probe buffers");
+        if (!st) st = cuda_check(cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking), "probe stream");
+        if (st) {
+            probe_release(P);
+            P = nullptr;
+            if (st == TG_ERR_CUDA) st = set_error(TG_ERR_NOMEM, "probe buffers");
+        }
+    }
+    if (status) *status = st;
+    return P;
+}
+
+int tg_tab_probe(int64_t m, const uint64_t *zh, const uint64_t *zl, const uint64_t *lg, const int32_t *R,
+                 int32_t *out, void *ctx) {
+    NativeProbe *P = static_cast<NativeProbe *>(ctx);
+    if (!P || m < 0 || (m && (!zh || !zl || !lg || !R || !out))) return 1;
+    for (int64_t off = 0; off < m; off += P->cap) {
+        const int64_t n = m - off < P->cap ? m - off : P->cap;
+        memcpy(P->h_in, zh + off, 8 * (size_t)n);
+        memcpy(P->h_in + 8 * n, zl + off, 8 * (size_t)n);
+        memcpy(P->h_in + 16 * n, lg + off, 8 * (size_t)n);
+        memcpy(P->h_in + 24 * n, R + off, 4 * (size_t)n);
+        if (cudaMemcpyAsync(P->d_in, P->h_in, 28 * (size_t)n, cudaMemcpyHostToDevice, P->st) != cudaSuccess) return 1;
+        k_tb_lookup<<<tb_grid(n), 256, 0, P->st>>>(*P->T, n, (const unsigned long long *)P->d_in,
+                                                   (const unsigned long long *)(P->d_in + 8 * n),
+                                                   (const unsigned long long *)(P->d_in + 16 * n),
+                                                   (const int *)(P->d_in + 24 * n), P->d_out);
+        if (cudaGetLastError() != cudaSuccess) return 1;
+        if (cudaMemcpyAsync(P->h_out, P->d_out, 4 * (size_t)n, cudaMemcpyDeviceToHost, P->st) != cudaSuccess) return 1;
+        if (cudaStreamSynchronize(P->st) != cudaSuccess) return 1;
+        memcpy(out + off, P->h_out, 4 * (size_t)n);
+    }
+    return 0;
+}
+
+void tg_tab_probe_free(void *ctx) { probe_release(static_cast<NativeProbe *>(ctx)); }
+
 void *tab_create(int log2slots, int wide) {
     int status = 0;
     return tg_tab_create(log2slots, wide, &status);

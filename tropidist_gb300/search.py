@@ -231,9 +231,19 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
         except Exception:                 # reported to the search, which stops with an error
             return 1
 
-    cb = probe_fn if probe_fn is not None else PROBE_FN(answer)
-    ctx = probe_ctx if probe_fn is not None else None
     L = _lib.lib()
+    native = None
+    if probe_fn is not None:
+        cb, ctx = probe_fn, probe_ctx
+    elif probe is None:
+        # the device table answers each wave natively (pinned staging, no interpreter in the loop)
+        st = ctypes.c_int(0)
+        native = L.tg_tab_probe_create(table.handle, max(1, int(wave)), ctypes.byref(st))
+        if not native:
+            _lib.check(st.value)
+        cb, ctx = PROBE_FN(("tg_tab_probe", L)), native
+    else:
+        cb, ctx = PROBE_FN(answer), None
     stats = np.zeros(8, dtype=np.int64)
     sol = np.zeros(64, dtype=np.int32)
     nsol = np.zeros(1, dtype=np.int32)
@@ -274,6 +284,8 @@ def distance(p: Problem, k_table=2, kmax=20, relaxed=None, rank=None, anchors=No
                 break
             out["lower_bound"] = K + 1
     finally:
+        if native:
+            L.tg_tab_probe_free(native)
         if table is not None:
             table.free()
     return out
