@@ -58,7 +58,7 @@ def parse():
                     help="only run the circuit-style sparse query at this threshold (profiling aid)")
     ap.add_argument("--tree-only", action="store_true",
                     help="run only the tree DP section (for profiling) and print its JSON")
-    ap.add_argument("--wide-bits", type=int, default=26,
+    ap.add_argument("--wide-bits", type=int, default=24,
                     help="served: dense requests with tables of 2^wide_bits entries or more take the wide lane (0: none)")
     ap.add_argument("--sections", default="search,tree,witness,sparse,sparse_full,batched,served",
                     help="secondary workloads reported beside the headline (comma list, empty for none)")
@@ -388,8 +388,8 @@ def section_served(args):
     """Poisson request streams (rates 10 to 2000 req/s) of 96 banded instances (widths 10-28, 1-12
     logical rows, seed 11) and 4 circuit-style sparse problems (n = 2000-20000, 24 checks per
     round), served by the persistent-kernel request loop with continuous batching (dense tables in
-    an arena of 60 % of the free HBM, sparse against 20 %; requests with tables of 2^26 entries or
-    more on the wide lane), against the plain path (one request at a time); per rate p50 / p99
+    an arena of 60 % of the free HBM, sparse against 20 %; requests with tables of 2^24 entries or
+    more on two wide lanes), against the plain path (one request at a time); per rate p50 / p99
     latency in ms and solves/s of both, and whether every distance is the same."""
     from tropidist_gb300 import serve
     res = {}
@@ -397,7 +397,8 @@ def section_served(args):
         arr = serve.poisson_arrivals(100, rate, seed=rate)
         r1, w1, peak = serve.serve_persistent(_serve_requests(), arr, budget_frac=0.8, sparse_frac=0.2,
                                               sparse_sms=24, jobs=1 << 21, param_bytes=2 << 30, plans=4096,
-                                              wide_bits=args.wide_bits if args.wide_bits > 0 else None)
+                                              wide_bits=args.wide_bits if args.wide_bits > 0 else None,
+                                              wide_workers=2)
         r2, w2 = serve.serve_plain(_serve_requests(), arr)
         s1, s2 = serve.summarize(r1, w1), serve.summarize(r2, w2)
         res[str(rate)] = {"p50": round(s1["p50_ms"], 1), "p99": round(s1["p99_ms"], 1),

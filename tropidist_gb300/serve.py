@@ -291,7 +291,8 @@ class PersistentServer:
     polling, and a request completes when all of its plans have."""
 
     def __init__(self, arena_bytes=None, budget_frac=0.8, jobs=1 << 20, param_bytes=1 << 30, plans=8192,
-                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2, sparse_planners=4, wide_bits=None):
+                 sparse_frac=0.0, sparse_sms=0, sparse_workers=2, sparse_planners=4, wide_bits=None,
+                 wide_workers=1):
         import ctypes
         import torch
         from . import _lib
@@ -337,10 +338,11 @@ class PersistentServer:
         self.wide_bits = wide_bits
         self.wide_q = collections.deque()
         self.wide_wake = threading.Event()
-        self.wide_thread = None
+        self.wide_threads = []
         if wide_bits is not None:
-            self.wide_thread = threading.Thread(target=self._wide_loop, daemon=True)
-            self.wide_thread.start()
+            self.wide_threads = [threading.Thread(target=self._wide_loop, daemon=True) for _ in range(wide_workers)]
+            for t in self.wide_threads:
+                t.start()
 
     def submit(self, req, arrival=None):
         req.arrival = time.perf_counter() if arrival is None else arrival
@@ -485,8 +487,8 @@ class PersistentServer:
         for t in self.sparse_threads:
             t.join(timeout=60)
         self.wide_wake.set()
-        if self.wide_thread is not None:
-            self.wide_thread.join(timeout=60)
+        for t in self.wide_threads:
+            t.join(timeout=60)
         if self.handle:
             self.L.tg_server_free(self.handle)
             self.handle = None
