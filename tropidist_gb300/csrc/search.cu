@@ -99,6 +99,12 @@ struct Search {
                 if (m == 0) return true;              // no free column reaches this row
                 sum += 1.0 / m;
                 if (sum + left * inv_wmax > lim) return true;
+                if (cover < 2) {
+                    // first dual only: once even weight 1 on every remaining row cannot pass the
+                    // budget, this node is not pruned (the rows left need not be scanned)
+                    if (sum + left <= lim) return false;
+                    continue;
+                }
                 cv_rows.push_back(r);
                 cv_y.push_back(1.0 / m);
             }
@@ -248,6 +254,8 @@ struct Search {
             add_probe(hz[d], lz[d], g[d], R, node_here(d), -1);
             return;
         }
+        // the covering bound on nodes beyond the table's reach (R > kt here) with more unsatisfied
+        // rows than budget, the gate of cdist/gmitm.c:610 at its default factor
         if (cover && pc > R && cover_prune(s, R, pc)) {
             cover_pruned++;
             return;
