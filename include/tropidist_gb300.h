@@ -179,6 +179,25 @@ int tg_spw_join(int W, const void *fkeys, const void *fvals, uint64_t nf, uint64
 int tg_spw_lookup(int W, const void *H, int lg, const void *keys, uint64_t stride, const void *q, uint64_t m,
                   void *out, void *stream);
 
+/* A leg of column steps on wide states in one call, with the table sizes kept on the device and
+ * one host read at the end (the multi-word counterpart of tg_sp_walk; the per-step rule of
+ * cdist/sparse_dp.py:338-403).  steps HOST int64 [nsteps][13] = cap, keep_below, w, trunc (< 0:
+ * none), keep (0, 1, 2: tables of at most 1024 states), join, ncls, use_h, extra, join table's keys
+ * (DEVICE pointer), its index (DEVICE pointer), index bits, key stride; words HOST uint64
+ * [nsteps][5][W] = upd, sel_mask, sel_bits, the bound's tmask, the join's tmask; masks HOST uint64
+ * [nsteps][maxc][W], weights HOST int64 [nsteps][maxc].  scratch: tg_spw_walk_scratch_bytes(W,
+ * cap, nsteps) DEVICE bytes, tables of at most cap states.  Kept tables go to the DEVICE arena: at
+ * offset o, keys [W][s], vals [s] at o + 8 W s, index [2^lg] at o + 8 W s + round_up(s, 256).
+ * out HOST int64 [nsteps][6] = states, changed states, kept offset (-1: not kept), kept stride s,
+ * index bits, states before the cut's truncation; res HOST uint64 [nsteps][2 + W] = least join
+ * total (all ones: none), forward value, forward key words.  Returns nsteps, or 0 with need[0]
+ * (states per table) or need[1] (arena bytes) set: run the leg again with more room. */
+int64_t tg_spw_walk_scratch_bytes(int W, uint64_t cap, int nsteps);
+int tg_spw_walk(int W, int nsteps, const int64_t *steps, const uint64_t *words, const uint64_t *masks,
+                const int64_t *weights, int maxc, int K, const void *keys0, const void *vals0, uint64_t n0,
+                uint64_t stride0, void *scratch, uint64_t cap, void *arena, uint64_t arena_bytes, int64_t *out,
+                uint64_t *res, int64_t *need, void *stream);
+
 /* ---------------------------------------------------------------- completion tables (search)
  * Same entry points as the reference's ctypes binding (cdist/search.py:58-67): */
 void *tg_tab_create(int log2slots, int wide, int *status);   /* cdist/gmitm.c:61 tab_create (NULL, *status -3: no memory) */

@@ -106,3 +106,38 @@ def test_wide_queries_and_distance():
         d = sparse_dp.distance(p, order=list(range(p.ncols)), kmax=12)
         d1 = sparse_dp.distance(first, order=list(range(first.ncols)), kmax=12)
         assert d["distance"] == d1["distance"]
+
+
+def test_wide_walk_grows_its_tables_and_arena():
+    """Device walks started with tables and an arena far too small run their legs again with more
+    room: the same counts, peaks and kept tables as the oracle's step-by-step sweep."""
+    from tropidist_gb300 import sparse_dp
+    from tropidist_gb300.sparse_tables import WideGpuTables
+    p, _ = interleaved(8, 4)
+    tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+    for direction in (+1, -1):
+        be = WideGpuTables(tr)
+        be._walk_cap, be._arena_guess = 1, 1
+        sw = sparse_dp.Sweep(tr, direction, 5, 5, every=3, backend=be)
+        sw.run()
+        assert be._walk_cap > 2
+        ref = sparse_dp.Sweep(tr, direction, 5, 5, every=3, backend=WideTables(tr))
+        ref.run(on_cut=lambda *a: False)
+        assert sw.counts == ref.counts and sw.peak == ref.peak
+        for c, t in sw.ckpt.items():
+            assert _tables(be, t) == _tables(ref.be, ref.ckpt[c]), (direction, c)
+
+
+def test_wide_meet_by_walks_equals_step_by_step():
+    """The meet in the middle run as device walks (joins inside the walk, frontier truncation)
+    gives the value, cut and witness weight of the step-by-step meet on the oracle tables."""
+    from tropidist_gb300 import sparse_dp
+    for copies, seed in ((8, 6), (9, 7)):
+        p, _ = interleaved(copies, seed)
+        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+        for K in (3, 5):
+            got = sparse_dp.query(tr, K, mode="mitm")
+            want = sparse_dp.query(tr, K, mode="mitm", backend=WideTables(tr))
+            assert got["value"] == want["value"] and got["peak_states"] == want["peak_states"], (copies, K)
+            if got["value"] is not None:
+                check_witness(p, got["witness"], got["value"], 0)

@@ -47,7 +47,6 @@ struct WideBound {
 struct WideStep {
     uint64_t upd[SPW_MAXW], sel_mask[SPW_MAXW], sel_bits[SPW_MAXW];
     int cap, keep_below, w, want_changed;
-    int sel_any;                // sel_mask != 0
 };
 
 // SplitMix64 finalizer (Steele, Lea, Flood 2014) over the words, each mixed with its position
@@ -150,10 +149,21 @@ __global__ void k_spw_fill(unsigned long long *H, uint64_t n) {
         H[i] = SPW_EMPTY;
 }
 
+// n_dev (or null): the table's size on the device, clamped to n (its capacity)
+__device__ __forceinline__ uint64_t spw_count(const unsigned long long *n_dev, uint64_t n) {
+    if (!n_dev) return n;
+    const uint64_t d = *n_dev;
+    return d < n ? d : n;
+}
+
 template <int W>
 __global__ void k_spw_emit(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t n,
                            uint64_t stride, uint64_t *ek, uint8_t *ev, uint64_t estride, unsigned long long *H, int lg,
-                           const WideStep P, const WideBound B, unsigned long long *counters) {
+                           const WideStep P, const WideBound B, unsigned long long *counters,
+                           const unsigned long long *n_dev = nullptr, const unsigned long long *lg_dev = nullptr,
+                           const unsigned long long *abort = nullptr) {
+    n = (abort && *abort) ? 0 : spw_count(n_dev, n);
+    if (lg_dev) lg = (int)*lg_dev;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t k[W];
         spw_load<W>(keys, stride, i, k);
@@ -191,7 +201,13 @@ __global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t
                               uint64_t estride, uint64_t *nk, uint8_t *nv, uint64_t ncap, unsigned long long *H2,
                               int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap, const unsigned long long *Hold,
                               int lg_old, const uint64_t *okeys, uint64_t ostride, const WideStep P,
-                              unsigned long long *counters) {
+                              unsigned long long *counters, const unsigned long long *lg_dev = nullptr,
+                              const unsigned long long *lg_old_dev = nullptr) {
+    if (lg_dev) {
+        lg2 = (int)*lg_dev;
+        hcap = 1ull << lg2;
+    }
+    if (lg_old_dev) lg_old = (int)*lg_old_dev;
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < hcap; s += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long cur = H[s];
         if (cur == SPW_EMPTY) continue;
@@ -234,11 +250,12 @@ __global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t
     }
 }
 
-// a table's states with value < below, with their own index
+// a table's states with value < below (all when below < 0) into (nk, nv) with their own index
 template <int W>
-__global__ void k_spw_filter(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t n,
-                             uint64_t stride, int below, uint64_t *nk, uint8_t *nv, uint64_t ncap,
-                             unsigned long long *H2, int lg2, unsigned long long *counters) {
+__device__ __forceinline__ void spw_filter_body(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals,
+                                                uint64_t n, uint64_t stride, int below, uint64_t *nk, uint8_t *nv,
+                                                uint64_t ncap, unsigned long long *H2, int lg2,
+                                                unsigned long long *counters) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t v = vals[i];
         if (below >= 0 && (int)v >= below) continue;
@@ -260,13 +277,25 @@ __global__ void k_spw_filter(const uint64_t *__restrict__ keys, const uint8_t *_
     }
 }
 
+template <int W>
+__global__ void k_spw_filter(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t n,
+                             uint64_t stride, int below, uint64_t *nk, uint8_t *nv, uint64_t ncap,
+                             unsigned long long *H2, int lg2, unsigned long long *counters,
+                             const unsigned long long *n_dev = nullptr, const unsigned long long *lg_dev = nullptr) {
+    n = spw_count(n_dev, n);
+    if (lg_dev) lg2 = (int)*lg_dev;
+    spw_filter_body<W>(keys, vals, n, stride, below, nk, nv, ncap, H2, lg2, counters);
+}
+
 // least f.value + b.value over changed f and backward b with key(b) = key(f) ^ tmask:
 // result = min(total << 40 | f)
 template <int W>
 __global__ void k_spw_join(const uint64_t *__restrict__ fk, const uint8_t *__restrict__ fv, uint64_t nf,
                            uint64_t fstride, const unsigned long long *__restrict__ Hb, int lgb,
                            const uint64_t *__restrict__ bk, uint64_t bstride, const WideBound T,
-                           unsigned long long *result) {
+                           unsigned long long *result, const unsigned long long *n_dev = nullptr,
+                           uint64_t tag = 0) {
+    nf = spw_count(n_dev, nf);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nf; i += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t q[W];
         spw_load<W>(fk, fstride, i, q);
@@ -274,7 +303,7 @@ __global__ void k_spw_join(const uint64_t *__restrict__ fk, const uint8_t *__res
         for (int w = 0; w < W; w++) q[w] ^= T.tmask[w];
         const uint32_t bv = spw_lookup<W>(Hb, lgb, bk, bstride, q);
         if (bv == 255u) continue;
-        atomicMin(result, ((unsigned long long)(fv[i] + bv) << 40) | i);
+        atomicMin(result, ((unsigned long long)(fv[i] + bv) << 40) | tag | i);
     }
 }
 
@@ -286,6 +315,97 @@ __global__ void k_spw_lookup(const unsigned long long *__restrict__ H, int lg, c
         spw_load<W>(q, m, i, k);
         out[i] = (uint8_t)spw_lookup<W>(H, lg, keys, stride, k);
     }
+}
+
+// ---- kernels of a walk: the table sizes and index widths stay on the device between steps
+#define SPW_TAG (1ull << 39)          // join result from a whole table (not the changed list)
+#define SPW_KEEP_SMALL 1024           // keep mode 2: only tables of at most this many states
+
+__device__ __forceinline__ int spw_lg_dev(uint64_t n) {         // index bits for n states at load <= 1/2
+    int lg = 6;
+    while ((1ull << lg) < 2 * n) lg++;
+    return lg;
+}
+
+// fill the index (or two) of 2^lg slots, lg = index bits for mult * n states; *lg_out = lg.  Once a
+// step has raised a flag (prev: its counter block) the walk is void: *abort is set and the later
+// steps run on empty tables (the host runs the leg again with more room).
+__global__ void k_spw_fill_dyn(const unsigned long long *n_dev, uint64_t ncap, int mult, unsigned long long *lg_out,
+                               unsigned long long *H1, unsigned long long *H2, const unsigned long long *prev,
+                               unsigned long long *abort) {
+    const bool bad = *abort || (prev && ((prev[2] | prev[6]) & 7ull));
+    if (bad && blockIdx.x == 0 && threadIdx.x == 0) *abort = 1;
+    const int lg = spw_lg_dev(bad ? 0 : (uint64_t)mult * spw_count(n_dev, ncap));
+    if (blockIdx.x == 0 && threadIdx.x == 0) *lg_out = (unsigned long long)lg;
+    const uint64_t m = 1ull << lg;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        H1[i] = SPW_EMPTY;
+        if (H2) H2[i] = SPW_EMPTY;
+    }
+}
+
+// place of a kept table in the arena: rec = [n, offset, flags, lg, stride, -, -, -]; flags 8: no
+// room (used still grows by the bytes it needed), 16: not kept (keep mode 2 and a large table)
+__device__ __forceinline__ uint64_t spw_keep_bytes(int W, uint64_t stride, int lg) {
+    return ((uint64_t)W * stride * 8 + (stride + 255) / 256 * 256 + (8ull << lg) + 255) / 256 * 256;
+}
+
+__global__ void k_spw_keep_alloc(const unsigned long long *n_dev, uint64_t ncap, int W, int mode,
+                                 unsigned long long *rec, unsigned long long *used, uint64_t arena_bytes) {
+    if (threadIdx.x || blockIdx.x) return;
+    const uint64_t n = spw_count(n_dev, ncap);
+    if (mode == 2 && n > SPW_KEEP_SMALL) {
+        rec[2] = 16;
+        return;
+    }
+    const uint64_t stride = n < 1 ? 1 : n;
+    const int lg = spw_lg_dev(n);
+    const uint64_t b = spw_keep_bytes(W, stride, lg), off = *used;
+    *used = off + b;
+    rec[3] = (unsigned long long)lg;
+    rec[4] = stride;
+    if (off + b > arena_bytes) {
+        rec[2] = 8;
+        return;
+    }
+    rec[1] = off;
+}
+
+__device__ __forceinline__ unsigned long long *spw_keep_index(uint8_t *arena, const unsigned long long *rec, int W) {
+    const uint64_t stride = rec[4];
+    return reinterpret_cast<unsigned long long *>(arena + rec[1] + (uint64_t)W * stride * 8 + (stride + 255) / 256 * 256);
+}
+
+__global__ void k_spw_keep_fill(uint8_t *arena, const unsigned long long *rec, int W) {
+    if (rec[2] & 24ull) return;
+    unsigned long long *H = spw_keep_index(arena, rec, W);
+    const uint64_t m = 1ull << rec[3];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+        H[i] = SPW_EMPTY;
+}
+
+template <int W>
+__global__ void k_spw_keep(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t stride,
+                           const unsigned long long *n_dev, uint8_t *arena, unsigned long long *rec) {
+    if (rec[2] & 24ull) return;
+    const uint64_t n = spw_count(n_dev, stride), ks = rec[4];
+    uint64_t *nk = reinterpret_cast<uint64_t *>(arena + rec[1]);
+    uint8_t *nv = arena + rec[1] + (uint64_t)W * ks * 8;
+    spw_filter_body<W>(keys, vals, n, stride, -1, nk, nv, ks, spw_keep_index(arena, rec, W), (int)rec[3], rec);
+}
+
+// the forward state (key words and value) behind a step's join result, for the host
+template <int W>
+__global__ void k_spw_capture(const unsigned long long *result, const uint64_t *ck, const uint8_t *cv,
+                              const uint64_t *tk, const uint8_t *tv, uint64_t stride, uint64_t *resk, uint8_t *resv) {
+    const unsigned long long r = *result;
+    if (threadIdx.x || blockIdx.x || r == SPW_EMPTY) return;
+    const uint64_t i = r & (SPW_TAG - 1);
+    const uint64_t *k = (r & SPW_TAG) ? tk : ck;
+    const uint8_t *v = (r & SPW_TAG) ? tv : cv;
+#pragma unroll
+    for (int w = 0; w < W; w++) resk[w] = k[(uint64_t)w * stride + i];
+    *resv = v[i];
 }
 
 static unsigned spw_grid(uint64_t n) {
@@ -331,6 +451,161 @@ static int spw_step_w(const uint64_t *keys, const uint8_t *vals, uint64_t n, uin
                                                             (const unsigned long long *)Hold, lg_old, keys, stride, P,
                                                             C);
     return cuda_check(cudaGetLastError(), "wide step");
+}
+
+// ---- a leg of column steps in one call (no host read between steps)
+// Per step, int64 fields (SPW_WALK_FIELDS): cap, keep_below, w, trunc (< 0: none), keep (0, 1, 2:
+// small tables only), join (a backward table to join), ncls, use_h, extra, join keys, join index,
+// join index bits, join key stride; uint64 words [5][W]: upd, sel_mask, sel_bits, the bound's
+// tmask, the join's tmask.
+#define SPW_WALK_FIELDS 13
+enum { WK_CAP, WK_KB, WK_W, WK_TRUNC, WK_KEEP, WK_JOIN, WK_NCLS, WK_USEH, WK_EXTRA, WK_JKEYS, WK_JH, WK_JLG, WK_JSTRIDE };
+
+struct SpwRing {
+    uint64_t *keys;
+    uint8_t *vals;
+    unsigned long long *H;
+};
+
+static int spw_walk_lg(uint64_t n) {
+    int lg = 6;
+    while ((1ull << lg) < 2 * n) lg++;
+    return lg;
+}
+
+// scratch: 3 ring tables and the changed list of cap states, a staging area of 2 cap, indexes of
+// 2^lg(2 cap) slots; then 8 counters per step (+2) and per step a keep record; join results
+static uint64_t spw_walk_layout(int W, uint64_t cap, int nsteps, uint8_t *base, SpwRing *ring, SpwRing *stage,
+                                SpwRing *chg, unsigned long long **cnt, unsigned long long **res, uint64_t **resk,
+                                uint8_t **resv) {
+    const uint64_t ib = 8ull << spw_walk_lg(2 * cap);
+    auto rnd = [](uint64_t x) { return (x + 255) / 256 * 256; };
+    uint64_t off = 0;
+    auto take = [&](uint64_t b) {
+        uint8_t *p = base ? base + off : nullptr;
+        off += rnd(b);
+        return p;
+    };
+    for (int r = 0; r < 3; r++) {
+        SpwRing t;
+        t.keys = reinterpret_cast<uint64_t *>(take((uint64_t)W * cap * 8));
+        t.vals = take(cap);
+        t.H = reinterpret_cast<unsigned long long *>(take(ib));
+        if (ring) ring[r] = t;
+    }
+    SpwRing sg;
+    sg.keys = reinterpret_cast<uint64_t *>(take((uint64_t)W * 2 * cap * 8));
+    sg.vals = take(2 * cap);
+    sg.H = reinterpret_cast<unsigned long long *>(take(ib));
+    SpwRing ch;
+    ch.keys = reinterpret_cast<uint64_t *>(take((uint64_t)W * cap * 8));
+    ch.vals = take(cap);
+    ch.H = nullptr;
+    unsigned long long *c = reinterpret_cast<unsigned long long *>(take(64ull * (2 * (uint64_t)nsteps + 2)));
+    unsigned long long *r = reinterpret_cast<unsigned long long *>(take(8ull * nsteps + 8));
+    uint64_t *rk = reinterpret_cast<uint64_t *>(take(8ull * W * nsteps + 8));
+    uint8_t *rv = take((uint64_t)nsteps + 1);
+    if (stage) *stage = sg;
+    if (chg) *chg = ch;
+    if (cnt) *cnt = c;
+    if (res) *res = r;
+    if (resk) *resk = rk;
+    if (resv) *resv = rv;
+    return off;
+}
+
+template <int W>
+static int spw_walk_w(int nsteps, const int64_t *steps, const uint64_t *words, const uint64_t *masks,
+                      const int64_t *weights, int maxc, int K, const uint64_t *k0, const uint8_t *v0, uint64_t n0,
+                      uint64_t stride0, uint8_t *scratch, uint64_t cap, uint8_t *arena, uint64_t arena_bytes,
+                      cudaStream_t st) {
+    SpwRing ring[3], sg, ch;
+    unsigned long long *cnt, *res;
+    uint64_t *resk;
+    uint8_t *resv;
+    spw_walk_layout(W, cap, nsteps, scratch, ring, &sg, &ch, &cnt, &res, &resk, &resv);
+    // counters: block 0 the start table, block i + 1 step i ([0] states, [1] changed, [2] flags,
+    // [3] index bits, [4] states after the cut's truncation, [5] its index bits, [6] its flags),
+    // block nsteps + 1 + i the keep record of step i, block 2 nsteps + 1 [0] the arena bytes used
+    const size_t cbytes = 64ull * (2 * (uint64_t)nsteps + 2);
+    int e = cuda_check(cudaMemsetAsync(cnt, 0, cbytes, st), "walk counters");
+    if (!e && nsteps) e = cuda_check(cudaMemsetAsync(res, 0xFF, 8ull * nsteps, st), "walk results");
+    if (e) return e;
+    unsigned long long *used = cnt + 8ull * (2 * (uint64_t)nsteps + 1), *abort = used + 1;
+    const unsigned gc = spw_grid(cap), gi = spw_grid(1ull << spw_walk_lg(2 * cap));
+    // the start table into ring slot 0
+    k_spw_fill_dyn<<<gi, 256, 0, st>>>(nullptr, n0, 1, cnt + 3, ring[0].H, nullptr, nullptr, abort);
+    if (n0)
+        k_spw_filter<W><<<spw_grid(n0), 256, 0, st>>>(k0, v0, n0, stride0, -1, ring[0].keys, ring[0].vals, cap,
+                                                      ring[0].H, 0, cnt, nullptr, cnt + 3);
+    int cur = 0;
+    const unsigned long long *ncur = cnt, *lgcur = cnt + 3, *cprev = cnt;
+    for (int i = 0; i < nsteps; i++) {
+        const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
+        const uint64_t *wd = words + (size_t)5 * W * i;
+        if (f[WK_CAP] > 254 || f[WK_W] < 1 || f[WK_W] > 254) return set_error(TG_ERR_ARG, "values beyond 8 bits");
+        WideStep P;
+        memset(&P, 0, sizeof(P));
+        for (int q = 0; q < W; q++) {
+            P.upd[q] = wd[q];
+            P.sel_mask[q] = wd[W + q];
+            P.sel_bits[q] = wd[2 * W + q];
+        }
+        P.cap = (int)f[WK_CAP];
+        P.keep_below = (int)f[WK_KB];
+        P.w = (int)f[WK_W];
+        const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[WK_JH]);
+        const uint64_t *jk = reinterpret_cast<const uint64_t *>((uintptr_t)f[WK_JKEYS]);
+        const bool join = f[WK_JOIN] && jH && jk;
+        P.want_changed = join;
+        WideBound B, T;
+        e = spw_bound(B, W, (int)f[WK_USEH], K, (int)f[WK_NCLS], masks + (size_t)i * maxc * W,
+                      weights + (size_t)i * maxc, f[WK_EXTRA], wd + 3 * W);
+        if (e) return e;
+        memset(&T, 0, sizeof(T));
+        for (int q = 0; q < W; q++) T.tmask[q] = wd[4 * W + q];
+        unsigned long long *c = cnt + 8ull * (i + 1);
+        const int out = (cur + 1) % 3;
+        // staging and new index for 2 n states, then the two kernels of the step
+        k_spw_fill_dyn<<<gi, 256, 0, st>>>(ncur, cap, 2, c + 3, sg.H, ring[out].H, cprev, abort);
+        k_spw_emit<W><<<gc, 256, 0, st>>>(ring[cur].keys, ring[cur].vals, cap, cap, sg.keys, sg.vals, 2 * cap, sg.H, 0,
+                                          P, B, c, ncur, c + 3, abort);
+        k_spw_compact<W><<<gi, 256, 0, st>>>(sg.H, 0, sg.keys, 2 * cap, ring[out].keys, ring[out].vals, cap,
+                                             ring[out].H, 0, ch.keys, ch.vals, cap, ring[cur].H, 0, ring[cur].keys,
+                                             cap, P, c, c + 3, lgcur);
+        if (join)
+            k_spw_join<W><<<gc, 256, 0, st>>>(ch.keys, ch.vals, cap, cap, jH, (int)f[WK_JLG], jk,
+                                              (uint64_t)f[WK_JSTRIDE], T, res + i, c + 1, 0);
+        int now = out;
+        const unsigned long long *nnow = c, *lgnow = c + 3;
+        if (f[WK_TRUNC] >= 0) {
+            // the cap drops at this cut: the whole table before the drop is joined too
+            if (join)
+                k_spw_join<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, jH, (int)f[WK_JLG], jk,
+                                                  (uint64_t)f[WK_JSTRIDE], T, res + i, c, SPW_TAG);
+            const int tr = (out + 1) % 3;
+            k_spw_fill_dyn<<<gi, 256, 0, st>>>(c, cap, 1, c + 5, ring[tr].H, nullptr, nullptr, abort);
+            k_spw_filter<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, (int)f[WK_TRUNC],
+                                                ring[tr].keys, ring[tr].vals, cap, ring[tr].H, 0, c + 4, c, c + 5);
+            now = tr;
+            nnow = c + 4;
+            lgnow = c + 5;
+        }
+        if (join)
+            k_spw_capture<W><<<1, 32, 0, st>>>(res + i, ch.keys, ch.vals, ring[out].keys, ring[out].vals, cap,
+                                               resk + (size_t)i * W, resv + i);
+        if (f[WK_KEEP]) {
+            unsigned long long *rec = cnt + 8ull * (nsteps + 1 + i);
+            k_spw_keep_alloc<<<1, 32, 0, st>>>(nnow, cap, W, (int)f[WK_KEEP], rec, used, arena ? arena_bytes : 0);
+            k_spw_keep_fill<<<gi, 256, 0, st>>>(arena, rec, W);
+            k_spw_keep<W><<<gc, 256, 0, st>>>(ring[now].keys, ring[now].vals, cap, nnow, arena, rec);
+        }
+        cur = now;
+        ncur = nnow;
+        lgcur = lgnow;
+        cprev = c;
+    }
+    return cuda_check(cudaGetLastError(), "wide walk");
 }
 
 }  // namespace tg
@@ -385,6 +660,103 @@ int tg_spw_step(int W, const void *keys, const void *vals, uint64_t n, uint64_t 
                    (uint64_t *)ckeys, (uint8_t *)cvals, ccap, P, B, counters, st)
     SPW_DISPATCH(W, SPW_STEP)
 #undef SPW_STEP
+}
+
+int64_t tg_spw_walk_scratch_bytes(int W, uint64_t cap, int nsteps) {
+    if (spw_check_words(W) || cap < 1 || nsteps < 0) return -1;
+    return (int64_t)spw_walk_layout(W, cap, nsteps, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                    nullptr);
+}
+
+// Run nsteps column steps from the table (keys0, vals0, n0 states, key stride stride0) on the device
+// with one host read at the end.  Returns nsteps when done: out int64 [nsteps][6] = states after
+// the step (and the cut's truncation), changed states, kept table's arena offset (-1: not kept),
+// its key stride, its index bits (the working index's when not kept), states before the
+// truncation; res uint64 [nsteps][2 + W] = least join total (all ones: none), the forward value,
+// the forward key words.  Returns 0 with need[0] (states a table must hold) or need[1] (arena
+// bytes) set when the tables or the arena were too small: the caller runs the leg again.
+int tg_spw_walk(int W, int nsteps, const int64_t *steps, const uint64_t *words, const uint64_t *masks,
+                const int64_t *weights, int maxc, int K, const void *keys0, const void *vals0, uint64_t n0,
+                uint64_t stride0, void *scratch, uint64_t cap, void *arena, uint64_t arena_bytes, int64_t *out,
+                uint64_t *res, int64_t *need, void *stream) {
+    int e = spw_check_words(W);
+    if (e) return e;
+    if (nsteps < 0 || (nsteps && (!steps || !words || !out || !res)) || !scratch || !need || cap < 1 ||
+        (n0 && (!keys0 || !vals0 || stride0 < n0)) || maxc < 1 || 2 * cap >= SPW_TAG)
+        return set_error(TG_ERR_ARG, "bad wide walk arguments");
+    need[0] = need[1] = 0;
+    if (n0 > cap) {
+        need[0] = (int64_t)n0;
+        return 0;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint8_t *base = static_cast<uint8_t *>(scratch);
+#define SPW_WALK(WW)                                                                                                  \
+    spw_walk_w<WW>(nsteps, steps, words, masks, weights, maxc, K, (const uint64_t *)keys0, (const uint8_t *)vals0, n0, \
+                   stride0, base, cap, (uint8_t *)arena, arena_bytes, st)
+    auto run = [&]() -> int { SPW_DISPATCH(W, SPW_WALK) };
+#undef SPW_WALK
+    e = run();
+    if (e) return e;
+    unsigned long long *cnt, *resd;
+    uint64_t *resk;
+    uint8_t *resv;
+    spw_walk_layout(W, cap, nsteps, base, nullptr, nullptr, nullptr, &cnt, &resd, &resk, &resv);
+    const size_t bytes = (size_t)((resv + nsteps + 1) - reinterpret_cast<uint8_t *>(cnt));
+    static thread_local uint8_t *hb = nullptr;
+    static thread_local size_t hb_bytes = 0;
+    if (hb_bytes < bytes) {
+        if (hb) cudaFreeHost(hb);
+        hb = nullptr;
+        hb_bytes = 0;
+        if (cudaMallocHost(&hb, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(TG_ERR_NOMEM, "pinned walk buffer");
+        }
+        hb_bytes = bytes;
+    }
+    e = cuda_check(cudaMemcpyAsync(hb, cnt, bytes, cudaMemcpyDeviceToHost, st), "walk read");
+    if (!e) e = cuda_check(cudaStreamSynchronize(st), "walk sync");
+    if (e) return e;
+    const unsigned long long *hc = reinterpret_cast<const unsigned long long *>(hb);
+    const uint8_t *hr = hb + (reinterpret_cast<uint8_t *>(resd) - reinterpret_cast<uint8_t *>(cnt));
+    const unsigned long long *hres = reinterpret_cast<const unsigned long long *>(hr);
+    const uint64_t *hk = reinterpret_cast<const uint64_t *>(hb + (reinterpret_cast<uint8_t *>(resk) -
+                                                                  reinterpret_cast<uint8_t *>(cnt)));
+    const uint8_t *hv = hb + (resv - reinterpret_cast<uint8_t *>(cnt));
+    uint64_t most = hc[0];
+    bool small = (hc[2] & 7ull) != 0, room = false;
+    for (int i = 0; i < nsteps; i++) {
+        const unsigned long long *c = hc + 8ull * (i + 1), *rec = hc + 8ull * (nsteps + 1 + i);
+        most = std::max<uint64_t>(most, std::max<uint64_t>(c[0], std::max<uint64_t>(c[1], c[4])));
+        small = small || ((c[2] | c[6] | rec[2]) & 7ull);
+        room = room || (rec[2] & 8ull);
+    }
+    if (small) {
+        need[0] = (int64_t)std::max<uint64_t>(2 * cap, most + 1);
+        return 0;
+    }
+    if (room) {
+        need[1] = (int64_t)hc[8ull * (2 * (uint64_t)nsteps + 1)];
+        return 0;
+    }
+    for (int i = 0; i < nsteps; i++) {
+        const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
+        const unsigned long long *c = hc + 8ull * (i + 1), *rec = hc + 8ull * (nsteps + 1 + i);
+        const bool tr = f[WK_TRUNC] >= 0, kept = f[WK_KEEP] && !(rec[2] & 16ull);
+        int64_t *o = out + 6 * (size_t)i;
+        o[0] = (int64_t)(tr ? c[4] : c[0]);
+        o[1] = (int64_t)c[1];
+        o[2] = kept ? (int64_t)rec[1] : -1;
+        o[3] = kept ? (int64_t)rec[4] : (int64_t)cap;
+        o[4] = kept ? (int64_t)rec[3] : (int64_t)(tr ? c[5] : c[3]);
+        o[5] = (int64_t)c[0];
+        uint64_t *r = res + (size_t)(2 + W) * i;
+        r[0] = hres[i] == SPW_EMPTY ? SPW_EMPTY : hres[i] >> 40;
+        r[1] = hv[i];
+        for (int q = 0; q < W; q++) r[2 + q] = hk[(size_t)i * W + q];
+    }
+    return nsteps;
 }
 
 int tg_spw_filter(int W, const void *keys, const void *vals, uint64_t n, uint64_t stride, int below, void *nkeys,

@@ -38,8 +38,8 @@ import time
 import numpy as np
 
 from . import _lib, trellis
-from .sparse_tables import (INF, KEYMASK, MAX_SLOTS, MAX_WIDE_SLOTS, BudgetExceeded, GpuTables, WideGpuTables,
-                            _Changed)
+from .sparse_tables import (INF, KEYMASK, M64, MAX_SLOTS, MAX_WIDE_SLOTS, BudgetExceeded, GpuTables,
+                            WideGpuTables, _Changed, pad_words, words_of)
 
 MAX_WEIGHT = INF - 1
 Q = 720720                      # lcm(1..16): lookahead weights are multiples of 1/Q (rounded down)
@@ -360,6 +360,7 @@ class Sweep:
         self.use_h, self.frontier = use_h, frontier
         self.be = _backend(backend, tr)
         self.on_device = isinstance(self.be, GpuTables)
+        self.legs = self.on_device or isinstance(self.be, WideGpuTables)    # steps run as device walks
         self.hd = tr.bound_arrays(direction > 0) if use_h else None
         self.every = every or max(1, int(math.isqrt(tr.N)))
         self.max_states, self.deadline = max_states, deadline
@@ -445,7 +446,7 @@ class Sweep:
     def run(self, on_cut=None):
         """The whole sweep, keeping checkpoints and per-cut counts; on_cut(cut, table, changed,
         extra) may return True to stop.  Returns the last cut reached."""
-        if on_cut is None and self.on_device:
+        if on_cut is None and self.legs:
             return self._device_legs()[0]
         c, tab = self._begin()
         if on_cut and on_cut(c, tab, _as_changed(self.be, tab), None):
@@ -461,7 +462,7 @@ class Sweep:
         """The forward (frontier) sweep of a meet in the middle against the finished backward sweep
         `back`: the least (total, cut, forward state, forward value, backward state) over every
         cut's joins, or None; it stops early once a total <= lower is found."""
-        if self.on_device and back.on_device:
+        if self.legs and back.legs:
             return self._device_meet(back, lower)
         tr = self.tr
         best = [None]
@@ -488,7 +489,7 @@ class Sweep:
                 join(c, extra if not isinstance(self.be, GpuTables) else _Changed(extra.arr, extra.n))
         return best[0]
 
-    # ------------------------------------------------------------------ device legs (GpuTables)
+    # ------------------------------------------------------------------ device legs (walks)
     def _device_meet(self, back, lower):
         store = _TablesAt(back)
         _, b = self._device_legs(join_with=store, lower=lower)
@@ -496,7 +497,7 @@ class Sweep:
         if b is None:
             return None
         total, c, fkey = b
-        bkey = fkey ^ (int(self.tr.tmask[c]) & KEYMASK)
+        bkey = fkey ^ (int(self.tr.tmask[c]) & KEYMASK if self.on_device else int(self.tr.tmask[c]))
         bval = back.be.lookup(store.at(c), bkey)
         return total, c, fkey, total - bval, bkey
 
@@ -522,41 +523,49 @@ class Sweep:
             keep = [1 if self.is_ckpt(x) else small for x in cuts]
             keep[-1] = 1
             joins = None if join_with is None else [(join_with.at(x), self.tr.tmask[x]) for x in cuts]
-            rows, masks, weights = self._rows(pos, keep, joins)
-            out, kept, res = self.be.walk(tab, rows, masks, weights, self.K, self.max_states,
+            out, kept, res = self.be.walk(tab, *self._rows(pos, keep, joins), self.K, self.max_states,
                                           want_res=join_with is not None)
             self.steps_done += len(pos)
             for x, a, b in zip(cuts, out[:, 0].tolist(), out[:, 1].tolist()):
                 self.counts[x], self.changed_counts[x] = a, b
-            self.peak = max(self.peak, int(out[:, [0, 1, 5]].max()))
+            self.peak = max(self.peak, int(out[:, [0, 1]].max()))
             if join_with is not None:
-                hit = np.nonzero(res != U64(0xFFFFFFFFFFFFFFFF))[0]
-                if len(hit):
-                    k = int(hit[np.argmin(res[hit] >> U64(56))])      # the first least total
-                    total = int(res[k]) >> 56
-                    if best is None or total < best[0]:
-                        best = (total, cuts[k], int(res[k]) & KEYMASK)
+                r = self._walk_best(res)
+                if r is not None and (best is None or r[1] < best[0]):
+                    best = (r[1], cuts[r[0]], r[2])
             for k, t in kept.items():
                 if keep[k] == 1 and k != len(pos) - 1:
                     self.ckpt[cuts[k]] = t
                     self._held_bytes += self.be.nbytes(t)
                 elif keep[k] == 2:
                     self.small_tabs[cuts[k]] = t
-                    self.small_bytes += 8 * (t.n + (1 << t.lg)) + 256
+                    self.small_bytes += self.be.nbytes(t) + 8 * (1 << t.lg) + 256
             tab = kept[len(pos) - 1]
             c = c1
             self.ckpt[c] = tab
             self._held_bytes += self.be.nbytes(tab)
-            self.peak_bytes = max(self.peak_bytes, self._held_bytes + 8 * int(out[:, 5].max()))
+            self.peak_bytes = max(self.peak_bytes, self._held_bytes + self.be.state_bytes * int(out[:, 5].max()))
             if self.max_states is not None and self.peak > self.max_states:
                 raise BudgetExceeded("%d states before cut %d" % (self.peak, c), "states")
             if self.deadline is not None and time.monotonic() > self.deadline:
                 raise BudgetExceeded("deadline at cut %d" % c, "deadline")
         return c, best
 
+    def _walk_best(self, res):
+        """The first least join total of a walk: (step, total, forward key) or None."""
+        if not self.on_device:
+            return self.be.walk_best(res)
+        hit = np.nonzero(res != U64(0xFFFFFFFFFFFFFFFF))[0]
+        if not len(hit):
+            return None
+        k = int(hit[np.argmin(res[hit] >> U64(56))])
+        return k, int(res[k]) >> 56, int(res[k]) & KEYMASK
+
     def _rows(self, positions, keep, joins=None):
         """Spec rows of tg_sp_walk for the steps at `positions` (as _step), with lookahead arrays;
         keep: per step 0/1; joins: per step None or (backward table, tmask)."""
+        if not self.on_device:
+            return self._wide_rows(positions, keep, joins)
         if getattr(self, "_all", None) is None:
             self._all = self._all_rows()
         rows0, masks0, weights0 = self._all
@@ -605,6 +614,64 @@ class Sweep:
             return rows, np.ascontiguousarray(masks[cut]), np.ascontiguousarray(wts[cut])
         return rows, np.zeros((N, 1), dtype=U64), np.zeros((N, 1), dtype=np.int64)
 
+    def _wide_rows(self, positions, keep, joins=None):
+        """Step records of tg_spw_walk (multi-word states) for the steps at `positions`:
+        (steps int64 [m, 13], words uint64 [m, 5, W], lookahead masks, weights)."""
+        if getattr(self, "_all", None) is None:
+            self._all = self._all_wide()
+        steps0, words0, masks0, weights0 = self._all
+        pos = np.asarray(positions, dtype=np.int64)
+        steps, words = steps0[pos].copy(), words0[pos].copy()
+        steps[:, 4] = np.asarray(keep, dtype=np.int64)
+        if joins is not None:
+            W = self.be.W
+            for k, j in enumerate(joins):
+                if j is None:
+                    continue
+                t, tmask = j
+                steps[k, 5] = 1
+                steps[k, 9], steps[k, 10] = t.keys.data_ptr(), t.H.data_ptr()
+                steps[k, 11], steps[k, 12] = t.lg, t.stride
+                words[k, 4] = words_of(tmask, W)
+        return steps, words, masks0[pos], weights0[pos]
+
+    def _all_wide(self):
+        """Step records of every step position of this sweep for tg_spw_walk (without keep / join)."""
+        tr, fwd, W = self.tr, self.direction > 0, self.be.W
+        N = tr.N
+        steps = np.zeros((max(1, N), 13), dtype=np.int64)
+        words = np.zeros((max(1, N), 5, W), dtype=U64)
+        if N == 0:
+            return steps, words, np.zeros((1, 1, W), dtype=U64), np.zeros((1, 1), dtype=np.int64)
+        p = np.arange(N)
+        cut = p + 1 if fwd else p
+        caps = np.asarray(self.caps, dtype=np.int64)
+        cap = caps[cut].copy()
+        kb = np.full(N, -1, dtype=np.int64)
+        trunc = np.full(N, -1, dtype=np.int64)
+        if self.frontier:
+            cap = caps[p].copy()
+            kb = cap.copy()
+            drop = caps[cut] < cap
+            trunc[drop] = caps[cut][drop]
+        steps[:, 0], steps[:, 1], steps[:, 3] = cap, kb, trunc
+        steps[:, 2] = np.asarray(tr.cw, dtype=np.int64)
+
+        def wv(xs):
+            xs = [int(x) for x in xs]
+            return np.array([[(x >> (64 * i)) & M64 for i in range(W)] for x in xs], dtype=U64).reshape(len(xs), W)
+        sm, sb = (tr.fsel_mask, tr.fsel_bits) if fwd else (tr.bsel_mask, tr.bsel_bits)
+        words[:, 0], words[:, 1], words[:, 2] = wv(tr.col), wv(sm), wv(sb)
+        words[:, 3] = words[:, 4] = wv(tr.tmask)[cut]
+        if self.use_h:
+            ncls, masks, wts, extra = tr.bound_raw(fwd)
+            masks = np.asarray(masks, dtype=U64)
+            if masks.ndim == 2:
+                masks = masks[:, :, None]
+            steps[:, 6], steps[:, 7], steps[:, 8] = ncls[cut], 1, extra[cut]
+            return steps, words, pad_words(masks[cut], W), np.ascontiguousarray(wts[cut])
+        return steps, words, np.zeros((N, 1, W), dtype=U64), np.zeros((N, 1), dtype=np.int64)
+
     # ------------------------------------------------------------------ recomputed tables
     def tables(self, lo, hi):
         """The tables at the cuts lo..hi (lo <= hi), recomputed from the checkpoint before them in
@@ -619,10 +686,9 @@ class Sweep:
         pos = self._positions(c0, stop)
         if not pos:
             return out
-        if self.on_device:
+        if self.legs:
             keep = [1 if lo <= self._cut_of(p) <= hi else 0 for p in pos]
-            rows, masks, weights = self._rows(pos, keep)
-            _, kept, _ = self.be.walk(tab, rows, masks, weights, self.K, self.max_states, want_res=False)
+            _, kept, _ = self.be.walk(tab, *self._rows(pos, keep), self.K, self.max_states, want_res=False)
             for k, p in enumerate(pos):
                 if keep[k]:
                     out[self._cut_of(p)] = kept[k]

@@ -122,6 +122,8 @@ class GpuTables:
         arr = self.torch.zeros(1, dtype=self.torch.int64, device="cuda")
         return self._build(arr, 1)
 
+    state_bytes = 8
+
     @staticmethod
     def size(tab):
         return tab.n
@@ -287,6 +289,16 @@ def words_of(x, W):
     return np.array([(x >> (64 * i)) & M64 for i in range(W)], dtype=U64)
 
 
+def pad_words(a, W):
+    """uint64 [..., w] word rows (w <= W) as [..., W], the higher words zero (contiguous)."""
+    a = np.asarray(a, dtype=U64)
+    if a.shape[-1] == W:
+        return np.ascontiguousarray(a)
+    out = np.zeros(a.shape[:-1] + (W,), dtype=U64)
+    out[..., :a.shape[-1]] = a
+    return out
+
+
 def ints_of(words):
     """uint64 [n, W] rows as Python ints."""
     words = np.asarray(words, dtype=U64)
@@ -364,6 +376,10 @@ class WideGpuTables:
     def size(tab):
         return tab.n
 
+    @property
+    def state_bytes(self):
+        return 8 * self.W + 1
+
     def nbytes(self, tab):
         return (8 * self.W + 1) * tab.n
 
@@ -435,8 +451,8 @@ class WideGpuTables:
         if hd is None:
             ncls, mp, wp, extra, use_h = 0, None, None, 0, 0
         else:
-            m_arr = np.ascontiguousarray(np.asarray(hd[0], dtype=U64).reshape(len(hd[1]), W) if len(hd[1])
-                                         else np.zeros((1, W), dtype=U64))
+            m_arr = pad_words(np.asarray(hd[0], dtype=U64).reshape(len(hd[1]), -1), W) if len(hd[1]) \
+                else np.zeros((1, W), dtype=U64)
             w_arr = np.ascontiguousarray(hd[1], dtype=np.int64) if len(hd[1]) else np.zeros(1, dtype=np.int64)
             ncls, mp, wp, extra, use_h = len(hd[1]), m_arr.ctypes.data, w_arr.ctypes.data, int(hd[2]), 1
         uw, sm, sb, tw = self._w(upd), self._w(sel_mask), self._w(sel_bits), self._w(tmask)
@@ -452,6 +468,69 @@ class WideGpuTables:
         new = _WTab(nk, nv, c[0], ncap, Hn, lgn)
         changed = _WTab(ck, cv, c[1], ccap, None, 0) if want_changed else None
         return new, changed
+
+    def walk(self, tab, steps, words, masks, weights, K, max_states=None, want_res=True):
+        """Run the column steps (int64 [m, 13] step records and uint64 [m, 5, W] words,
+        csrc/sparse_wide.cu tg_spw_walk) from `tab` in one call, the table sizes kept on the device:
+        (out int64 [m, 6], {step: kept table}, join results uint64 [m, 2 + W] or None)."""
+        torch, L, W = self.torch, self.L, self.W
+        m = len(steps)
+        steps = np.ascontiguousarray(steps, dtype=np.int64)
+        words = np.ascontiguousarray(words, dtype=U64)
+        masks = np.ascontiguousarray(masks, dtype=U64)
+        weights = np.ascontiguousarray(weights, dtype=np.int64)
+        maxc = weights.shape[1] if weights.ndim == 2 else 1
+        cap = max(getattr(self, "_walk_cap", 1 << 12), 2 * tab.n)
+        arena_bytes = max(getattr(self, "_arena_guess", 1 << 20), 1 << 16)
+        out = np.zeros((max(1, m), 6), dtype=np.int64)
+        res = np.zeros((max(1, m), 2 + W), dtype=U64)
+        need = np.zeros(2, dtype=np.int64)
+        while True:
+            if max_states is not None and cap > 4 * max(max_states, 1) + 4 * tab.n:
+                raise BudgetExceeded("a walk needs tables of %d states" % (cap // 2), "states")
+            sb = int(L.tg_spw_walk_scratch_bytes(W, cap, m))
+            if sb < 0:
+                raise ValueError("bad wide walk size")
+            if getattr(self, "_scratch", None) is None or self._scratch.numel() * 8 < sb:
+                self._scratch = None
+                self._scratch = torch.empty((sb + 7) // 8, dtype=torch.int64, device="cuda")
+            arena = None
+            arena = torch.empty((arena_bytes + 7) // 8, dtype=torch.int64, device="cuda")
+            r = L.tg_spw_walk(W, m, steps.ctypes.data, words.ctypes.data, masks.ctypes.data, weights.ctypes.data,
+                              maxc, int(K), tab.keys.data_ptr() if tab.n else None,
+                              tab.vals.data_ptr() if tab.n else None, tab.n, tab.stride, self._scratch.data_ptr(),
+                              cap, arena.data_ptr(), arena_bytes, out.ctypes.data, res.ctypes.data,
+                              need.ctypes.data, device.stream_ptr())
+            if r < 0:
+                _lib.check(r)
+            if r == m:
+                break
+            if need[0]:
+                cap = max(2 * cap, int(need[0]))
+            if need[1]:
+                arena_bytes = max(arena_bytes + (arena_bytes >> 1), int(need[1]) + (1 << 20))
+        self._walk_cap = cap
+        kept, used = {}, 0
+        u8 = arena.view(torch.uint8)
+        for i in np.nonzero(out[:m, 2] >= 0)[0].tolist():
+            n, o, st, lg = (int(x) for x in out[i, [0, 2, 3, 4]])
+            vo = o + 8 * W * st
+            ho = vo + (st + 255) // 256 * 256
+            kept[i] = _WTab(arena[o // 8:o // 8 + W * st], u8[vo:vo + st], n, st, arena[ho // 8:ho // 8 + (1 << lg)],
+                            lg)
+            used = max(used, ho + (8 << lg))
+        self._arena_guess = max(1 << 16, used + (used >> 2))
+        return out[:m], kept, (res[:m] if want_res else None)
+
+    @staticmethod
+    def walk_best(res):
+        """The first least join total of a walk's results: (step, total, forward key) or None."""
+        tot = res[:, 0]
+        hit = np.nonzero(tot != U64(M64))[0]
+        if not len(hit):
+            return None
+        k = int(hit[np.argmin(tot[hit])])
+        return k, int(tot[k]), ints_of(res[k:k + 1, 2:])[0]
 
     def join(self, ch, btab, tmask):
         """(total, forward key, forward value, backward key) of the least f.value + b.value over
