@@ -113,6 +113,7 @@ __global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_con
                           unsigned long long *Hnew, unsigned long long *changed, uint64_t changed_cap,
                           unsigned long long *counters) {
     const uint64_t clr = ~P.sel_mask & SP_KEYMASK;
+    unsigned long long inserted = 0;      // new keys, added to counters[0] once at the end
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long x = A[i];
         const uint64_t key = x & SP_KEYMASK;
@@ -122,7 +123,7 @@ __global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_con
             const uint64_t k2 = key & clr;
             if ((int)v <= P.cap && sp_keep(B, k2, v)) {
                 const int r = sp_insert_min(Hnew, P.lg_new, k2, v);
-                if (r > 0) atomicAdd(counters + 0, 1ull);
+                if (r > 0) inserted++;
                 else if (r < 0) atomicOr(counters + 2, 1ull);
             }
         }
@@ -136,28 +137,30 @@ __global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_con
                     const uint32_t vo = sp_lookup(Hold, P.lg_old, t);
                     const bool hit = vo != 255u;
                     if (vc < vo && P.want_changed) {
-                        const unsigned long long slot = atomicAdd(counters + 1, 1ull);
+                        const unsigned long long slot = agg_inc(counters + 1);
                         if (slot < changed_cap) changed[slot] = t2 | ((unsigned long long)vc << 56);
                         else atomicOr(counters + 2, 2ull);
                     }
                     if (hit || P.keep_below < 0 || (int)vc < P.keep_below) {
                         const int r = sp_insert_min(Hnew, P.lg_new, t2, vc);
-                        if (r > 0) atomicAdd(counters + 0, 1ull);
+                        if (r > 0) inserted++;
                         else if (r < 0) atomicOr(counters + 2, 1ull);
                     }
                 }
             }
         }
     }
+    agg_add(counters + 0, inserted);
 }
 
 // the occupied slots of an index into an array; counters[3] = states written
 __global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t cap, unsigned long long *out,
                              uint64_t out_cap, unsigned long long *counters) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cap; i += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long x = H[i];
+    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < cap; t0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t0 + threadIdx.x;
+        const unsigned long long x = i < cap ? H[i] : SP_EMPTY;
+        const unsigned long long s = block_claim(counters + 3, x != SP_EMPTY);
         if (x != SP_EMPTY) {
-            const unsigned long long s = atomicAdd(counters + 3, 1ull);
             if (s < out_cap) out[s] = x;
             else atomicOr(counters + 2, 4ull);
         }
@@ -168,12 +171,17 @@ __global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t 
 // from the copy written to `kept` when below >= 0)
 __global__ void k_sp_build(const unsigned long long *__restrict__ A, uint64_t n, unsigned long long *H, int lg,
                            int below, unsigned long long *kept, unsigned long long *counters) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long x = A[i];
-        if (below >= 0 && (int)(x >> 56) >= below) continue;
+    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < n; t0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t0 + threadIdx.x;
+        const unsigned long long x = i < n ? A[i] : SP_EMPTY;
+        const bool want = i < n && !(below >= 0 && (int)(x >> 56) >= below);
+        if (kept) {
+            const unsigned long long j = block_claim(counters + 3, want);
+            if (want) kept[j] = x;
+        }
+        if (!want) continue;
         const int r = sp_insert_min(H, lg, x & SP_KEYMASK, (uint32_t)(x >> 56));
         if (r < 0) atomicOr(counters + 2, 1ull);
-        if (kept) kept[atomicAdd(counters + 3, 1ull)] = x;
     }
 }
 

@@ -208,21 +208,30 @@ __global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t
         hcap = 1ull << lg2;
     }
     if (lg_old_dev) lg_old = (int)*lg_old_dev;
-    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < hcap; s += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long cur = H[s];
-        if (cur == SPW_EMPTY) continue;
+    // tiles of blockDim slots (the trip count is the same for every thread of a block: output
+    // positions are claimed once per block and tile)
+    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < hcap; t0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = t0 + threadIdx.x;
+        const unsigned long long cur = s < hcap ? H[s] : SPW_EMPTY;
+        const bool occ = cur != SPW_EMPTY;
         const uint64_t e = cur & SPW_IDX;
         const uint32_t v = (uint32_t)(cur >> 56);
         uint64_t k[W];
-        spw_load<W>(ek, estride, e, k);
-        if (P.want_changed && (e & 1ull)) {
+#pragma unroll
+        for (int w = 0; w < W; w++) k[w] = 0;
+        if (occ) spw_load<W>(ek, estride, e, k);
+        bool chg = false;
+        if (occ && P.want_changed && (e & 1ull)) {
             // a candidate won: changed unless the old table had this key (closing bits restored)
             // with a value <= v
             uint64_t o[W];
 #pragma unroll
             for (int w = 0; w < W; w++) o[w] = k[w] | P.sel_bits[w];
-            if (v < spw_lookup<W>(Hold, lg_old, okeys, ostride, o)) {
-                const unsigned long long j = atomicAdd(counters + 1, 1ull);
+            chg = v < spw_lookup<W>(Hold, lg_old, okeys, ostride, o);
+        }
+        if (P.want_changed) {
+            const unsigned long long j = block_claim(counters + 1, chg);
+            if (chg) {
                 if (j < ccap) {
 #pragma unroll
                     for (int w = 0; w < W; w++) ck[(uint64_t)w * ccap + j] = k[w];
@@ -232,8 +241,9 @@ __global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t
                 }
             }
         }
-        if (P.keep_below >= 0 && (int)v >= P.keep_below) continue;
-        const unsigned long long j = atomicAdd(counters, 1ull);
+        const bool keep = occ && !(P.keep_below >= 0 && (int)v >= P.keep_below);
+        const unsigned long long j = block_claim(counters, keep);
+        if (!keep) continue;
         if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
 #pragma unroll
         for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
@@ -256,13 +266,15 @@ __device__ __forceinline__ void spw_filter_body(const uint64_t *__restrict__ key
                                                 uint64_t n, uint64_t stride, int below, uint64_t *nk, uint8_t *nv,
                                                 uint64_t ncap, unsigned long long *H2, int lg2,
                                                 unsigned long long *counters) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = vals[i];
-        if (below >= 0 && (int)v >= below) continue;
+    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < n; t0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t0 + threadIdx.x;
+        const uint32_t v = i < n ? vals[i] : 255u;
+        const bool want = i < n && !(below >= 0 && (int)v >= below);
+        const unsigned long long j = block_claim(counters, want);
+        if (!want) continue;
+        if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
         uint64_t k[W];
         spw_load<W>(keys, stride, i, k);
-        const unsigned long long j = atomicAdd(counters, 1ull);
-        if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
 #pragma unroll
         for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
         nv[j] = (uint8_t)v;

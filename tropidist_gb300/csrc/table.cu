@@ -80,7 +80,7 @@ __global__ void k_tb_build(TableHandle T, int s, uint64_t nsub, int n, const uns
                     unsigned long long prev = atomicCAS(T.keys + i, 0ull, (unsigned long long)key);
                     if (prev == 0ull) {
                         T.cost[i] = (uint8_t)s;
-                        atomicAdd(T.count, 1ull);
+                        agg_inc(T.count);
                         done = true;
                         break;
                     }
@@ -99,7 +99,7 @@ __global__ void k_tb_build(TableHandle T, int s, uint64_t nsub, int n, const uns
                     unsigned __int128 prev = atomicCAS(slot, (unsigned __int128)0, want);
                     if (prev == 0) {
                         T.cost[i] = (uint8_t)s;
-                        atomicAdd(T.count, 1ull);
+                        agg_inc(T.count);
                         done = true;
                         break;
                     }

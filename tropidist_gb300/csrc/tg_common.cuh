@@ -7,6 +7,7 @@
 // add-then-min instructions, which need no saturation step at all.
 #pragma once
 #include <cstdint>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #define TG_INF8 255u
@@ -65,6 +66,54 @@ __device__ __forceinline__ uint32_t minplus_u16x2(uint32_t a, uint32_t b, uint32
 __device__ __forceinline__ uint32_t xor_bytes(uint32_t v, uint32_t x) {
     const uint32_t sel = (0u ^ x) | ((1u ^ x) << 4) | ((2u ^ x) << 8) | ((3u ^ x) << 12);
     return __byte_perm(v, 0u, sel);
+}
+
+// A counter increment shared by the lanes that reach it together: one atomic per group of
+// converged lanes (same-address atomics from every lane serialise in one L2 slice).  Returns this
+// lane's value of the counter before the increment.
+__device__ __forceinline__ unsigned long long agg_inc(unsigned long long *ctr) {
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(ctr, (unsigned long long)g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+
+// Output slots for the threads of a block that want one, with one atomic per block and call.  Every
+// thread of the block must make the call, the same number of times (want may be false); blockDim.x
+// a multiple of 32, at most 1024.  Returns this thread's slot (meaningless when !want).
+__device__ __forceinline__ unsigned long long block_claim(unsigned long long *ctr, bool want) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned long long s_base;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        const unsigned nw = blockDim.x >> 5;
+        for (unsigned i = 0; i < nw; i++) {
+            const unsigned c = s_warp[i];
+            s_warp[i] = tot;
+            tot += c;
+        }
+        s_base = tot ? atomicAdd(ctr, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long j = s_base + s_warp[warp] + __popc(bal & ((1u << lane) - 1u));
+    __syncthreads();
+    return j;
+}
+
+// Add every thread's count to a counter, one atomic per group of converged lanes (at kernel end).
+__device__ __forceinline__ void agg_add(unsigned long long *ctr, unsigned long long x) {
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group g = cg::coalesced_threads();
+    for (unsigned off = 1; off < g.size(); off <<= 1) {
+        const unsigned long long y = g.shfl_down(x, off);
+        if (g.thread_rank() + off < g.size()) x += y;
+    }
+    if (g.thread_rank() == 0 && x) atomicAdd(ctr, x);
 }
 
 // 16-byte chunk as 4 words
