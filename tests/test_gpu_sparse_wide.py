@@ -115,12 +115,14 @@ def test_wide_walk_grows_its_tables_and_arena():
     from tropidist_gb300.sparse_tables import WideGpuTables
     p, _ = interleaved(8, 4)
     tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
-    for direction in (+1, -1):
+    # capacity 1: every leg runs again; 64: the one-block walk hands over to the separate launches
+    # and back many times
+    for direction, cap0 in ((+1, 1), (-1, 1), (+1, 64), (-1, 64)):
         be = WideGpuTables(tr)
-        be._walk_cap, be._arena_guess = 1, 1
+        be._walk_cap, be._arena_guess = cap0, 1
         sw = sparse_dp.Sweep(tr, direction, 5, 5, every=3, backend=be)
         sw.run()
-        assert be._walk_cap > 2
+        assert be._walk_cap >= 64
         ref = sparse_dp.Sweep(tr, direction, 5, 5, every=3, backend=WideTables(tr))
         ref.run(on_cut=lambda *a: False)
         assert sw.counts == ref.counts and sw.peak == ref.peak

@@ -82,14 +82,6 @@ __device__ __forceinline__ bool spw_equal_cg(const uint64_t *keys, uint64_t stri
     return eq;
 }
 
-template <int W>
-__device__ __forceinline__ bool spw_equal(const uint64_t *keys, uint64_t stride, uint64_t i, const uint64_t (&k)[W]) {
-    bool eq = true;
-#pragma unroll
-    for (int w = 0; w < W; w++) eq = eq && keys[(uint64_t)w * stride + i] == k[w];
-    return eq;
-}
-
 // ceil((extra + sum_c w_c * |(key ^ tmask) & mask_c|) / QW)   (cdist/sparse_dp.py:208-217)
 template <int W>
 __device__ __forceinline__ bool spw_keep(const WideBound &b, const uint64_t (&k)[W], uint32_t v) {
@@ -112,29 +104,44 @@ __device__ __forceinline__ uint32_t spw_lookup(const unsigned long long *H, int 
     const uint32_t mask = (1u << lg) - 1u;
     uint32_t s = spw_slot<W>(k, lg);
     for (uint32_t probe = 0; probe <= mask; probe++) {
-        const unsigned long long cur = H[s];
+        const unsigned long long cur = __ldcg(H + s);
         if (cur == SPW_EMPTY) return 255u;
-        if (spw_equal<W>(keys, stride, cur & SPW_IDX, k)) return (uint32_t)(cur >> 56);
+        if (spw_equal_cg<W>(keys, stride, cur & SPW_IDX, k)) return (uint32_t)(cur >> 56);
         s = (s + 1) & mask;
     }
     return 255u;
 }
 
-// staging: write the key, then insert value << 56 | e keeping the least word per key
-template <int W>
+// The threads that share a range: the whole grid (separate launches per phase) or one block (a
+// walk of small tables in one launch).  Element loops step by `step` from `first`; tile loops (block
+// collectives inside) step by `tstep` from `tile0` and add threadIdx.x.
+struct Lanes {
+    uint64_t first, step, tile0, tstep;
+};
+__device__ __forceinline__ Lanes grid_lanes() {
+    const uint64_t nt = (uint64_t)gridDim.x * blockDim.x, b0 = (uint64_t)blockIdx.x * blockDim.x;
+    return Lanes{b0 + threadIdx.x, nt, b0, nt};
+}
+__device__ __forceinline__ Lanes block_lanes() { return Lanes{threadIdx.x, blockDim.x, 0, blockDim.x}; }
+
+// staging: write the key, then insert value << 56 | e keeping the least word per key (BLK: all
+// writers and readers are threads of one block)
+template <int W, bool BLK>
 __device__ __forceinline__ void spw_emit(uint64_t *ek, uint64_t estride, uint8_t *ev, unsigned long long *H, int lg,
                                          uint64_t e, const uint64_t (&k)[W], uint32_t v, unsigned long long *err) {
 #pragma unroll
     for (int w = 0; w < W; w++) __stcg(ek + (uint64_t)w * estride + e, k[w]);
     ev[e] = (uint8_t)v;
-    __threadfence();
+    if (BLK) __threadfence_block();
+    else __threadfence();
     const unsigned long long word = ((unsigned long long)v << 56) | e;
     const uint32_t mask = (1u << lg) - 1u;
     uint32_t s = spw_slot<W>(k, lg);
     for (uint32_t probe = 0; probe <= mask; probe++) {
         unsigned long long cur = atomicCAS(H + s, SPW_EMPTY, word);
         if (cur == SPW_EMPTY) return;
-        __threadfence();
+        if (BLK) __threadfence_block();
+        else __threadfence();
         if (spw_equal_cg<W>(ek, estride, cur & SPW_IDX, k)) {
             atomicMin(H + s, word);
             return;
@@ -144,27 +151,27 @@ __device__ __forceinline__ void spw_emit(uint64_t *ek, uint64_t estride, uint8_t
     atomicOr(err, 1ull);
 }
 
-__global__ void k_spw_fill(unsigned long long *H, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        H[i] = SPW_EMPTY;
+__device__ __forceinline__ void spw_fill_body(const Lanes &L, unsigned long long *H, uint64_t m) {
+    for (uint64_t i = L.first; i < m; i += L.step) H[i] = SPW_EMPTY;
 }
+
+__global__ void k_spw_fill(unsigned long long *H, uint64_t n) { spw_fill_body(grid_lanes(), H, n); }
 
 // n_dev (or null): the table's size on the device, clamped to n (its capacity)
 __device__ __forceinline__ uint64_t spw_count(const unsigned long long *n_dev, uint64_t n) {
     if (!n_dev) return n;
-    const uint64_t d = *n_dev;
+    const uint64_t d = __ldcg(n_dev);
     return d < n ? d : n;
 }
 
-template <int W>
-__global__ void k_spw_emit(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t n,
-                           uint64_t stride, uint64_t *ek, uint8_t *ev, uint64_t estride, unsigned long long *H, int lg,
-                           const WideStep P, const WideBound B, unsigned long long *counters,
-                           const unsigned long long *n_dev = nullptr, const unsigned long long *lg_dev = nullptr,
-                           const unsigned long long *abort = nullptr) {
-    n = (abort && *abort) ? 0 : spw_count(n_dev, n);
-    if (lg_dev) lg = (int)*lg_dev;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+// every old state and its candidate through the column into the staging index
+template <int W, bool BLK>
+__device__ __forceinline__ void spw_emit_body(const Lanes &L, const uint64_t *__restrict__ keys,
+                                              const uint8_t *__restrict__ vals, uint64_t n, uint64_t stride,
+                                              uint64_t *ek, uint8_t *ev, uint64_t estride, unsigned long long *H,
+                                              int lg, const WideStep &P, const WideBound &B,
+                                              unsigned long long *counters) {
+    for (uint64_t i = L.first; i < n; i += L.step) {
         uint64_t k[W];
         spw_load<W>(keys, stride, i, k);
         const uint32_t v = vals[i];
@@ -176,7 +183,8 @@ __global__ void k_spw_emit(const uint64_t *__restrict__ keys, const uint8_t *__r
             uint64_t c[W];
 #pragma unroll
             for (int w = 0; w < W; w++) c[w] = k[w] & ~P.sel_mask[w];
-            if ((int)v <= P.cap && spw_keep<W>(B, c, v)) spw_emit<W>(ek, estride, ev, H, lg, 2 * i, c, v, counters + 2);
+            if ((int)v <= P.cap && spw_keep<W>(B, c, v))
+                spw_emit<W, BLK>(ek, estride, ev, H, lg, 2 * i, c, v, counters + 2);
         }
         // its candidate
         if ((int)v < P.cap && (int)v + P.w <= P.cap) {
@@ -190,29 +198,35 @@ __global__ void k_spw_emit(const uint64_t *__restrict__ keys, const uint8_t *__r
                 c[w] &= ~P.sel_mask[w];
             }
             const uint32_t cv = v + (uint32_t)P.w;
-            if (any && cpass && spw_keep<W>(B, c, cv)) spw_emit<W>(ek, estride, ev, H, lg, 2 * i + 1, c, cv, counters + 2);
+            if (any && cpass && spw_keep<W>(B, c, cv))
+                spw_emit<W, BLK>(ek, estride, ev, H, lg, 2 * i + 1, c, cv, counters + 2);
         }
     }
 }
 
-// new table (keys, vals, index lg2) from the staging index; changed states from candidate slots
 template <int W>
-__global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t hcap, const uint64_t *__restrict__ ek,
-                              uint64_t estride, uint64_t *nk, uint8_t *nv, uint64_t ncap, unsigned long long *H2,
-                              int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap, const unsigned long long *Hold,
-                              int lg_old, const uint64_t *okeys, uint64_t ostride, const WideStep P,
-                              unsigned long long *counters, const unsigned long long *lg_dev = nullptr,
-                              const unsigned long long *lg_old_dev = nullptr) {
-    if (lg_dev) {
-        lg2 = (int)*lg_dev;
-        hcap = 1ull << lg2;
-    }
-    if (lg_old_dev) lg_old = (int)*lg_old_dev;
-    // tiles of blockDim slots (the trip count is the same for every thread of a block: output
-    // positions are claimed once per block and tile)
-    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < hcap; t0 += (uint64_t)gridDim.x * blockDim.x) {
+__global__ void k_spw_emit(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t n,
+                           uint64_t stride, uint64_t *ek, uint8_t *ev, uint64_t estride, unsigned long long *H, int lg,
+                           const WideStep P, const WideBound B, unsigned long long *counters,
+                           const unsigned long long *n_dev = nullptr, const unsigned long long *lg_dev = nullptr,
+                           const unsigned long long *abort = nullptr) {
+    n = (abort && *abort) ? 0 : spw_count(n_dev, n);
+    if (lg_dev) lg = (int)*lg_dev;
+    spw_emit_body<W, false>(grid_lanes(), keys, vals, n, stride, ek, ev, estride, H, lg, P, B, counters);
+}
+
+// new table (keys, vals, index lg2) from the staging index; changed states from candidate slots.
+// Tiles of blockDim slots: output positions are claimed once per block and tile.
+template <int W>
+__device__ __forceinline__ void spw_compact_body(const Lanes &L, const unsigned long long *__restrict__ H,
+                                                 uint64_t hcap, const uint64_t *__restrict__ ek, uint64_t estride,
+                                                 uint64_t *nk, uint8_t *nv, uint64_t ncap, unsigned long long *H2,
+                                                 int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap,
+                                                 const unsigned long long *Hold, int lg_old, const uint64_t *okeys,
+                                                 uint64_t ostride, const WideStep &P, unsigned long long *counters) {
+    for (uint64_t t0 = L.tile0; t0 < hcap; t0 += L.tstep) {
         const uint64_t s = t0 + threadIdx.x;
-        const unsigned long long cur = s < hcap ? H[s] : SPW_EMPTY;
+        const unsigned long long cur = s < hcap ? __ldcg(H + s) : SPW_EMPTY;
         const bool occ = cur != SPW_EMPTY;
         const uint64_t e = cur & SPW_IDX;
         const uint32_t v = (uint32_t)(cur >> 56);
@@ -260,13 +274,29 @@ __global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t
     }
 }
 
+template <int W>
+__global__ void k_spw_compact(const unsigned long long *__restrict__ H, uint64_t hcap, const uint64_t *__restrict__ ek,
+                              uint64_t estride, uint64_t *nk, uint8_t *nv, uint64_t ncap, unsigned long long *H2,
+                              int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap, const unsigned long long *Hold,
+                              int lg_old, const uint64_t *okeys, uint64_t ostride, const WideStep P,
+                              unsigned long long *counters, const unsigned long long *lg_dev = nullptr,
+                              const unsigned long long *lg_old_dev = nullptr) {
+    if (lg_dev) {
+        lg2 = (int)*lg_dev;
+        hcap = 1ull << lg2;
+    }
+    if (lg_old_dev) lg_old = (int)*lg_old_dev;
+    spw_compact_body<W>(grid_lanes(), H, hcap, ek, estride, nk, nv, ncap, H2, lg2, ck, cv, ccap, Hold, lg_old, okeys,
+                        ostride, P, counters);
+}
+
 // a table's states with value < below (all when below < 0) into (nk, nv) with their own index
 template <int W>
-__device__ __forceinline__ void spw_filter_body(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals,
-                                                uint64_t n, uint64_t stride, int below, uint64_t *nk, uint8_t *nv,
-                                                uint64_t ncap, unsigned long long *H2, int lg2,
-                                                unsigned long long *counters) {
-    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < n; t0 += (uint64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void spw_filter_body(const Lanes &L, const uint64_t *__restrict__ keys,
+                                                const uint8_t *__restrict__ vals, uint64_t n, uint64_t stride,
+                                                int below, uint64_t *nk, uint8_t *nv, uint64_t ncap,
+                                                unsigned long long *H2, int lg2, unsigned long long *counters) {
+    for (uint64_t t0 = L.tile0; t0 < n; t0 += L.tstep) {
         const uint64_t i = t0 + threadIdx.x;
         const uint32_t v = i < n ? vals[i] : 255u;
         const bool want = i < n && !(below >= 0 && (int)v >= below);
@@ -296,11 +326,28 @@ __global__ void k_spw_filter(const uint64_t *__restrict__ keys, const uint8_t *_
                              const unsigned long long *n_dev = nullptr, const unsigned long long *lg_dev = nullptr) {
     n = spw_count(n_dev, n);
     if (lg_dev) lg2 = (int)*lg_dev;
-    spw_filter_body<W>(keys, vals, n, stride, below, nk, nv, ncap, H2, lg2, counters);
+    spw_filter_body<W>(grid_lanes(), keys, vals, n, stride, below, nk, nv, ncap, H2, lg2, counters);
 }
 
 // least f.value + b.value over changed f and backward b with key(b) = key(f) ^ tmask:
-// result = min(total << 40 | f)
+// result = min(total << 40 | tag | f)
+template <int W>
+__device__ __forceinline__ void spw_join_body(const Lanes &L, const uint64_t *__restrict__ fk,
+                                              const uint8_t *__restrict__ fv, uint64_t nf, uint64_t fstride,
+                                              const unsigned long long *__restrict__ Hb, int lgb,
+                                              const uint64_t *__restrict__ bk, uint64_t bstride,
+                                              const uint64_t *tmask, unsigned long long *result, uint64_t tag) {
+    for (uint64_t i = L.first; i < nf; i += L.step) {
+        uint64_t q[W];
+        spw_load<W>(fk, fstride, i, q);
+#pragma unroll
+        for (int w = 0; w < W; w++) q[w] ^= tmask[w];
+        const uint32_t bv = spw_lookup<W>(Hb, lgb, bk, bstride, q);
+        if (bv == 255u) continue;
+        atomicMin(result, ((unsigned long long)(fv[i] + bv) << 40) | tag | i);
+    }
+}
+
 template <int W>
 __global__ void k_spw_join(const uint64_t *__restrict__ fk, const uint8_t *__restrict__ fv, uint64_t nf,
                            uint64_t fstride, const unsigned long long *__restrict__ Hb, int lgb,
@@ -308,15 +355,7 @@ __global__ void k_spw_join(const uint64_t *__restrict__ fk, const uint8_t *__res
                            unsigned long long *result, const unsigned long long *n_dev = nullptr,
                            uint64_t tag = 0) {
     nf = spw_count(n_dev, nf);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nf; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t q[W];
-        spw_load<W>(fk, fstride, i, q);
-#pragma unroll
-        for (int w = 0; w < W; w++) q[w] ^= T.tmask[w];
-        const uint32_t bv = spw_lookup<W>(Hb, lgb, bk, bstride, q);
-        if (bv == 255u) continue;
-        atomicMin(result, ((unsigned long long)(fv[i] + bv) << 40) | tag | i);
-    }
+    spw_join_body<W>(grid_lanes(), fk, fv, nf, fstride, Hb, lgb, bk, bstride, T.tmask, result, tag);
 }
 
 template <int W>
@@ -339,33 +378,14 @@ __device__ __forceinline__ int spw_lg_dev(uint64_t n) {         // index bits fo
     return lg;
 }
 
-// fill the index (or two) of 2^lg slots, lg = index bits for mult * n states; *lg_out = lg.  Once a
-// step has raised a flag (prev: its counter block) the walk is void: *abort is set and the later
-// steps run on empty tables (the host runs the leg again with more room).
-__global__ void k_spw_fill_dyn(const unsigned long long *n_dev, uint64_t ncap, int mult, unsigned long long *lg_out,
-                               unsigned long long *H1, unsigned long long *H2, const unsigned long long *prev,
-                               unsigned long long *abort) {
-    const bool bad = *abort || (prev && ((prev[2] | prev[6]) & 7ull));
-    if (bad && blockIdx.x == 0 && threadIdx.x == 0) *abort = 1;
-    const int lg = spw_lg_dev(bad ? 0 : (uint64_t)mult * spw_count(n_dev, ncap));
-    if (blockIdx.x == 0 && threadIdx.x == 0) *lg_out = (unsigned long long)lg;
-    const uint64_t m = 1ull << lg;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
-        H1[i] = SPW_EMPTY;
-        if (H2) H2[i] = SPW_EMPTY;
-    }
-}
-
 // place of a kept table in the arena: rec = [n, offset, flags, lg, stride, -, -, -]; flags 8: no
 // room (used still grows by the bytes it needed), 16: not kept (keep mode 2 and a large table)
 __device__ __forceinline__ uint64_t spw_keep_bytes(int W, uint64_t stride, int lg) {
     return ((uint64_t)W * stride * 8 + (stride + 255) / 256 * 256 + (8ull << lg) + 255) / 256 * 256;
 }
 
-__global__ void k_spw_keep_alloc(const unsigned long long *n_dev, uint64_t ncap, int W, int mode,
-                                 unsigned long long *rec, unsigned long long *used, uint64_t arena_bytes) {
-    if (threadIdx.x || blockIdx.x) return;
-    const uint64_t n = spw_count(n_dev, ncap);
+__device__ __forceinline__ void spw_keep_place(uint64_t n, int W, int mode, unsigned long long *rec,
+                                               unsigned long long *used, uint64_t arena_bytes) {
     if (mode == 2 && n > SPW_KEEP_SMALL) {
         rec[2] = 16;
         return;
@@ -383,6 +403,12 @@ __global__ void k_spw_keep_alloc(const unsigned long long *n_dev, uint64_t ncap,
     rec[1] = off;
 }
 
+__global__ void k_spw_keep_alloc(const unsigned long long *n_dev, uint64_t ncap, int W, int mode,
+                                 unsigned long long *rec, unsigned long long *used, uint64_t arena_bytes) {
+    if (threadIdx.x || blockIdx.x) return;
+    spw_keep_place(spw_count(n_dev, ncap), W, mode, rec, used, arena_bytes);
+}
+
 __device__ __forceinline__ unsigned long long *spw_keep_index(uint8_t *arena, const unsigned long long *rec, int W) {
     const uint64_t stride = rec[4];
     return reinterpret_cast<unsigned long long *>(arena + rec[1] + (uint64_t)W * stride * 8 + (stride + 255) / 256 * 256);
@@ -390,34 +416,218 @@ __device__ __forceinline__ unsigned long long *spw_keep_index(uint8_t *arena, co
 
 __global__ void k_spw_keep_fill(uint8_t *arena, const unsigned long long *rec, int W) {
     if (rec[2] & 24ull) return;
-    unsigned long long *H = spw_keep_index(arena, rec, W);
-    const uint64_t m = 1ull << rec[3];
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
-        H[i] = SPW_EMPTY;
+    spw_fill_body(grid_lanes(), spw_keep_index(arena, rec, W), 1ull << rec[3]);
+}
+
+template <int W>
+__device__ __forceinline__ void spw_keep_body(const Lanes &L, const uint64_t *__restrict__ keys,
+                                              const uint8_t *__restrict__ vals, uint64_t n, uint64_t stride,
+                                              uint8_t *arena, unsigned long long *rec) {
+    const uint64_t ks = rec[4];
+    uint64_t *nk = reinterpret_cast<uint64_t *>(arena + rec[1]);
+    uint8_t *nv = arena + rec[1] + (uint64_t)W * ks * 8;
+    spw_filter_body<W>(L, keys, vals, n, stride, -1, nk, nv, ks, spw_keep_index(arena, rec, W), (int)rec[3], rec);
 }
 
 template <int W>
 __global__ void k_spw_keep(const uint64_t *__restrict__ keys, const uint8_t *__restrict__ vals, uint64_t stride,
                            const unsigned long long *n_dev, uint8_t *arena, unsigned long long *rec) {
     if (rec[2] & 24ull) return;
-    const uint64_t n = spw_count(n_dev, stride), ks = rec[4];
-    uint64_t *nk = reinterpret_cast<uint64_t *>(arena + rec[1]);
-    uint8_t *nv = arena + rec[1] + (uint64_t)W * ks * 8;
-    spw_filter_body<W>(keys, vals, n, stride, -1, nk, nv, ks, spw_keep_index(arena, rec, W), (int)rec[3], rec);
+    spw_keep_body<W>(grid_lanes(), keys, vals, spw_count(n_dev, stride), stride, arena, rec);
 }
 
 // the forward state (key words and value) behind a step's join result, for the host
 template <int W>
-__global__ void k_spw_capture(const unsigned long long *result, const uint64_t *ck, const uint8_t *cv,
-                              const uint64_t *tk, const uint8_t *tv, uint64_t stride, uint64_t *resk, uint8_t *resv) {
+__device__ __forceinline__ void spw_capture_one(const unsigned long long *result, const uint64_t *ck,
+                                                const uint8_t *cv, const uint64_t *tk, const uint8_t *tv,
+                                                uint64_t stride, uint64_t *resk, uint8_t *resv) {
     const unsigned long long r = *result;
-    if (threadIdx.x || blockIdx.x || r == SPW_EMPTY) return;
+    if (r == SPW_EMPTY) return;
     const uint64_t i = r & (SPW_TAG - 1);
     const uint64_t *k = (r & SPW_TAG) ? tk : ck;
     const uint8_t *v = (r & SPW_TAG) ? tv : cv;
 #pragma unroll
     for (int w = 0; w < W; w++) resk[w] = k[(uint64_t)w * stride + i];
     *resv = v[i];
+}
+
+template <int W>
+__global__ void k_spw_capture(const unsigned long long *result, const uint64_t *ck, const uint8_t *cv,
+                              const uint64_t *tk, const uint8_t *tv, uint64_t stride, uint64_t *resk, uint8_t *resv) {
+    if (threadIdx.x || blockIdx.x) return;
+    spw_capture_one<W>(result, ck, cv, tk, tv, stride, resk, resv);
+}
+
+// fill the index (or two) of 2^lg slots, lg = index bits for mult * n states; *lg_out = lg.  Once a
+// step has raised a flag (prev: its counter block) the walk is void: *abort is set and the later
+// steps run on empty tables (the host runs the leg again with more room).  With cap_res, thread 0
+// first captures the previous step's join result (its changed list and table are still intact).
+template <int W>
+__global__ void k_spw_fill_dyn(const unsigned long long *n_dev, uint64_t ncap, int mult, unsigned long long *lg_out,
+                               unsigned long long *H1, unsigned long long *H2, const unsigned long long *prev,
+                               unsigned long long *abort, const unsigned long long *cap_res = nullptr,
+                               const uint64_t *cap_ck = nullptr, const uint8_t *cap_cv = nullptr,
+                               const uint64_t *cap_tk = nullptr, const uint8_t *cap_tv = nullptr,
+                               uint64_t cap_stride = 0, uint64_t *cap_k = nullptr, uint8_t *cap_v = nullptr) {
+    if (cap_res && blockIdx.x == 0 && threadIdx.x == 0)
+        spw_capture_one<W>(cap_res, cap_ck, cap_cv, cap_tk, cap_tv, cap_stride, cap_k, cap_v);
+    const bool bad = *abort || (prev && ((prev[2] | prev[6]) & 7ull));
+    if (bad && blockIdx.x == 0 && threadIdx.x == 0) *abort = 1;
+    const int lg = spw_lg_dev(bad ? 0 : (uint64_t)mult * spw_count(n_dev, ncap));
+    if (blockIdx.x == 0 && threadIdx.x == 0) *lg_out = (unsigned long long)lg;
+    const uint64_t m = 1ull << lg;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        H1[i] = SPW_EMPTY;
+        if (H2) H2[i] = SPW_EMPTY;
+    }
+}
+
+// ---- a leg of column steps (tg_spw_walk).  Per step, int64 fields (SPW_WALK_FIELDS): cap,
+// keep_below, w, trunc (< 0: none), keep (0, 1, 2: small tables only), join (a backward table to
+// join), ncls, use_h, extra, join keys, join index, join index bits, join key stride; uint64 words
+// [5][W]: upd, sel_mask, sel_bits, the bound's tmask, the join's tmask.
+#define SPW_WALK_FIELDS 13
+enum { WK_CAP, WK_KB, WK_W, WK_TRUNC, WK_KEEP, WK_JOIN, WK_NCLS, WK_USEH, WK_EXTRA, WK_JKEYS, WK_JH, WK_JLG, WK_JSTRIDE };
+
+struct SpwRing {
+    uint64_t *keys;
+    uint8_t *vals;
+    unsigned long long *H;
+};
+
+// Counters of a walk (uint64 blocks of 8): block 0 the start table, block i + 1 step i ([0] states,
+// [1] changed, [2] flags, [3] index bits, [4] states after the cut's truncation, [5] its index
+// bits, [6] its flags), block nsteps + 1 + i the keep record of step i, block 2 nsteps + 1: [0]
+// arena bytes used, [1] abort, [2..4] the one-block walk's stop state.  The table before step i:
+__host__ __device__ __forceinline__ int spw_prev_off(const int64_t *steps, int i, int &noff, int &lgoff) {
+    const bool tr = i > 0 && steps[(size_t)SPW_WALK_FIELDS * (i - 1) + WK_TRUNC] >= 0;
+    noff = tr ? 4 : 0;
+    lgoff = tr ? 5 : 3;
+    return 8 * i;
+}
+
+#define SPW_SMALL_THREADS 512
+#define SPW_SMALL_LIMIT 8192          // the one-block walk steps tables while 2 n <= this
+
+struct SpwSmall {
+    const int64_t *steps;             // device copies of the walk's step records
+    const uint64_t *words, *masks;
+    const int64_t *weights;
+    int maxc, K, i0, nsteps, cur;
+    uint64_t cap, limit, arena_bytes;
+    SpwRing ring[3], sg, ch;
+    unsigned long long *cnt, *res;
+    uint64_t *resk;
+    uint8_t *resv, *arena;
+};
+
+// Steps i0.. of a walk in one block while the tables are small (no launch per kernel of a step):
+// the same bodies as the separate kernels, with the block's barriers between them.  Stops before a
+// step whose table holds more than limit / 2 states (reason 1) or after a step that raised a flag
+// (reason 4, the walk is void); state: [0] next step, [1] ring slot of its table, [2] reason.
+template <int W>
+__global__ void __launch_bounds__(SPW_SMALL_THREADS) k_spw_walk_small(const __grid_constant__ SpwSmall S) {
+    __shared__ WideStep P;
+    __shared__ WideBound B;
+    __shared__ uint64_t jt[SPW_MAXW];
+    const Lanes L = block_lanes();
+    const unsigned tid = threadIdx.x;
+    unsigned long long *abort = S.cnt + 8ull * (2 * (uint64_t)S.nsteps + 1) + 1, *state = abort + 1;
+    const uint64_t cap = S.cap;
+    int cur = S.cur, i = S.i0, reason = 0;
+    for (; i < S.nsteps; i++) {
+        int noff, lgoff;
+        const unsigned long long *pc = S.cnt + spw_prev_off(S.steps, i, noff, lgoff);
+        const uint64_t n = spw_count(pc + noff, cap);
+        const int lg_old = (int)__ldcg(pc + lgoff);
+        if (__ldcg(abort)) { reason = 4; break; }
+        if (2 * n > S.limit) { reason = 1; break; }
+        const int64_t *f = S.steps + (size_t)SPW_WALK_FIELDS * i;
+        const uint64_t *wd = S.words + (size_t)5 * W * i;
+        const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[WK_JH]);
+        const uint64_t *jk = reinterpret_cast<const uint64_t *>((uintptr_t)f[WK_JKEYS]);
+        const bool join = f[WK_JOIN] && jH && jk;
+        const int ncls = f[WK_USEH] ? (int)f[WK_NCLS] : 0;
+        if (tid == 0) {
+            P.cap = (int)f[WK_CAP];
+            P.keep_below = (int)f[WK_KB];
+            P.w = (int)f[WK_W];
+            P.want_changed = join;
+            B.on = (int)f[WK_USEH];
+            B.ncls = ncls;
+            B.K = S.K;
+            B.extra = f[WK_EXTRA];
+        }
+        for (unsigned q = tid; q < (unsigned)W; q += blockDim.x) {
+            P.upd[q] = wd[q];
+            P.sel_mask[q] = wd[W + q];
+            P.sel_bits[q] = wd[2 * W + q];
+            B.tmask[q] = wd[3 * W + q];
+            jt[q] = wd[4 * W + q];
+        }
+        for (unsigned c = tid; c < (unsigned)(ncls * W); c += blockDim.x)
+            B.mask[c / W][c % W] = S.masks[((size_t)i * S.maxc) * W + c];
+        for (unsigned c = tid; c < (unsigned)ncls; c += blockDim.x) B.w[c] = S.weights[(size_t)i * S.maxc + c];
+        unsigned long long *c = S.cnt + 8ull * (i + 1);
+        const int lgs = spw_lg_dev(2 * n);
+        if (tid == 0) c[3] = (unsigned long long)lgs;
+        const int out = (cur + 1) % 3;
+        spw_fill_body(L, S.sg.H, 1ull << lgs);
+        spw_fill_body(L, S.ring[out].H, 1ull << lgs);
+        __syncthreads();
+        spw_emit_body<W, true>(L, S.ring[cur].keys, S.ring[cur].vals, n, cap, S.sg.keys, S.sg.vals, 2 * cap, S.sg.H, lgs,
+                               P, B, c);
+        __syncthreads();
+        spw_compact_body<W>(L, S.sg.H, 1ull << lgs, S.sg.keys, 2 * cap, S.ring[out].keys, S.ring[out].vals, cap,
+                            S.ring[out].H, lgs, S.ch.keys, S.ch.vals, cap, S.ring[cur].H, lg_old, S.ring[cur].keys,
+                            cap, P, c);
+        __syncthreads();
+        if (__ldcg(c + 2) & 7ull) { reason = 4; break; }
+        const uint64_t nout = spw_count(c, cap);
+        if (join)
+            spw_join_body<W>(L, S.ch.keys, S.ch.vals, spw_count(c + 1, cap), cap, jH, (int)f[WK_JLG], jk,
+                             (uint64_t)f[WK_JSTRIDE], jt, S.res + i, 0);
+        int now = out;
+        const unsigned long long *nnow = c;
+        if (f[WK_TRUNC] >= 0) {
+            // the cap drops at this cut: the whole table before the drop is joined too
+            if (join)
+                spw_join_body<W>(L, S.ring[out].keys, S.ring[out].vals, nout, cap, jH, (int)f[WK_JLG], jk,
+                                 (uint64_t)f[WK_JSTRIDE], jt, S.res + i, SPW_TAG);
+            const int tr = (out + 1) % 3, lgt = spw_lg_dev(nout);
+            if (tid == 0) c[5] = (unsigned long long)lgt;
+            spw_fill_body(L, S.ring[tr].H, 1ull << lgt);
+            __syncthreads();
+            spw_filter_body<W>(L, S.ring[out].keys, S.ring[out].vals, nout, cap, (int)f[WK_TRUNC], S.ring[tr].keys,
+                               S.ring[tr].vals, cap, S.ring[tr].H, lgt, c + 4);
+            now = tr;
+            nnow = c + 4;
+        }
+        __syncthreads();
+        if (__ldcg(c + 6) & 7ull) { reason = 4; break; }
+        if (join && tid == 0)
+            spw_capture_one<W>(S.res + i, S.ch.keys, S.ch.vals, S.ring[out].keys, S.ring[out].vals, cap,
+                               S.resk + (size_t)i * W, S.resv + i);
+        if (f[WK_KEEP]) {
+            unsigned long long *rec = S.cnt + 8ull * (S.nsteps + 1 + i);
+            const uint64_t nk = spw_count(nnow, cap);
+            if (tid == 0) spw_keep_place(nk, W, (int)f[WK_KEEP], rec, abort - 1, S.arena ? S.arena_bytes : 0);
+            __syncthreads();
+            if (!(__ldcg(rec + 2) & 24ull)) {
+                spw_fill_body(L, spw_keep_index(S.arena, rec, W), 1ull << __ldcg(rec + 3));
+                __syncthreads();
+                spw_keep_body<W>(L, S.ring[now].keys, S.ring[now].vals, nk, cap, S.arena, rec);
+            }
+        }
+        __syncthreads();
+        cur = now;
+    }
+    if (reason == 4 && tid == 0) *abort = 1;
+    if (tid == 0) {
+        state[0] = (unsigned long long)i;
+        state[1] = (unsigned long long)cur;
+        state[2] = (unsigned long long)reason;
+    }
 }
 
 static unsigned spw_grid(uint64_t n) {
@@ -466,18 +676,6 @@ static int spw_step_w(const uint64_t *keys, const uint8_t *vals, uint64_t n, uin
 }
 
 // ---- a leg of column steps in one call (no host read between steps)
-// Per step, int64 fields (SPW_WALK_FIELDS): cap, keep_below, w, trunc (< 0: none), keep (0, 1, 2:
-// small tables only), join (a backward table to join), ncls, use_h, extra, join keys, join index,
-// join index bits, join key stride; uint64 words [5][W]: upd, sel_mask, sel_bits, the bound's
-// tmask, the join's tmask.
-#define SPW_WALK_FIELDS 13
-enum { WK_CAP, WK_KB, WK_W, WK_TRUNC, WK_KEEP, WK_JOIN, WK_NCLS, WK_USEH, WK_EXTRA, WK_JKEYS, WK_JH, WK_JLG, WK_JSTRIDE };
-
-struct SpwRing {
-    uint64_t *keys;
-    uint8_t *vals;
-    unsigned long long *H;
-};
 
 static int spw_walk_lg(uint64_t n) {
     int lg = 6;
@@ -526,96 +724,205 @@ static uint64_t spw_walk_layout(int W, uint64_t cap, int nsteps, uint8_t *base, 
     return off;
 }
 
+// device copies of a walk's step records (for the one-block walk), grown as needed
+struct SpwRecords {
+    int64_t *steps = nullptr;
+    uint64_t *words = nullptr, *masks = nullptr;
+    int64_t *weights = nullptr;
+};
+
+static int spw_records(int W, int nsteps, int maxc, const int64_t *steps, const uint64_t *words,
+                       const uint64_t *masks, const int64_t *weights, cudaStream_t st, SpwRecords &R) {
+    static thread_local uint8_t *buf = nullptr;
+    static thread_local size_t buf_bytes = 0;
+    auto rnd = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t bs = rnd(8ull * SPW_WALK_FIELDS * nsteps), bw = rnd(8ull * 5 * W * nsteps),
+                 bm = rnd(8ull * maxc * W * nsteps), bg = rnd(8ull * maxc * nsteps), tot = bs + bw + bm + bg + 256;
+    if (buf_bytes < tot) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        buf_bytes = 0;
+        if (cudaMalloc(&buf, tot) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(TG_ERR_NOMEM, "wide walk records");
+        }
+        buf_bytes = tot;
+    }
+    R.steps = reinterpret_cast<int64_t *>(buf);
+    R.words = reinterpret_cast<uint64_t *>(buf + bs);
+    R.masks = reinterpret_cast<uint64_t *>(buf + bs + bw);
+    R.weights = reinterpret_cast<int64_t *>(buf + bs + bw + bm);
+    int e = cuda_check(cudaMemcpyAsync(R.steps, steps, 8ull * SPW_WALK_FIELDS * nsteps, cudaMemcpyHostToDevice, st),
+                       "walk records");
+    if (!e) e = cuda_check(cudaMemcpyAsync(R.words, words, 8ull * 5 * W * nsteps, cudaMemcpyHostToDevice, st),
+                           "walk records");
+    if (!e) e = cuda_check(cudaMemcpyAsync(R.masks, masks, 8ull * maxc * W * nsteps, cudaMemcpyHostToDevice, st),
+                           "walk records");
+    if (!e) e = cuda_check(cudaMemcpyAsync(R.weights, weights, 8ull * maxc * nsteps, cudaMemcpyHostToDevice, st),
+                           "walk records");
+    return e;
+}
+
+#define SPW_CHUNK 32                  // steps of separate launches between two reads of the table size
+
+// The walk: while the table is small, one launch of the one-block walk runs steps until the table
+// outgrows it; larger tables take a few launches per step, SPW_CHUNK steps between reads of the
+// table size (the next small stretch starts once it is back under a quarter of the limit).
 template <int W>
 static int spw_walk_w(int nsteps, const int64_t *steps, const uint64_t *words, const uint64_t *masks,
                       const int64_t *weights, int maxc, int K, const uint64_t *k0, const uint8_t *v0, uint64_t n0,
                       uint64_t stride0, uint8_t *scratch, uint64_t cap, uint8_t *arena, uint64_t arena_bytes,
-                      cudaStream_t st) {
+                      unsigned long long *hb, cudaStream_t st) {
     SpwRing ring[3], sg, ch;
     unsigned long long *cnt, *res;
     uint64_t *resk;
     uint8_t *resv;
     spw_walk_layout(W, cap, nsteps, scratch, ring, &sg, &ch, &cnt, &res, &resk, &resv);
-    // counters: block 0 the start table, block i + 1 step i ([0] states, [1] changed, [2] flags,
-    // [3] index bits, [4] states after the cut's truncation, [5] its index bits, [6] its flags),
-    // block nsteps + 1 + i the keep record of step i, block 2 nsteps + 1 [0] the arena bytes used
     const size_t cbytes = 64ull * (2 * (uint64_t)nsteps + 2);
     int e = cuda_check(cudaMemsetAsync(cnt, 0, cbytes, st), "walk counters");
     if (!e && nsteps) e = cuda_check(cudaMemsetAsync(res, 0xFF, 8ull * nsteps, st), "walk results");
     if (e) return e;
-    unsigned long long *used = cnt + 8ull * (2 * (uint64_t)nsteps + 1), *abort = used + 1;
+    for (int i = 0; i < nsteps; i++) {
+        const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
+        if (f[WK_USEH] && (f[WK_NCLS] < 0 || f[WK_NCLS] > maxc))
+            return set_error(TG_ERR_ARG, "lookahead classes beyond the step's arrays");
+        if (f[WK_USEH] && f[WK_NCLS] > SPW_MAXCLS) return set_error(TG_ERR_TOO_BIG, "more than 32 lookahead classes");
+    }
+    SpwRecords R;
+    if (nsteps) e = spw_records(W, nsteps, maxc, steps, words, masks, weights, st, R);
+    if (e) return e;
+    unsigned long long *used = cnt + 8ull * (2 * (uint64_t)nsteps + 1), *abort = used + 1, *sstate = used + 2;
     const unsigned gc = spw_grid(cap), gi = spw_grid(1ull << spw_walk_lg(2 * cap));
     // the start table into ring slot 0
-    k_spw_fill_dyn<<<gi, 256, 0, st>>>(nullptr, n0, 1, cnt + 3, ring[0].H, nullptr, nullptr, abort);
+    k_spw_fill_dyn<W><<<gi, 256, 0, st>>>(nullptr, n0, 1, cnt + 3, ring[0].H, nullptr, nullptr, abort);
     if (n0)
         k_spw_filter<W><<<spw_grid(n0), 256, 0, st>>>(k0, v0, n0, stride0, -1, ring[0].keys, ring[0].vals, cap,
                                                       ring[0].H, 0, cnt, nullptr, cnt + 3);
-    int cur = 0;
-    const unsigned long long *ncur = cnt, *lgcur = cnt + 3, *cprev = cnt;
-    for (int i = 0; i < nsteps; i++) {
-        const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
-        const uint64_t *wd = words + (size_t)5 * W * i;
-        if (f[WK_CAP] > 254 || f[WK_W] < 1 || f[WK_W] > 254) return set_error(TG_ERR_ARG, "values beyond 8 bits");
-        WideStep P;
-        memset(&P, 0, sizeof(P));
-        for (int q = 0; q < W; q++) {
-            P.upd[q] = wd[q];
-            P.sel_mask[q] = wd[W + q];
-            P.sel_bits[q] = wd[2 * W + q];
+    const uint64_t limit = std::min<uint64_t>(SPW_SMALL_LIMIT, cap);
+    uint64_t host_n = n0;             // the table size before step i, when known on the host
+    int cur = 0, i = 0;
+    while (i < nsteps) {
+        if (4 * host_n <= limit) {
+            SpwSmall S;
+            S.steps = R.steps;
+            S.words = R.words;
+            S.masks = R.masks;
+            S.weights = R.weights;
+            S.maxc = maxc;
+            S.K = K;
+            S.i0 = i;
+            S.nsteps = nsteps;
+            S.cur = cur;
+            S.cap = cap;
+            S.limit = limit;
+            S.arena_bytes = arena_bytes;
+            for (int r = 0; r < 3; r++) S.ring[r] = ring[r];
+            S.sg = sg;
+            S.ch = ch;
+            S.cnt = cnt;
+            S.res = res;
+            S.resk = resk;
+            S.resv = resv;
+            S.arena = arena;
+            k_spw_walk_small<W><<<1, SPW_SMALL_THREADS, 0, st>>>(S);
+            e = cuda_check(cudaGetLastError(), "small wide walk");
+            if (!e) e = cuda_check(cudaMemcpyAsync(hb, sstate, 24, cudaMemcpyDeviceToHost, st), "walk state");
+            if (!e) e = cuda_check(cudaStreamSynchronize(st), "walk sync");
+            if (e) return e;
+            i = (int)hb[0];
+            cur = (int)hb[1];
+            if (hb[2] == 4) break;    // a flag: the walk is void, the host reads why at the end
+            host_n = ~0ull >> 3;      // beyond the limit until read again
+            if (i >= nsteps) break;
         }
-        P.cap = (int)f[WK_CAP];
-        P.keep_below = (int)f[WK_KB];
-        P.w = (int)f[WK_W];
-        const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[WK_JH]);
-        const uint64_t *jk = reinterpret_cast<const uint64_t *>((uintptr_t)f[WK_JKEYS]);
-        const bool join = f[WK_JOIN] && jH && jk;
-        P.want_changed = join;
-        WideBound B, T;
-        e = spw_bound(B, W, (int)f[WK_USEH], K, (int)f[WK_NCLS], masks + (size_t)i * maxc * W,
-                      weights + (size_t)i * maxc, f[WK_EXTRA], wd + 3 * W);
-        if (e) return e;
-        memset(&T, 0, sizeof(T));
-        for (int q = 0; q < W; q++) T.tmask[q] = wd[4 * W + q];
-        unsigned long long *c = cnt + 8ull * (i + 1);
-        const int out = (cur + 1) % 3;
-        // staging and new index for 2 n states, then the two kernels of the step
-        k_spw_fill_dyn<<<gi, 256, 0, st>>>(ncur, cap, 2, c + 3, sg.H, ring[out].H, cprev, abort);
-        k_spw_emit<W><<<gc, 256, 0, st>>>(ring[cur].keys, ring[cur].vals, cap, cap, sg.keys, sg.vals, 2 * cap, sg.H, 0,
-                                          P, B, c, ncur, c + 3, abort);
-        k_spw_compact<W><<<gi, 256, 0, st>>>(sg.H, 0, sg.keys, 2 * cap, ring[out].keys, ring[out].vals, cap,
-                                             ring[out].H, 0, ch.keys, ch.vals, cap, ring[cur].H, 0, ring[cur].keys,
-                                             cap, P, c, c + 3, lgcur);
-        if (join)
-            k_spw_join<W><<<gc, 256, 0, st>>>(ch.keys, ch.vals, cap, cap, jH, (int)f[WK_JLG], jk,
-                                              (uint64_t)f[WK_JSTRIDE], T, res + i, c + 1, 0);
-        int now = out;
-        const unsigned long long *nnow = c, *lgnow = c + 3;
-        if (f[WK_TRUNC] >= 0) {
-            // the cap drops at this cut: the whole table before the drop is joined too
+        const int stop = std::min(nsteps, i + SPW_CHUNK);
+        int pend = -1, pend_out = 0;      // a join result not yet captured: its step and output slot
+        for (; i < stop; i++) {
+            const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
+            const uint64_t *wd = words + (size_t)5 * W * i;
+            if (f[WK_CAP] > 254 || f[WK_W] < 1 || f[WK_W] > 254) return set_error(TG_ERR_ARG, "values beyond 8 bits");
+            int noff, lgoff;
+            const unsigned long long *pc = cnt + spw_prev_off(steps, i, noff, lgoff);
+            const unsigned long long *ncur = pc + noff, *lgcur = pc + lgoff;
+            WideStep P;
+            memset(&P, 0, sizeof(P));
+            for (int q = 0; q < W; q++) {
+                P.upd[q] = wd[q];
+                P.sel_mask[q] = wd[W + q];
+                P.sel_bits[q] = wd[2 * W + q];
+            }
+            P.cap = (int)f[WK_CAP];
+            P.keep_below = (int)f[WK_KB];
+            P.w = (int)f[WK_W];
+            const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[WK_JH]);
+            const uint64_t *jk = reinterpret_cast<const uint64_t *>((uintptr_t)f[WK_JKEYS]);
+            const bool join = f[WK_JOIN] && jH && jk;
+            P.want_changed = join;
+            WideBound B, T;
+            e = spw_bound(B, W, (int)f[WK_USEH], K, (int)f[WK_NCLS], masks + (size_t)i * maxc * W,
+                          weights + (size_t)i * maxc, f[WK_EXTRA], wd + 3 * W);
+            if (e) return e;
+            memset(&T, 0, sizeof(T));
+            for (int q = 0; q < W; q++) T.tmask[q] = wd[4 * W + q];
+            unsigned long long *c = cnt + 8ull * (i + 1);
+            const int out = (cur + 1) % 3;
+            // staging and new index for 2 n states, then the two kernels of the step
+            if (pend >= 0)
+                k_spw_fill_dyn<W><<<gi, 256, 0, st>>>(ncur, cap, 2, c + 3, sg.H, ring[out].H, pc, abort, res + pend,
+                                                      ch.keys, ch.vals, ring[pend_out].keys, ring[pend_out].vals, cap,
+                                                      resk + (size_t)pend * W, resv + pend);
+            else
+                k_spw_fill_dyn<W><<<gi, 256, 0, st>>>(ncur, cap, 2, c + 3, sg.H, ring[out].H, pc, abort);
+            pend = -1;
+            k_spw_emit<W><<<gc, 256, 0, st>>>(ring[cur].keys, ring[cur].vals, cap, cap, sg.keys, sg.vals, 2 * cap,
+                                              sg.H, 0, P, B, c, ncur, c + 3, abort);
+            k_spw_compact<W><<<gi, 256, 0, st>>>(sg.H, 0, sg.keys, 2 * cap, ring[out].keys, ring[out].vals, cap,
+                                                 ring[out].H, 0, ch.keys, ch.vals, cap, ring[cur].H, 0, ring[cur].keys,
+                                                 cap, P, c, c + 3, lgcur);
             if (join)
-                k_spw_join<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, jH, (int)f[WK_JLG], jk,
-                                                  (uint64_t)f[WK_JSTRIDE], T, res + i, c, SPW_TAG);
-            const int tr = (out + 1) % 3;
-            k_spw_fill_dyn<<<gi, 256, 0, st>>>(c, cap, 1, c + 5, ring[tr].H, nullptr, nullptr, abort);
-            k_spw_filter<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, (int)f[WK_TRUNC],
-                                                ring[tr].keys, ring[tr].vals, cap, ring[tr].H, 0, c + 4, c, c + 5);
-            now = tr;
-            nnow = c + 4;
-            lgnow = c + 5;
+                k_spw_join<W><<<gc, 256, 0, st>>>(ch.keys, ch.vals, cap, cap, jH, (int)f[WK_JLG], jk,
+                                                  (uint64_t)f[WK_JSTRIDE], T, res + i, c + 1, 0);
+            int now = out;
+            const unsigned long long *nnow = c;
+            if (f[WK_TRUNC] >= 0) {
+                // the cap drops at this cut: the whole table before the drop is joined too
+                if (join)
+                    k_spw_join<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, jH, (int)f[WK_JLG],
+                                                      jk, (uint64_t)f[WK_JSTRIDE], T, res + i, c, SPW_TAG);
+                const int tr = (out + 1) % 3;
+                k_spw_fill_dyn<W><<<gi, 256, 0, st>>>(c, cap, 1, c + 5, ring[tr].H, nullptr, nullptr, abort);
+                k_spw_filter<W><<<gc, 256, 0, st>>>(ring[out].keys, ring[out].vals, cap, cap, (int)f[WK_TRUNC],
+                                                    ring[tr].keys, ring[tr].vals, cap, ring[tr].H, 0, c + 4, c, c + 5);
+                now = tr;
+                nnow = c + 4;
+            }
+            if (join) {
+                pend = i;
+                pend_out = out;
+            }
+            // keep mode 2 (small tables, a cache of the caller's) is left to the one-block walk
+            if (f[WK_KEEP] == 1) {
+                unsigned long long *rec = cnt + 8ull * (nsteps + 1 + i);
+                k_spw_keep_alloc<<<1, 32, 0, st>>>(nnow, cap, W, (int)f[WK_KEEP], rec, used, arena ? arena_bytes : 0);
+                k_spw_keep_fill<<<gi, 256, 0, st>>>(arena, rec, W);
+                k_spw_keep<W><<<gc, 256, 0, st>>>(ring[now].keys, ring[now].vals, cap, nnow, arena, rec);
+            }
+            cur = now;
         }
-        if (join)
-            k_spw_capture<W><<<1, 32, 0, st>>>(res + i, ch.keys, ch.vals, ring[out].keys, ring[out].vals, cap,
-                                               resk + (size_t)i * W, resv + i);
-        if (f[WK_KEEP]) {
-            unsigned long long *rec = cnt + 8ull * (nsteps + 1 + i);
-            k_spw_keep_alloc<<<1, 32, 0, st>>>(nnow, cap, W, (int)f[WK_KEEP], rec, used, arena ? arena_bytes : 0);
-            k_spw_keep_fill<<<gi, 256, 0, st>>>(arena, rec, W);
-            k_spw_keep<W><<<gc, 256, 0, st>>>(ring[now].keys, ring[now].vals, cap, nnow, arena, rec);
-        }
-        cur = now;
-        ncur = nnow;
-        lgcur = lgnow;
-        cprev = c;
+        if (pend >= 0)
+            k_spw_capture<W><<<1, 32, 0, st>>>(res + pend, ch.keys, ch.vals, ring[pend_out].keys, ring[pend_out].vals,
+                                               cap, resk + (size_t)pend * W, resv + pend);
+        e = cuda_check(cudaGetLastError(), "wide walk");
+        if (e || i >= nsteps) return e;
+        // the table size before step i (and whether a flag voided the walk)
+        int noff, lgoff;
+        const unsigned long long *pc = cnt + spw_prev_off(steps, i, noff, lgoff);
+        e = cuda_check(cudaMemcpyAsync(hb, pc, 64, cudaMemcpyDeviceToHost, st), "walk read");
+        if (!e) e = cuda_check(cudaMemcpyAsync(hb + 8, abort, 8, cudaMemcpyDeviceToHost, st), "walk read");
+        if (!e) e = cuda_check(cudaStreamSynchronize(st), "walk sync");
+        if (e) return e;
+        if (hb[8]) break;
+        host_n = std::min<uint64_t>(hb[noff], cap);
     }
     return cuda_check(cudaGetLastError(), "wide walk");
 }
@@ -703,30 +1010,33 @@ int tg_spw_walk(int W, int nsteps, const int64_t *steps, const uint64_t *words, 
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint8_t *base = static_cast<uint8_t *>(scratch);
-#define SPW_WALK(WW)                                                                                                  \
-    spw_walk_w<WW>(nsteps, steps, words, masks, weights, maxc, K, (const uint64_t *)keys0, (const uint8_t *)vals0, n0, \
-                   stride0, base, cap, (uint8_t *)arena, arena_bytes, st)
-    auto run = [&]() -> int { SPW_DISPATCH(W, SPW_WALK) };
-#undef SPW_WALK
-    e = run();
-    if (e) return e;
     unsigned long long *cnt, *resd;
     uint64_t *resk;
     uint8_t *resv;
     spw_walk_layout(W, cap, nsteps, base, nullptr, nullptr, nullptr, &cnt, &resd, &resk, &resv);
     const size_t bytes = (size_t)((resv + nsteps + 1) - reinterpret_cast<uint8_t *>(cnt));
+    // pinned host buffer: the walk's reads of its state, then all its counters and results
     static thread_local uint8_t *hb = nullptr;
     static thread_local size_t hb_bytes = 0;
-    if (hb_bytes < bytes) {
+    const size_t want = std::max<size_t>(bytes, 128);
+    if (hb_bytes < want) {
         if (hb) cudaFreeHost(hb);
         hb = nullptr;
         hb_bytes = 0;
-        if (cudaMallocHost(&hb, bytes) != cudaSuccess) {
+        if (cudaMallocHost(&hb, want) != cudaSuccess) {
             cudaGetLastError();
             return set_error(TG_ERR_NOMEM, "pinned walk buffer");
         }
-        hb_bytes = bytes;
+        hb_bytes = want;
     }
+    unsigned long long *hsmall = reinterpret_cast<unsigned long long *>(hb);
+#define SPW_WALK(WW)                                                                                                  \
+    spw_walk_w<WW>(nsteps, steps, words, masks, weights, maxc, K, (const uint64_t *)keys0, (const uint8_t *)vals0, n0, \
+                   stride0, base, cap, (uint8_t *)arena, arena_bytes, hsmall, st)
+    auto run = [&]() -> int { SPW_DISPATCH(W, SPW_WALK) };
+#undef SPW_WALK
+    e = run();
+    if (e) return e;
     e = cuda_check(cudaMemcpyAsync(hb, cnt, bytes, cudaMemcpyDeviceToHost, st), "walk read");
     if (!e) e = cuda_check(cudaStreamSynchronize(st), "walk sync");
     if (e) return e;
