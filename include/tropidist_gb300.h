@@ -193,6 +193,9 @@ int tg_spw_lookup(int W, const void *H, int lg, const void *keys, uint64_t strid
  * total (all ones: none), forward value, forward key words.  Returns nsteps, or 0 with need[0]
  * (states per table) or need[1] (arena bytes) set: run the leg again with more room. */
 int64_t tg_spw_walk_scratch_bytes(int W, uint64_t cap, int nsteps);
+/* tables of at most limit / 2 states are stepped by one block per launch (default 512; 0: never);
+ * returns the previous limit (a negative argument only reads it) */
+int64_t tg_spw_set_small_limit(int64_t limit);
 int tg_spw_walk(int W, int nsteps, const int64_t *steps, const uint64_t *words, const uint64_t *masks,
                 const int64_t *weights, int maxc, int K, const void *keys0, const void *vals0, uint64_t n0,
                 uint64_t stride0, void *scratch, uint64_t cap, void *arena, uint64_t arena_bytes, int64_t *out,

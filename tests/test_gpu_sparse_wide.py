@@ -130,16 +130,27 @@ def test_wide_walk_grows_its_tables_and_arena():
             assert _tables(be, t) == _tables(ref.be, ref.ckpt[c]), (direction, c)
 
 
-def test_wide_meet_by_walks_equals_step_by_step():
+@pytest.mark.parametrize("limit", [0, 64, None])
+def test_wide_meet_by_walks_equals_step_by_step(limit):
     """The meet in the middle run as device walks (joins inside the walk, frontier truncation)
-    gives the value, cut and witness weight of the step-by-step meet on the oracle tables."""
-    from tropidist_gb300 import sparse_dp
-    for copies, seed in ((8, 6), (9, 7)):
-        p, _ = interleaved(copies, seed)
-        tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
-        for K in (3, 5):
-            got = sparse_dp.query(tr, K, mode="mitm")
-            want = sparse_dp.query(tr, K, mode="mitm", backend=WideTables(tr))
-            assert got["value"] == want["value"] and got["peak_states"] == want["peak_states"], (copies, K)
-            if got["value"] is not None:
-                check_witness(p, got["witness"], got["value"], 0)
+    gives the value, peak, join counts and a valid witness as the step-by-step meet on the oracle
+    tables: with separate launches only (limit 0), the one-block walk handing over at 32 states,
+    and the default."""
+    from tropidist_gb300 import _lib, sparse_dp
+    L = _lib.lib()
+    old = L.tg_spw_set_small_limit(-1)
+    try:
+        if limit is not None:
+            L.tg_spw_set_small_limit(limit)
+        for copies, seed in ((8, 6), (9, 7)):
+            p, _ = interleaved(copies, seed)
+            tr = sparse_dp.Trellis.for_query(p, 0, list(range(p.ncols)))
+            for K in (3, 5):
+                got = sparse_dp.query(tr, K, mode="mitm")
+                want = sparse_dp.query(tr, K, mode="mitm", backend=WideTables(tr))
+                assert got["value"] == want["value"] and got["peak_states"] == want["peak_states"], (copies, K)
+                assert got["changed_counts"] == want["changed_counts"], (copies, K)
+                if got["value"] is not None:
+                    check_witness(p, got["witness"], got["value"], 0)
+    finally:
+        L.tg_spw_set_small_limit(old)

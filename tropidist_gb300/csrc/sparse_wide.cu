@@ -507,7 +507,7 @@ __host__ __device__ __forceinline__ int spw_prev_off(const int64_t *steps, int i
 }
 
 #define SPW_SMALL_THREADS 512
-#define SPW_SMALL_LIMIT 8192          // the one-block walk steps tables while 2 n <= this
+static uint64_t g_spw_small_limit = 512;       // the one-block walk steps tables while 2 n <= this
 
 struct SpwSmall {
     const int64_t *steps;             // device copies of the walk's step records
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(SPW_SMALL_THREADS) k_spw_walk_small(const __gr
             P.cap = (int)f[WK_CAP];
             P.keep_below = (int)f[WK_KB];
             P.w = (int)f[WK_W];
-            P.want_changed = join;
+            P.want_changed = f[WK_JOIN] != 0;
             B.on = (int)f[WK_USEH];
             B.ncls = ncls;
             B.K = S.K;
@@ -798,7 +798,7 @@ static int spw_walk_w(int nsteps, const int64_t *steps, const uint64_t *words, c
     if (n0)
         k_spw_filter<W><<<spw_grid(n0), 256, 0, st>>>(k0, v0, n0, stride0, -1, ring[0].keys, ring[0].vals, cap,
                                                       ring[0].H, 0, cnt, nullptr, cnt + 3);
-    const uint64_t limit = std::min<uint64_t>(SPW_SMALL_LIMIT, cap);
+    const uint64_t limit = std::min<uint64_t>(g_spw_small_limit, cap);
     uint64_t host_n = n0;             // the table size before step i, when known on the host
     int cur = 0, i = 0;
     while (i < nsteps) {
@@ -857,7 +857,7 @@ static int spw_walk_w(int nsteps, const int64_t *steps, const uint64_t *words, c
             const unsigned long long *jH = reinterpret_cast<const unsigned long long *>((uintptr_t)f[WK_JH]);
             const uint64_t *jk = reinterpret_cast<const uint64_t *>((uintptr_t)f[WK_JKEYS]);
             const bool join = f[WK_JOIN] && jH && jk;
-            P.want_changed = join;
+            P.want_changed = f[WK_JOIN] != 0;
             WideBound B, T;
             e = spw_bound(B, W, (int)f[WK_USEH], K, (int)f[WK_NCLS], masks + (size_t)i * maxc * W,
                           weights + (size_t)i * maxc, f[WK_EXTRA], wd + 3 * W);
@@ -981,6 +981,13 @@ int tg_spw_step(int W, const void *keys, const void *vals, uint64_t n, uint64_t 
 #undef SPW_STEP
 }
 
+// the one-block walk of wide tables runs while 2 n <= limit (0: never); returns the previous limit
+int64_t tg_spw_set_small_limit(int64_t limit) {
+    const int64_t old = (int64_t)g_spw_small_limit;
+    if (limit >= 0) g_spw_small_limit = (uint64_t)limit;
+    return old;
+}
+
 int64_t tg_spw_walk_scratch_bytes(int W, uint64_t cap, int nsteps) {
     if (spw_check_words(W) || cap < 1 || nsteps < 0) return -1;
     return (int64_t)spw_walk_layout(W, cap, nsteps, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -1065,7 +1072,8 @@ int tg_spw_walk(int W, int nsteps, const int64_t *steps, const uint64_t *words, 
     for (int i = 0; i < nsteps; i++) {
         const int64_t *f = steps + (size_t)SPW_WALK_FIELDS * i;
         const unsigned long long *c = hc + 8ull * (i + 1), *rec = hc + 8ull * (nsteps + 1 + i);
-        const bool tr = f[WK_TRUNC] >= 0, kept = f[WK_KEEP] && !(rec[2] & 16ull);
+        // kept: placed in the arena (the separate-launch path leaves keep mode 2 to the one-block walk)
+        const bool tr = f[WK_TRUNC] >= 0, kept = f[WK_KEEP] && !(rec[2] & 16ull) && rec[4] != 0;
         int64_t *o = out + 6 * (size_t)i;
         o[0] = (int64_t)(tr ? c[4] : c[0]);
         o[1] = (int64_t)c[1];
