@@ -156,10 +156,11 @@ __global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_con
 // the occupied slots of an index into an array; counters[3] = states written
 __global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t cap, unsigned long long *out,
                              uint64_t out_cap, unsigned long long *counters) {
+    unsigned phase = 0;
     for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < cap; t0 += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i = t0 + threadIdx.x;
         const unsigned long long x = i < cap ? H[i] : SP_EMPTY;
-        const unsigned long long s = block_claim(counters + 3, x != SP_EMPTY);
+        const unsigned long long s = block_claim(phase, counters + 3, x != SP_EMPTY);
         if (x != SP_EMPTY) {
             if (s < out_cap) out[s] = x;
             else atomicOr(counters + 2, 4ull);
@@ -171,12 +172,13 @@ __global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t 
 // from the copy written to `kept` when below >= 0)
 __global__ void k_sp_build(const unsigned long long *__restrict__ A, uint64_t n, unsigned long long *H, int lg,
                            int below, unsigned long long *kept, unsigned long long *counters) {
+    unsigned phase = 0;
     for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < n; t0 += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i = t0 + threadIdx.x;
         const unsigned long long x = i < n ? A[i] : SP_EMPTY;
         const bool want = i < n && !(below >= 0 && (int)(x >> 56) >= below);
         if (kept) {
-            const unsigned long long j = block_claim(counters + 3, want);
+            const unsigned long long j = block_claim(phase, counters + 3, want);
             if (want) kept[j] = x;
         }
         if (!want) continue;

@@ -224,6 +224,7 @@ __device__ __forceinline__ void spw_compact_body(const Lanes &L, const unsigned 
                                                  int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap,
                                                  const unsigned long long *Hold, int lg_old, const uint64_t *okeys,
                                                  uint64_t ostride, const WideStep &P, unsigned long long *counters) {
+    unsigned phase = 0;
     for (uint64_t t0 = L.tile0; t0 < hcap; t0 += L.tstep) {
         const uint64_t s = t0 + threadIdx.x;
         const unsigned long long cur = s < hcap ? __ldcg(H + s) : SPW_EMPTY;
@@ -243,20 +244,18 @@ __device__ __forceinline__ void spw_compact_body(const Lanes &L, const unsigned 
             for (int w = 0; w < W; w++) o[w] = k[w] | P.sel_bits[w];
             chg = v < spw_lookup<W>(Hold, lg_old, okeys, ostride, o);
         }
-        if (P.want_changed) {
-            const unsigned long long j = block_claim(counters + 1, chg);
-            if (chg) {
-                if (j < ccap) {
+        const bool keep = occ && !(P.keep_below >= 0 && (int)v >= P.keep_below);
+        unsigned long long j, jc;
+        block_claim2(phase, counters, keep, P.want_changed ? counters + 1 : nullptr, chg, j, jc);
+        if (chg) {
+            if (jc < ccap) {
 #pragma unroll
-                    for (int w = 0; w < W; w++) ck[(uint64_t)w * ccap + j] = k[w];
-                    cv[j] = (uint8_t)v;
-                } else {
-                    atomicOr(counters + 2, 2ull);
-                }
+                for (int w = 0; w < W; w++) ck[(uint64_t)w * ccap + jc] = k[w];
+                cv[jc] = (uint8_t)v;
+            } else {
+                atomicOr(counters + 2, 2ull);
             }
         }
-        const bool keep = occ && !(P.keep_below >= 0 && (int)v >= P.keep_below);
-        const unsigned long long j = block_claim(counters, keep);
         if (!keep) continue;
         if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
 #pragma unroll
@@ -296,11 +295,12 @@ __device__ __forceinline__ void spw_filter_body(const Lanes &L, const uint64_t *
                                                 const uint8_t *__restrict__ vals, uint64_t n, uint64_t stride,
                                                 int below, uint64_t *nk, uint8_t *nv, uint64_t ncap,
                                                 unsigned long long *H2, int lg2, unsigned long long *counters) {
+    unsigned phase = 0;
     for (uint64_t t0 = L.tile0; t0 < n; t0 += L.tstep) {
         const uint64_t i = t0 + threadIdx.x;
         const uint32_t v = i < n ? vals[i] : 255u;
         const bool want = i < n && !(below >= 0 && (int)v >= below);
-        const unsigned long long j = block_claim(counters, want);
+        const unsigned long long j = block_claim(phase, counters, want);
         if (!want) continue;
         if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
         uint64_t k[W];

@@ -79,29 +79,54 @@ __device__ __forceinline__ unsigned long long agg_inc(unsigned long long *ctr) {
     return g.shfl(base, 0) + g.thread_rank();
 }
 
-// Output slots for the threads of a block that want one, with one atomic per block and call.  Every
-// thread of the block must make the call, the same number of times (want may be false); blockDim.x
-// a multiple of 32, at most 1024.  Returns this thread's slot (meaningless when !want).
-__device__ __forceinline__ unsigned long long block_claim(unsigned long long *ctr, bool want) {
-    __shared__ unsigned s_warp[32];
-    __shared__ unsigned long long s_base;
+// Output slots for the threads of a block that want them, in up to two counters at once, with one
+// atomic per block, call and counter.  Every thread of the block must make the call the same
+// number of times (wants may be false), with the same phase variable (it alternates two sets of
+// shared slots, so that one call needs two barriers); blockDim.x a multiple of 32, at most 1024.
+// ja / jb: this thread's slots (meaningless where it did not want one); cb may be null.
+__device__ __forceinline__ void block_claim2(unsigned &phase, unsigned long long *ca, bool wa, unsigned long long *cb,
+                                             bool wb, unsigned long long &ja, unsigned long long &jb) {
+    __shared__ unsigned s_off[2][2][32];
+    __shared__ unsigned long long s_base[2][2];
+    const unsigned buf = phase & 1u;
+    phase++;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const unsigned bal = __ballot_sync(0xffffffffu, want);
-    if (lane == 0) s_warp[warp] = __popc(bal);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned tot = 0;
-        const unsigned nw = blockDim.x >> 5;
-        for (unsigned i = 0; i < nw; i++) {
-            const unsigned c = s_warp[i];
-            s_warp[i] = tot;
-            tot += c;
-        }
-        s_base = tot ? atomicAdd(ctr, (unsigned long long)tot) : 0ull;
+    const unsigned balA = __ballot_sync(0xffffffffu, wa), balB = __ballot_sync(0xffffffffu, wb);
+    if (lane == 0) {
+        s_off[buf][0][warp] = __popc(balA);
+        s_off[buf][1][warp] = __popc(balB);
     }
     __syncthreads();
-    const unsigned long long j = s_base + s_warp[warp] + __popc(bal & ((1u << lane) - 1u));
+    if (warp == 0) {
+        const unsigned nw = blockDim.x >> 5;
+        const unsigned ca0 = lane < nw ? s_off[buf][0][lane] : 0u, cb0 = lane < nw ? s_off[buf][1][lane] : 0u;
+        unsigned xa = ca0, xb = cb0;
+        for (unsigned off = 1; off < 32; off <<= 1) {
+            const unsigned ya = __shfl_up_sync(0xffffffffu, xa, off), yb = __shfl_up_sync(0xffffffffu, xb, off);
+            if (lane >= off) {
+                xa += ya;
+                xb += yb;
+            }
+        }
+        const unsigned ta = __shfl_sync(0xffffffffu, xa, 31), tb = __shfl_sync(0xffffffffu, xb, 31);
+        if (lane < nw) {
+            s_off[buf][0][lane] = xa - ca0;
+            s_off[buf][1][lane] = xb - cb0;
+        }
+        if (lane == 0) {
+            s_base[buf][0] = ta ? atomicAdd(ca, (unsigned long long)ta) : 0ull;
+            s_base[buf][1] = (tb && cb) ? atomicAdd(cb, (unsigned long long)tb) : 0ull;
+        }
+    }
     __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+    ja = s_base[buf][0] + s_off[buf][0][warp] + __popc(balA & below);
+    jb = s_base[buf][1] + s_off[buf][1][warp] + __popc(balB & below);
+}
+
+__device__ __forceinline__ unsigned long long block_claim(unsigned &phase, unsigned long long *ctr, bool want) {
+    unsigned long long j, unused;
+    block_claim2(phase, ctr, want, nullptr, false, j, unused);
     return j;
 }
 
