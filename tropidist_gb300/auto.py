@@ -85,14 +85,27 @@ def _dtype_for(p):
     return "u16" if sum(w) >= 255 else "u8"
 
 
+_SIDE = {}
+
+
+def _side_stream():
+    """A second stream of the current device for the observables' sweeps (created once)."""
+    import torch
+    dev = torch.cuda.current_device()
+    if dev not in _SIDE:
+        _SIDE[dev] = torch.cuda.Stream(device=dev)
+    return _SIDE[dev]
+
+
 def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
     """Exact distance min over observables i of min{|e| : H e = 0, (L e)_i = 1}; None if no
     logical exists.  MemoryError if a table would exceed max_table_bytes, TimeoutError past the
     deadline (time.monotonic), OverflowError if a distance reaches the table's INF.
 
-    The observables' sweeps are queued on the stream one after another and their final entries
-    copied on the device; the host plans and schedules observable i + 1 while the GPU sweeps
-    observable i, and waits once at the end."""
+    The observables' sweeps are queued on two streams in turn (each with its own pair of tables,
+    while both pairs fit in half the free device memory), so that one sweep's pass boundaries
+    overlap the other's passes; their final entries are copied on the device.  The host plans and
+    schedules observable i + 1 while the GPU sweeps observable i, and waits once at the end."""
     import torch
     from . import device
     device.require_gpu()
@@ -100,11 +113,15 @@ def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
     eb = kernel.entry_bytes(dtype)
     inf = kernel.INF if eb == 1 else kernel.INF16
     per, slots = [], []
-    bufs = [None, None]
+    main = torch.cuda.current_stream()
+    lanes = [main, _side_stream()]
+    bufs = [[None, None], [None, None]]
+    free_bytes = torch.cuda.mem_get_info()[0]
     res = None
+    nrun = 0
     for i, plan in _plans(p, order):
         if deadline is not None and time.monotonic() > deadline:
-            torch.cuda.current_stream().synchronize()
+            torch.cuda.synchronize()
             raise TimeoutError("DP stopped at the time limit")
         if not plan.feasible:
             per.append(None)
@@ -113,17 +130,24 @@ def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
             raise MemoryError("DP table of 2^%d entries exceeds the limit" % plan.peak_bits)
         cp = kernel.CompiledPlan(plan, dtype)
         need = eb << cp.peak_bits
-        if bufs[0] is None or bufs[0].numel() < need:
-            bufs = [device.empty(need), device.empty(need)]
+        lane = nrun % 2 if 4 * need <= free_bytes // 2 else 0
+        nrun += 1
+        if bufs[lane][0] is None or bufs[lane][0].numel() < need:
+            bufs[lane] = [device.empty(need), device.empty(need)]
         if res is None:
             res = torch.zeros(max(1, 2 * p.nobs), dtype=torch.uint8, device="cuda")
-        a, b = bufs
-        cp.execute(a, b)
+        st = lanes[lane]
+        if lane:
+            st.wait_stream(main)
+        a, b = bufs[lane]
+        cp.execute(a, b, stream=st.cuda_stream)
         k = len(per)
-        res[eb * k:eb * k + eb].copy_((b if cp.final_buf else a)[:eb])
+        with torch.cuda.stream(st):
+            res[eb * k:eb * k + eb].copy_((b if cp.final_buf else a)[:eb])
         cp.free()
         per.append(k)
         slots.append(k)
+    main.wait_stream(lanes[1])
     vals = res.cpu().numpy() if res is not None else None
     best = None
     out = []
