@@ -95,6 +95,15 @@ int tg_dense_set_stream_span(int span, int span_sel);
  *     host threads) race: run them one after another. */
 int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, uint64_t table_entries,
                          uint32_t *value, void *stream);
+/* Witness of a small plan in one launch (the traceback of cdist/auto.py:126-182 on the device): one
+ * block applies the ops (HOST int64 [n][3] as tg_dense_plan, entries of eb bytes) keeping every
+ * table of the sweep in `tables` (DEVICE, tg_dense_witness_bytes(ops, n, eb) bytes), then one
+ * thread walks back from the final entry.  out_dev: DEVICE int32 [3 + out_cap] = final entry,
+ * number of used updates, their op indices (last op first), status (0 ok, 1 bad op stream or
+ * storage, 2 the walk lost the path).  tg_dense_witness_bytes returns -1 for a bad op stream. */
+int64_t tg_dense_witness_bytes(const int64_t *ops, int64_t n, int eb);
+int tg_dense_witness_small(const int64_t *ops, int64_t n, int eb, void *tables, uint64_t table_bytes,
+                           int32_t *out_dev, int64_t out_cap, void *stream);
 /* Runs a scheduled plan on HOST buffers with the launch parameters and index arithmetic of the
  * kernels; for checking the scheduler on a machine without a GPU.  Not an evaluator. */
 int tg_debug_emulate_dense(void *plan, void *host_a, void *host_b, void **ckpt_host);

@@ -254,9 +254,10 @@ def test_full_width_schedules_agree():
 
 
 @pytest.mark.parametrize("case", [(60, 120, 14, 3, None), (80, 160, 16, 5, None), (60, 120, 12, 7, (1, 2, 3))])
-def test_witness_traceback_on_device(case):
-    """dp_witness: device checkpoints and a bisection traceback give a logical of the distance's
-    weight (zero syndrome, the observable flipped), small budgets forcing several checkpoints."""
+def test_witness_traceback_on_device(case, monkeypatch):
+    """dp_witness: the one-launch traceback of small plans (every table kept on the device), and
+    device checkpoints with a bisection traceback (small budgets forcing several checkpoints), give
+    a logical of the distance's weight (zero syndrome, the observable flipped)."""
     from tropidist_gb300 import auto, synth
     from tropidist_gb300.problem import verify_witness
     m, n, win, seed, wts = case
@@ -267,7 +268,8 @@ def test_witness_traceback_on_device(case):
         p.weights = [rng.choice(wts) for _ in range(p.ncols)]
     order = list(range(p.ncols))
     best, per = auto.dp_distance(p, order)
-    for budget in (None, 1 << 16):
+    for small, budget in ((True, None), (False, None), (False, 1 << 16)):
+        monkeypatch.setattr(auto, "SMALL_WITNESS_BYTES", 256 << 20 if small else 0)
         r = auto.dp_witness(p, order, budget_bytes=budget, leaf=4)
         assert r["distance"] == best
         cols = r["witness"]

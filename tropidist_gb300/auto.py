@@ -173,6 +173,43 @@ def _widths(ops):
     return out
 
 
+SMALL_WITNESS_BYTES = 256 << 20      # every table of a sweep kept on the device up to this size
+
+
+def _witness_small(cands, order, eb, inf):
+    """dp_witness for plans whose tables all fit SMALL_WITNESS_BYTES together: per observable one
+    launch that runs the sweep keeping every table and walks back on the device
+    (tg_dense_witness_small); None when a plan is larger."""
+    import numpy as np
+    import torch
+    from . import _lib, device
+    L = _lib.lib()
+    encs = [np.ascontiguousarray(plan.encode(), dtype=np.int64) for _, plan in cands]
+    sizes = [int(L.tg_dense_witness_bytes(e.ctypes.data if len(e) else None, len(e), eb)) for e in encs]
+    if any(sz < 0 or sz > SMALL_WITNESS_BYTES for sz in sizes):
+        return None
+    best = None
+    for (i, plan), enc, sz in zip(cands, encs, sizes):
+        nupd = int((enc[:, 0] == trellis.OP_UPDATE).sum()) if len(enc) else 0
+        tabs = torch.empty(max(sz, 1), dtype=torch.uint8, device="cuda")
+        out = torch.empty(3 + nupd, dtype=torch.int32, device="cuda")
+        _lib.check(L.tg_dense_witness_small(enc.ctypes.data if len(enc) else None, len(enc), eb, tabs.data_ptr(),
+                                            sz, out.data_ptr(), nupd, device.stream_ptr()))
+        o = out.cpu().numpy()
+        status = int(o[2 + nupd])
+        if status == 1:
+            raise ValueError("witness: op stream out of range")
+        if status == 2:
+            raise AssertionError("traceback lost the path")
+        v = kernel.final_value(int(o[0]) & (0xFF if eb == 1 else 0xFFFF), inf)
+        if best is None or v < best[0]:
+            best = (v, i, plan, o[2:2 + int(o[1])].tolist())
+    value, i, plan, ks = best
+    upd_index = np.cumsum(plan.encode()[:, 0] == trellis.OP_UPDATE) - 1
+    used = [order[plan.columns[int(upd_index[k])]] for k in ks]
+    return {"distance": value, "witness": sorted(used), "observable": i}
+
+
 def dp_witness(p, order, obs=None, dtype=None, budget_bytes=None, leaf=16):
     """Columns (problem indices) of a minimum-weight solution, with its weight and observable:
     {"distance", "witness", "observable"} (cdist/auto.py:126-182), or None if no logical exists.
@@ -183,19 +220,23 @@ def dp_witness(p, order, obs=None, dtype=None, budget_bytes=None, leaf=16):
     checkpoints is walked back by bisection — the table at the segment's midpoint is recomputed
     from its start by a plan that begins with that table (tg_dense_plan_from), the second half is
     traced first — so only O(log segment) tables exist at once.  A leaf of at most `leaf` ops is
-    recomputed with a table after every op; the walk reads two entries per update op."""
+    recomputed with a table after every op; the walk reads two entries per update op.  Plans whose
+    tables all fit SMALL_WITNESS_BYTES together take one launch per observable instead (every table
+    kept, the walk back on the device)."""
     import torch
     from . import device
     dtype = dtype or _dtype_for(p)
     eb = kernel.entry_bytes(dtype)
     dt = torch.uint8 if eb == 1 else torch.int16
     inf = kernel.INF if eb == 1 else 65535
+    cands = [(i, plan) for i, plan in _plans(p, order) if (obs is None or i == obs) and plan.feasible]
+    if not cands:
+        return None
+    small = _witness_small(cands, order, eb, inf)
+    if small is not None:
+        return small
     best = None
-    for i, plan in _plans(p, order):
-        if obs is not None and i != obs:
-            continue
-        if not plan.feasible:
-            continue
+    for i, plan in cands:
         v, _ = kernel.run_plan(plan, dtype=dtype)
         if v is not None and (best is None or v < best[0]):
             best = (v, i, plan)

@@ -1529,6 +1529,95 @@ static int noalloc_scratch(uint8_t **out) {
     return TG_OK;
 }
 
+
+// ------------------------------------------------------------------ witness of a small plan
+// One block applies the ops one after another, keeping every table of the sweep (T_0 = {0: 0},
+// T_k+1 = op_k(T_k)) one after another in `tabs`; then one thread walks back from the final entry:
+// a select restores its bit, an update whose table before it does not hold the current value at
+// the current state was used (the state moves by its mask, the value drops by its weight), the
+// traceback of the reference's auto.py.  out: [0] final entry, [1] number of used updates, [2..]
+// their op indices (last op first), [2 + out_cap] status (0 ok, 1 storage or op out of range, 2
+// traceback lost the path).
+template <typename E>
+__global__ void __launch_bounds__(1024) k_witness_small(const int64_t *ops, int64_t n, E *tabs, uint64_t cap,
+                                                        int32_t *out, int64_t out_cap) {
+    constexpr uint32_t INF = Entry<E>::INF;
+    const unsigned tid = threadIdx.x, NT = blockDim.x;
+    uint64_t off = 0;
+    int w = 0;
+    if (tid == 0) tabs[0] = 0;
+    __syncthreads();
+    for (int64_t k = 0; k < n; k++) {
+        const int code = (int)ops[3 * k];
+        const uint64_t a = (uint64_t)ops[3 * k + 1];
+        const int64_t b = ops[3 * k + 2];
+        const int w2 = code == 0 ? w + 1 : code == 2 ? w - 1 : w;
+        const uint64_t m = 1ull << w, m2 = 1ull << (w2 < 0 ? 0 : w2);
+        const bool bad = w2 < 0 || w2 > 30 || off + m + m2 > cap || (code == 1 && (a >> w)) ||
+                         (code == 2 && (a >= (uint64_t)w || b < 0 || b > 1)) || code < 0 || code > 2 ||
+                         (code == 1 && (b < 1 || b > (int64_t)INF));
+        if (bad) {
+            if (tid == 0) out[2 + out_cap] = 1;
+            return;
+        }
+        const E *S = tabs + off;
+        E *D = tabs + off + m;
+        if (code == 0) {
+            for (uint64_t i = tid; i < m; i += NT) {
+                D[i] = S[i];
+                D[i + m] = (E)INF;
+            }
+        } else if (code == 1) {
+            for (uint64_t i = tid; i < m; i += NT) {
+                const uint32_t x = S[i], y = S[i ^ a];
+                const uint32_t c = y == INF ? INF : min(y + (uint32_t)b, INF);
+                D[i] = (E)min(x, c);
+            }
+        } else {
+            const uint64_t low = (1ull << a) - 1ull;
+            for (uint64_t i = tid; i < m2; i += NT)
+                D[i] = S[((i & ~low) << 1) | ((uint64_t)b << a) | (i & low)];
+        }
+        off += m;
+        w = w2;
+        __syncthreads();
+    }
+    if (tid != 0) return;
+    const uint32_t value = tabs[off];
+    out[0] = (int32_t)value;
+    int64_t used = 0;
+    int status = 0;
+    if (w == 0 && value != INF) {
+        uint64_t st = 0;
+        uint32_t v = value;
+        for (int64_t k = n - 1; k >= 0; k--) {
+            const int code = (int)ops[3 * k];
+            const uint64_t a = (uint64_t)ops[3 * k + 1];
+            const int64_t b = ops[3 * k + 2];
+            const int wb = code == 0 ? w - 1 : code == 2 ? w + 1 : w;      // width before op k
+            off -= 1ull << wb;
+            if (code == 2) {
+                const uint64_t low = (1ull << a) - 1ull;
+                st = ((st & ~low) << 1) | ((uint64_t)b << a) | (st & low);
+            } else if (code == 0) {
+                if (st >> wb) { status = 2; break; }
+            } else if (tabs[off + st] != v) {
+                st ^= a;
+                v -= (uint32_t)b;
+                if (tabs[off + st] != v) { status = 2; break; }
+                if (used < out_cap) out[2 + used] = (int32_t)k;
+                used++;
+            }
+            w = wb;
+        }
+        if (!status && (st != 0 || v != 0)) status = 2;
+    } else if (w != 0) {
+        status = 1;
+    }
+    out[1] = (int32_t)used;
+    out[2 + out_cap] = status;
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -1798,4 +1887,54 @@ int tg_dense_set_tuning(int dmax8, int dmax16, int sweep_bits8, int sweep_bits16
     return TG_OK;
 }
 
+
+// bytes of every table of a sweep (T_0 .. T_n), for tg_dense_witness_small; -1 on a bad op stream
+int64_t tg_dense_witness_bytes(const int64_t *ops, int64_t n, int eb) {
+    if ((eb != 1 && eb != 2) || n < 0 || (n && !ops)) return -1;
+    int64_t w = 0, tot = 1;
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t code = ops[3 * k];
+        w += code == 0 ? 1 : code == 2 ? -1 : 0;
+        if (w < 0 || w > 30) return -1;
+        tot += 1ll << w;
+    }
+    return tot * eb;
+}
+
+// The witness of a small plan in one launch (ops: HOST int64 [n][3] as tg_dense_plan): every table
+// of the sweep is kept in `tables` (DEVICE, tg_dense_witness_bytes bytes), one block applies the
+// ops and one thread walks back.  out_dev: DEVICE int32 [3 + out_cap] = final entry, number of used
+// updates, their op indices (last op first), then a status (0 ok, 1 bad op stream or storage, 2
+// the walk lost the path).
+int tg_dense_witness_small(const int64_t *ops, int64_t n, int eb, void *tables, uint64_t table_bytes,
+                           int32_t *out_dev, int64_t out_cap, void *stream) {
+    if ((eb != 1 && eb != 2) || n < 0 || (n && !ops) || !tables || !out_dev || out_cap < 0)
+        return set_error(TG_ERR_ARG, "bad witness arguments");
+    const int64_t need = tg_dense_witness_bytes(ops, n, eb);
+    if (need < 0) return set_error(TG_ERR_ARG, "bad op stream");
+    if ((uint64_t)need > table_bytes) return set_error(TG_ERR_TOO_BIG, "witness tables larger than the buffer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    static thread_local int64_t *dops = nullptr;
+    static thread_local int64_t dops_n = 0;
+    if (dops_n < n) {
+        if (dops) cudaFree(dops);
+        dops = nullptr;
+        dops_n = 0;
+        if (cudaMalloc(&dops, 24 * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(TG_ERR_NOMEM, "witness op stream");
+        }
+        dops_n = n;
+    }
+    int e = TG_OK;
+    if (n) e = cuda_check(cudaMemcpyAsync(dops, ops, 24 * (size_t)n, cudaMemcpyHostToDevice, st), "witness ops");
+    if (!e) e = cuda_check(cudaMemsetAsync(out_dev, 0, 4 * (size_t)(3 + out_cap), st), "witness out");
+    if (e) return e;
+    const uint64_t cap = (uint64_t)need / eb;
+    if (eb == 1)
+        k_witness_small<uint8_t><<<1, 1024, 0, st>>>(dops, n, static_cast<uint8_t *>(tables), cap, out_dev, out_cap);
+    else
+        k_witness_small<uint16_t><<<1, 1024, 0, st>>>(dops, n, static_cast<uint16_t *>(tables), cap, out_dev, out_cap);
+    return cuda_check(cudaGetLastError(), "witness kernel");
+}
 }  // extern "C"
