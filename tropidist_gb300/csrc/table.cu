@@ -32,6 +32,7 @@ struct TableHandle {
     unsigned long long *count;     // device counter of entries
     int64_t entries;
     int k;
+    size_t keys_bytes, cost_bytes;  // allocated sizes (a reused buffer may be larger)
 };
 
 __device__ __forceinline__ uint64_t tb_compact_key(uint64_t zl, uint64_t lg) {
@@ -147,6 +148,56 @@ __global__ void k_tb_lookup(TableHandle T, uint64_t m, const unsigned long long 
     }
 }
 
+// One released allocation of each kind per host thread, handed to the next request that fits: a
+// search creates and frees a table and its probe buffers per call, and cudaMalloc, cudaMallocHost,
+// cudaFreeHost and the device-synchronizing cudaFree cost tens to hundreds of microseconds each.
+struct Reuse {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+enum { RU_KEYS, RU_COST, RU_COUNT, RU_BUILD, RU_DIN, RU_DOUT, RU_HIN, RU_HOUT, RU_N };
+static thread_local Reuse g_reuse[RU_N];
+
+static bool ru_host(int kind) { return kind == RU_HIN || kind == RU_HOUT; }
+
+static void ru_release(int kind, void *p) {
+    if (ru_host(kind)) cudaFreeHost(p);
+    else cudaFree(p);
+}
+
+// a buffer of at least `bytes` (*got: its size), from the cache or newly allocated; null on failure
+static void *ru_take(int kind, size_t bytes, size_t *got) {
+    Reuse &r = g_reuse[kind];
+    if (r.p && r.bytes >= bytes) {
+        void *p = r.p;
+        *got = r.bytes;
+        r.p = nullptr;
+        r.bytes = 0;
+        return p;
+    }
+    void *p = nullptr;
+    const cudaError_t e = ru_host(kind) ? cudaMallocHost(&p, bytes) : cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    *got = bytes;
+    return p;
+}
+
+// back to the cache (the larger of the two buffers stays)
+static void ru_give(int kind, void *p, size_t bytes) {
+    if (!p) return;
+    Reuse &r = g_reuse[kind];
+    if (r.p && r.bytes >= bytes) {
+        ru_release(kind, p);
+        return;
+    }
+    if (r.p) ru_release(kind, r.p);
+    r.p = p;
+    r.bytes = bytes;
+}
+
 static unsigned tb_grid(uint64_t items) {
     uint64_t g = (items + 255) / 256;
     uint64_t cap = (uint64_t)sm_count() * 16;
@@ -173,12 +224,14 @@ void *tg_tab_create(int log2slots, int wide, int *status) {
         T->wide = wide ? 1 : 0;
         T->slots = 1ull << log2slots;
         const uint64_t nwords = T->slots * (wide ? 2 : 1);
-        if (cudaMalloc(&T->keys, nwords * 8) != cudaSuccess || cudaMalloc(&T->cost, T->slots) != cudaSuccess ||
-            cudaMalloc(&T->count, 8) != cudaSuccess) {
-            cudaGetLastError();
-            if (T->keys) cudaFree(T->keys);
-            if (T->cost) cudaFree(T->cost);
-            if (T->count) cudaFree(T->count);
+        size_t cb = 0;
+        T->keys = static_cast<unsigned long long *>(ru_take(RU_KEYS, nwords * 8, &T->keys_bytes));
+        T->cost = static_cast<uint8_t *>(ru_take(RU_COST, T->slots, &T->cost_bytes));
+        T->count = static_cast<unsigned long long *>(ru_take(RU_COUNT, 8, &cb));
+        if (!T->keys || !T->cost || !T->count) {
+            ru_give(RU_KEYS, T->keys, T->keys_bytes);
+            ru_give(RU_COST, T->cost, T->cost_bytes);
+            ru_give(RU_COUNT, T->count, 8);
             delete T;
             T = nullptr;
             st = set_error(TG_ERR_NOMEM, "device table allocation failed");
@@ -195,9 +248,10 @@ void *tg_tab_create(int log2slots, int wide, int *status) {
 void tg_tab_free(void *p) {
     TableHandle *T = static_cast<TableHandle *>(p);
     if (!T) return;
-    cudaFree(T->keys);
-    cudaFree(T->cost);
-    cudaFree(T->count);
+    cudaDeviceSynchronize();        // kernels still reading the table finish before it is reused
+    ru_give(RU_KEYS, T->keys, T->keys_bytes);
+    ru_give(RU_COST, T->cost, T->cost_bytes);
+    ru_give(RU_COUNT, T->count, 8);
     delete T;
 }
 
@@ -221,12 +275,10 @@ int tg_tab_build(void *p, int n, const uint64_t *zh, const uint64_t *zl, const u
             binom[(uint64_t)c * (TB_MAXK + 1) + j] = binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j - 1] +
                                                      (j <= c - 1 ? binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j] : 0ull);
     }
-    unsigned long long *d = nullptr;
     const size_t nb = binom.size() * 8, nh = (size_t)std::max(n, 1) * 8;
-    if (cudaMalloc(&d, nb + 3 * nh + 8) != cudaSuccess) {
-        cudaGetLastError();
-        return set_error(TG_ERR_NOMEM, "device buffers for the build");
-    }
+    size_t dbytes = 0;
+    unsigned long long *d = static_cast<unsigned long long *>(ru_take(RU_BUILD, nb + 3 * nh + 8, &dbytes));
+    if (!d) return set_error(TG_ERR_NOMEM, "device buffers for the build");
     unsigned long long *dbin = d, *dzh = d + binom.size(), *dzl = dzh + std::max(n, 1), *dlg = dzl + std::max(n, 1);
     unsigned long long *derr = dlg + std::max(n, 1);
     int e = cuda_check(cudaMemcpy(dbin, binom.data(), nb, cudaMemcpyHostToDevice), "binomials");
@@ -242,7 +294,7 @@ int tg_tab_build(void *p, int n, const uint64_t *zh, const uint64_t *zl, const u
     unsigned long long err = 0, cnt = 0;
     if (!e) e = cuda_check(cudaMemcpy(&err, derr, 8, cudaMemcpyDeviceToHost), "flag read");
     if (!e) e = cuda_check(cudaMemcpy(&cnt, T->count, 8, cudaMemcpyDeviceToHost), "count read");
-    cudaFree(d);
+    ru_give(RU_BUILD, d, dbytes);
     if (e) return e;
     if (err) return set_error(TG_ERR_TOO_BIG, "completion table full");
     T->entries = (int64_t)cnt;
@@ -269,16 +321,19 @@ struct NativeProbe {
     int64_t cap;                   // probes per round trip
     uint8_t *h_in, *d_in;          // zh, zl, lg (8 bytes each) and R (4 bytes): 28 bytes per probe
     int32_t *h_out, *d_out;
+    size_t b_hin, b_din, b_hout, b_dout;
     cudaStream_t st;
 };
 
+static thread_local cudaStream_t g_probe_stream = nullptr;    // one probe stream per host thread, kept
+
 static void probe_release(NativeProbe *P) {
     if (!P) return;
-    if (P->h_in) cudaFreeHost(P->h_in);
-    if (P->h_out) cudaFreeHost(P->h_out);
-    if (P->d_in) cudaFree(P->d_in);
-    if (P->d_out) cudaFree(P->d_out);
-    if (P->st) cudaStreamDestroy(P->st);
+    if (P->st) cudaStreamSynchronize(P->st);
+    ru_give(RU_HIN, P->h_in, P->b_hin);
+    ru_give(RU_HOUT, P->h_out, P->b_hout);
+    ru_give(RU_DIN, P->d_in, P->b_din);
+    ru_give(RU_DOUT, P->d_out, P->b_dout);
     delete P;
 }
 
@@ -296,11 +351,14 @@ void *tg_tab_probe_create(void *table, int64_t cap, int *status) {
         memset(P, 0, sizeof(*P));
         P->T = static_cast<TableHandle *>(table);
         P->cap = cap;
-        st = cuda_check(cudaMallocHost((void **)&P->h_in, 28 * (size_t)cap), "probe staging");
-        if (!st) st = cuda_check(cudaMallocHost((void **)&P->h_out, 4 * (size_t)cap), "probe staging");
-        if (!st) st = cuda_check(cudaMalloc((void **)&P->d_in, 28 * (size_t)cap), "probe buffers");
-        if (!st) st = cuda_check(cudaMalloc((void **)&P->d_out, 4 * (size_t)cap), "probe buffers");
-        if (!st) st = cuda_check(cudaStreamCreateWithFlags(&P->st, cudaStreamNonBlocking), "probe stream");
+        P->h_in = static_cast<uint8_t *>(ru_take(RU_HIN, 28 * (size_t)cap, &P->b_hin));
+        P->h_out = static_cast<int32_t *>(ru_take(RU_HOUT, 4 * (size_t)cap, &P->b_hout));
+        P->d_in = static_cast<uint8_t *>(ru_take(RU_DIN, 28 * (size_t)cap, &P->b_din));
+        P->d_out = static_cast<int32_t *>(ru_take(RU_DOUT, 4 * (size_t)cap, &P->b_dout));
+        if (!g_probe_stream) st = cuda_check(cudaStreamCreateWithFlags(&g_probe_stream, cudaStreamNonBlocking),
+                                             "probe stream");
+        P->st = g_probe_stream;
+        if (!st && (!P->h_in || !P->h_out || !P->d_in || !P->d_out)) st = set_error(TG_ERR_NOMEM, "probe buffers");
         if (st) {
             probe_release(P);
             P = nullptr;
