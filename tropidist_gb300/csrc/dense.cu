@@ -940,11 +940,19 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
 
         return TG_OK;
     };
+    // the first checkpoint after each op (nops when none)
+    std::vector<int64_t> next_ckpt(nops + 2, nops);
+    for (int64_t k = nops - 1; k >= 0; k--) next_ckpt[k] = is_ckpt[k + 1] ? k + 1 : next_ckpt[k + 1];
+    // scratch of the pass-growing loop (assigned per candidate op, no allocation once grown)
+    std::vector<int> t2, cur2, need;
+    std::vector<uint64_t> b2;
+    t2.reserve(64);
+    cur2.reserve(64);
+    need.reserve(64);
+    b2.reserve(64);
     while (i < nops) {
         const int w_in = (int)canon.size();
-        int64_t limit = nops;
-        for (int64_t k = i + 1; k <= nops; k++)
-            if (is_ckpt[k]) { limit = k; break; }
+        const int64_t limit = next_ckpt[i];
         Seg S;
         S.w_in = w_in;
         if (sweep_next(w_in, i) && phys != canon) {
@@ -998,14 +1006,15 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
             int nsel_in = 0;
             while (j < limit && nupd < FP_MAXU) {
                 const HostOp &o = hops[j];
-                std::vector<int> t2 = touched, cur2 = cur;
+                t2.assign(touched.begin(), touched.end());
+                cur2.assign(cur.begin(), cur.end());
                 if (o.code == 0) t2.push_back(RI.exp_row[j]);
                 else if (o.code == 1) {
                     for (int r : RI.upd_rows[j]) if (!has_row(t2, r)) t2.push_back(r);
                 } else if (!has_row(t2, RI.sel_row[j])) t2.push_back(RI.sel_row[j]);
                 apply_canon(j, cur2);
                 if ((int)cur2.size() < CB) break;
-                std::vector<int> need = t2;
+                need.assign(t2.begin(), t2.end());
                 for (int r : inchunk) if (!has_row(need, r)) need.push_back(r);
                 if (must_canon(j + 1, cur2)) {
                     for (int p = 0; p < CB; p++) if (!has_row(need, cur2[p])) need.push_back(cur2[p]);
@@ -1014,7 +1023,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                 }
                 if ((int)need.size() > DMAX) break;
                 if (srule) {
-                    std::vector<uint64_t> b2 = sbasis;
+                    b2.assign(sbasis.begin(), sbasis.end());
                     int ns2 = nsel_in;
                     if (o.code == 1) {
                         uint64_t v = 0;
