@@ -67,7 +67,7 @@ def test_wide_frontier_sweeps_match_oracle_cut_by_cut():
     assert rec["gpu"] == rec["oracle"]
 
 
-@pytest.mark.parametrize("words", [1, 2])
+@pytest.mark.parametrize("words", [1, 2, 8])
 def test_wide_tables_reproduce_reference_queries(words):
     """One-word problems through the multi-word device tables: the reference's values and peaks."""
     from tropidist_gb300 import sparse_dp
