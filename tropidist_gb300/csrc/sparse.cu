@@ -156,14 +156,27 @@ __global__ void k_sp_step(const __grid_constant__ StepParams P, const __grid_con
 // the occupied slots of an index into an array; counters[3] = states written
 __global__ void k_sp_compact(const unsigned long long *__restrict__ H, uint64_t cap, unsigned long long *out,
                              uint64_t out_cap, unsigned long long *counters) {
+    // tiles of SPC_PER slots per thread: output positions are claimed once per block and tile
+    constexpr int SPC_PER = 8;
     unsigned phase = 0;
-    for (uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x; t0 < cap; t0 += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t i = t0 + threadIdx.x;
-        const unsigned long long x = i < cap ? H[i] : SP_EMPTY;
-        const unsigned long long s = block_claim(phase, counters + 3, x != SP_EMPTY);
-        if (x != SP_EMPTY) {
-            if (s < out_cap) out[s] = x;
+    const uint64_t tile = (uint64_t)blockDim.x * SPC_PER;
+    for (uint64_t t0 = blockIdx.x * tile; t0 < cap; t0 += (uint64_t)gridDim.x * tile) {
+        unsigned long long x[SPC_PER];
+        unsigned cnt = 0;
+#pragma unroll
+        for (int q = 0; q < SPC_PER; q++) {
+            const uint64_t i = t0 + (uint64_t)q * blockDim.x + threadIdx.x;
+            x[q] = i < cap ? H[i] : SP_EMPTY;
+            cnt += x[q] != SP_EMPTY;
+        }
+        unsigned long long s, unused;
+        block_claim2_n(phase, counters + 3, cnt, nullptr, 0u, s, unused);
+#pragma unroll
+        for (int q = 0; q < SPC_PER; q++) {
+            if (x[q] == SP_EMPTY) continue;
+            if (s < out_cap) out[s] = x[q];
             else atomicOr(counters + 2, 4ull);
+            s++;
         }
     }
 }
@@ -752,7 +765,7 @@ int tg_sp_step(const void *A, uint64_t n, const void *Hold, int lg_old, void *Hn
     if (n) k_sp_step<<<sp_grid(n), 256, 0, st>>>(P, B, (const unsigned long long *)A, n, (const unsigned long long *)Hold,
                                                 (unsigned long long *)Hnew, (unsigned long long *)changed, changed_cap,
                                                 (unsigned long long *)counters);
-    k_sp_compact<<<sp_grid(capn), 256, 0, st>>>((const unsigned long long *)Hnew, capn, (unsigned long long *)Anew,
+    k_sp_compact<<<sp_grid((capn + 7) / 8), 256, 0, st>>>((const unsigned long long *)Hnew, capn, (unsigned long long *)Anew,
                                                 anew_cap, (unsigned long long *)counters);
     return cuda_check(cudaGetLastError(), "sparse step");
 }
@@ -915,7 +928,7 @@ int tg_sp_walk(int nsteps, const int64_t *spec, const uint64_t *masks, const int
         const uint64_t capn = 1ull << lgn;
         k_sp_fill<<<sp_grid(capn), 256, 0, st>>>(W.idx[os], capn);
         if (n) k_sp_step<<<sp_grid(n), 256, 0, st>>>(P, B, curA, n, curH, W.idx[os], W.changed, W.cap_n, cnt);
-        k_sp_compact<<<sp_grid(capn), 256, 0, st>>>(W.idx[os], capn, W.arr[os], W.cap_n, cnt);
+        k_sp_compact<<<sp_grid((capn + 7) / 8), 256, 0, st>>>(W.idx[os], capn, W.arr[os], W.cap_n, cnt);
         e = cuda_check(cudaGetLastError(), "walk step");
         if (!e) e = read_counters();
         if (e) return e;

@@ -35,6 +35,7 @@ namespace tg {
 #define SPW_QW 720720ll
 #define SPW_MAXW 8
 #define SPW_MAXCLS 32
+#define SPW_PER 4               // slots per thread in a tile of a compaction or a filter
 
 struct WideBound {
     int on, ncls, K, pad;
@@ -224,52 +225,70 @@ __device__ __forceinline__ void spw_compact_body(const Lanes &L, const unsigned 
                                                  int lg2, uint64_t *ck, uint8_t *cv, uint64_t ccap,
                                                  const unsigned long long *Hold, int lg_old, const uint64_t *okeys,
                                                  uint64_t ostride, const WideStep &P, unsigned long long *counters) {
+    // tiles of SPW_PER slots per thread: output positions are claimed once per block and tile;
+    // the key words of a slot are read when its flags are decided and again when it is written
     unsigned phase = 0;
-    for (uint64_t t0 = L.tile0; t0 < hcap; t0 += L.tstep) {
-        const uint64_t s = t0 + threadIdx.x;
-        const unsigned long long cur = s < hcap ? __ldcg(H + s) : SPW_EMPTY;
-        const bool occ = cur != SPW_EMPTY;
-        const uint64_t e = cur & SPW_IDX;
-        const uint32_t v = (uint32_t)(cur >> 56);
-        uint64_t k[W];
+    const uint32_t mask2 = (1u << lg2) - 1u;
+    for (uint64_t t0 = L.tile0 * SPW_PER; t0 < hcap; t0 += L.tstep * SPW_PER) {
+        unsigned long long cw[SPW_PER];
+        unsigned kmask = 0, cmask = 0;
 #pragma unroll
-        for (int w = 0; w < W; w++) k[w] = 0;
-        if (occ) spw_load<W>(ek, estride, e, k);
-        bool chg = false;
-        if (occ && P.want_changed && (e & 1ull)) {
-            // a candidate won: changed unless the old table had this key (closing bits restored)
-            // with a value <= v
-            uint64_t o[W];
+        for (int q = 0; q < SPW_PER; q++) {
+            const uint64_t s = t0 + (uint64_t)q * blockDim.x + threadIdx.x;
+            const unsigned long long cur = s < hcap ? __ldcg(H + s) : SPW_EMPTY;
+            cw[q] = cur;
+            if (cur == SPW_EMPTY) continue;
+            const uint64_t e = cur & SPW_IDX;
+            const uint32_t v = (uint32_t)(cur >> 56);
+            if (!(P.keep_below >= 0 && (int)v >= P.keep_below)) kmask |= 1u << q;
+            if (P.want_changed && (e & 1ull)) {
+                // a candidate won: changed unless the old table had this key (closing bits
+                // restored) with a value <= v
+                uint64_t o[W];
+                spw_load<W>(ek, estride, e, o);
 #pragma unroll
-            for (int w = 0; w < W; w++) o[w] = k[w] | P.sel_bits[w];
-            chg = v < spw_lookup<W>(Hold, lg_old, okeys, ostride, o);
-        }
-        const bool keep = occ && !(P.keep_below >= 0 && (int)v >= P.keep_below);
-        unsigned long long j, jc;
-        block_claim2(phase, counters, keep, P.want_changed ? counters + 1 : nullptr, chg, j, jc);
-        if (chg) {
-            if (jc < ccap) {
-#pragma unroll
-                for (int w = 0; w < W; w++) ck[(uint64_t)w * ccap + jc] = k[w];
-                cv[jc] = (uint8_t)v;
-            } else {
-                atomicOr(counters + 2, 2ull);
+                for (int w = 0; w < W; w++) o[w] |= P.sel_bits[w];
+                if (v < spw_lookup<W>(Hold, lg_old, okeys, ostride, o)) cmask |= 1u << q;
             }
         }
-        if (!keep) continue;
-        if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
+        unsigned long long j, jc;
+        block_claim2_n(phase, counters, __popc(kmask), P.want_changed ? counters + 1 : nullptr, __popc(cmask), j, jc);
 #pragma unroll
-        for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
-        nv[j] = (uint8_t)v;
-        // the keys are distinct: claim the first empty slot
-        const uint32_t mask = (1u << lg2) - 1u;
-        uint32_t t = spw_slot<W>(k, lg2);
-        uint32_t probe = 0;
-        for (; probe <= mask; probe++) {
-            if (atomicCAS(H2 + t, SPW_EMPTY, ((unsigned long long)v << 56) | j) == SPW_EMPTY) break;
-            t = (t + 1) & mask;
+        for (int q = 0; q < SPW_PER; q++) {
+            if (!(((kmask | cmask) >> q) & 1u)) continue;
+            const uint64_t e = cw[q] & SPW_IDX;
+            const uint32_t v = (uint32_t)(cw[q] >> 56);
+            uint64_t k[W];
+            spw_load<W>(ek, estride, e, k);
+            if ((cmask >> q) & 1u) {
+                if (jc < ccap) {
+#pragma unroll
+                    for (int w = 0; w < W; w++) ck[(uint64_t)w * ccap + jc] = k[w];
+                    cv[jc] = (uint8_t)v;
+                } else {
+                    atomicOr(counters + 2, 2ull);
+                }
+                jc++;
+            }
+            if (!((kmask >> q) & 1u)) continue;
+            if (j >= ncap) {
+                atomicOr(counters + 2, 4ull);
+                j++;
+                continue;
+            }
+#pragma unroll
+            for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
+            nv[j] = (uint8_t)v;
+            // the keys are distinct: claim the first empty slot
+            uint32_t t = spw_slot<W>(k, lg2);
+            uint32_t probe = 0;
+            for (; probe <= mask2; probe++) {
+                if (atomicCAS(H2 + t, SPW_EMPTY, ((unsigned long long)v << 56) | j) == SPW_EMPTY) break;
+                t = (t + 1) & mask2;
+            }
+            if (probe > mask2) atomicOr(counters + 2, 1ull);
+            j++;
         }
-        if (probe > mask) atomicOr(counters + 2, 1ull);
     }
 }
 
@@ -296,26 +315,40 @@ __device__ __forceinline__ void spw_filter_body(const Lanes &L, const uint64_t *
                                                 int below, uint64_t *nk, uint8_t *nv, uint64_t ncap,
                                                 unsigned long long *H2, int lg2, unsigned long long *counters) {
     unsigned phase = 0;
-    for (uint64_t t0 = L.tile0; t0 < n; t0 += L.tstep) {
-        const uint64_t i = t0 + threadIdx.x;
-        const uint32_t v = i < n ? vals[i] : 255u;
-        const bool want = i < n && !(below >= 0 && (int)v >= below);
-        const unsigned long long j = block_claim(phase, counters, want);
-        if (!want) continue;
-        if (j >= ncap) { atomicOr(counters + 2, 4ull); continue; }
-        uint64_t k[W];
-        spw_load<W>(keys, stride, i, k);
+    const uint32_t mask2 = (1u << lg2) - 1u;
+    for (uint64_t t0 = L.tile0 * SPW_PER; t0 < n; t0 += L.tstep * SPW_PER) {
+        unsigned wmask = 0;
 #pragma unroll
-        for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
-        nv[j] = (uint8_t)v;
-        const uint32_t mask = (1u << lg2) - 1u;
-        uint32_t t = spw_slot<W>(k, lg2);
-        uint32_t probe = 0;
-        for (; probe <= mask; probe++) {
-            if (atomicCAS(H2 + t, SPW_EMPTY, ((unsigned long long)v << 56) | j) == SPW_EMPTY) break;
-            t = (t + 1) & mask;
+        for (int q = 0; q < SPW_PER; q++) {
+            const uint64_t i = t0 + (uint64_t)q * blockDim.x + threadIdx.x;
+            if (i < n && !(below >= 0 && (int)vals[i] >= below)) wmask |= 1u << q;
         }
-        if (probe > mask) atomicOr(counters + 2, 1ull);
+        unsigned long long j, unused;
+        block_claim2_n(phase, counters, __popc(wmask), nullptr, 0u, j, unused);
+#pragma unroll
+        for (int q = 0; q < SPW_PER; q++) {
+            if (!((wmask >> q) & 1u)) continue;
+            const uint64_t i = t0 + (uint64_t)q * blockDim.x + threadIdx.x;
+            if (j >= ncap) {
+                atomicOr(counters + 2, 4ull);
+                j++;
+                continue;
+            }
+            const uint32_t v = vals[i];
+            uint64_t k[W];
+            spw_load<W>(keys, stride, i, k);
+#pragma unroll
+            for (int w = 0; w < W; w++) nk[(uint64_t)w * ncap + j] = k[w];
+            nv[j] = (uint8_t)v;
+            uint32_t t = spw_slot<W>(k, lg2);
+            uint32_t probe = 0;
+            for (; probe <= mask2; probe++) {
+                if (atomicCAS(H2 + t, SPW_EMPTY, ((unsigned long long)v << 56) | j) == SPW_EMPTY) break;
+                t = (t + 1) & mask2;
+            }
+            if (probe > mask2) atomicOr(counters + 2, 1ull);
+            j++;
+        }
     }
 }
 

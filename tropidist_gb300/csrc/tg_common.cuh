@@ -124,6 +124,56 @@ __device__ __forceinline__ void block_claim2(unsigned &phase, unsigned long long
     jb = s_base[buf][1] + s_off[buf][1][warp] + __popc(balB & below);
 }
 
+// block_claim2 for counts: this thread wants na slots of counter ca and nb of cb (an inclusive
+// scan over the warp, then over the warps); ja / jb: the first of its slots.  Same rules as
+// block_claim2 (every thread calls, the same number of times, one phase variable).
+__device__ __forceinline__ void block_claim2_n(unsigned &phase, unsigned long long *ca, unsigned na,
+                                               unsigned long long *cb, unsigned nb, unsigned long long &ja,
+                                               unsigned long long &jb) {
+    __shared__ unsigned s_w[2][2][32];
+    __shared__ unsigned long long s_b[2][2];
+    const unsigned buf = phase & 1u;
+    phase++;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    unsigned xa = na, xb = nb;
+    for (unsigned off = 1; off < 32; off <<= 1) {
+        const unsigned ya = __shfl_up_sync(0xffffffffu, xa, off), yb = __shfl_up_sync(0xffffffffu, xb, off);
+        if (lane >= off) {
+            xa += ya;
+            xb += yb;
+        }
+    }
+    if (lane == 31) {
+        s_w[buf][0][warp] = xa;
+        s_w[buf][1][warp] = xb;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const unsigned nw = blockDim.x >> 5;
+        const unsigned va = lane < nw ? s_w[buf][0][lane] : 0u, vb = lane < nw ? s_w[buf][1][lane] : 0u;
+        unsigned za = va, zb = vb;
+        for (unsigned off = 1; off < 32; off <<= 1) {
+            const unsigned ya = __shfl_up_sync(0xffffffffu, za, off), yb = __shfl_up_sync(0xffffffffu, zb, off);
+            if (lane >= off) {
+                za += ya;
+                zb += yb;
+            }
+        }
+        const unsigned ta = __shfl_sync(0xffffffffu, za, 31), tb = __shfl_sync(0xffffffffu, zb, 31);
+        if (lane < nw) {
+            s_w[buf][0][lane] = za - va;
+            s_w[buf][1][lane] = zb - vb;
+        }
+        if (lane == 0) {
+            s_b[buf][0] = ta ? atomicAdd(ca, (unsigned long long)ta) : 0ull;
+            s_b[buf][1] = (tb && cb) ? atomicAdd(cb, (unsigned long long)tb) : 0ull;
+        }
+    }
+    __syncthreads();
+    ja = s_b[buf][0] + s_w[buf][0][warp] + (xa - na);
+    jb = s_b[buf][1] + s_w[buf][1][warp] + (xb - nb);
+}
+
 __device__ __forceinline__ unsigned long long block_claim(unsigned &phase, unsigned long long *ctr, bool want) {
     unsigned long long j, unused;
     block_claim2(phase, ctr, want, nullptr, false, j, unused);
