@@ -95,6 +95,13 @@ int tg_dense_set_stream_span(int span, int span_sel);
  *     host threads) race: run them one after another. */
 int tg_dense_run_noalloc(const int64_t *ops, int64_t nops, uint8_t *table_dev, uint64_t table_entries,
                          uint32_t *value, void *stream);
+/* tg_dense_plan + tg_dense_execute in one call: each segment is launched on `stream` as soon as the
+ * scheduler emits it, so the first passes run while the rest of the plan is scheduled.  Returns
+ * the plan (for tg_dense_result, tg_dense_plan_info and tg_dense_plan_free; no checkpoints, not to be
+ * executed again); NULL and *status on an error (the launches made so far stay queued).  Both
+ * buffers hold buf_entries entries; an op stream wider than that launches nothing. */
+void *tg_dense_plan_execute(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
+                            uint64_t buf_entries, void *stream, int *status);
 /* Witness of a small plan in one launch (the traceback of cdist/auto.py:126-182 on the device): one
  * block applies the ops (HOST int64 [n][3] as tg_dense_plan, entries of eb bytes) keeping every
  * table of the sweep in `tables` (DEVICE, tg_dense_witness_bytes(ops, n, eb) bytes), then one

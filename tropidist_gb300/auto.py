@@ -128,8 +128,7 @@ def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
             continue
         if max_table_bytes is not None and (eb << plan.peak_bits) > max_table_bytes:
             raise MemoryError("DP table of 2^%d entries exceeds the limit" % plan.peak_bits)
-        cp = kernel.CompiledPlan(plan, dtype)
-        need = eb << cp.peak_bits
+        need = eb << plan.peak_bits
         lane = nrun % 2 if 4 * need <= free_bytes // 2 else 0
         nrun += 1
         if bufs[lane][0] is None or bufs[lane][0].numel() < need:
@@ -140,7 +139,8 @@ def dp_distance(p, order, max_table_bytes=None, deadline=None, dtype=None):
         if lane:
             st.wait_stream(main)
         a, b = bufs[lane]
-        cp.execute(a, b, stream=st.cuda_stream)
+        # scheduled and launched together: the first passes run while the rest is scheduled
+        cp = kernel.CompiledPlan(plan, dtype, launch=(a, b, st.cuda_stream))
         k = len(per)
         with torch.cuda.stream(st):
             res[eb * k:eb * k + eb].copy_((b if cp.final_buf else a)[:eb])

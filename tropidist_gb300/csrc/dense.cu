@@ -730,7 +730,7 @@ static void row_info(const std::vector<HostOp> &hops, RowInfo &R, int w0 = 0) {
 
 
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt,
-                     DensePlan &P, int w_start, bool open_end) {
+                     DensePlan &P, int w_start, bool open_end, SegHook on_seg, void *hook_ctx) {
     std::vector<HostOp> hops;
     int peak = 0, final_w = 0;
     if (w_start < 0 || w_start > 40) return set_error(TG_ERR_ARG, "start width out of range");
@@ -1091,6 +1091,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
         const bool end_table = open_end && S.op_end == nops;
         if ((is_ckpt[S.op_end] || end_table) && phys != canon) {
             P.segs.push_back(S);
+            if (on_seg && (e = on_seg(P.segs.back(), hook_ctx))) return e;
             Seg R;
             R.w_in = (int)canon.size();
             e = build_pass(S.op_end, S.op_end, {}, true, R);
@@ -1104,6 +1105,7 @@ int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ck
                 if (P.ckpt_ops[c] == S.op_end) { S.ckpt = (int)c; break; }
         }
         P.segs.push_back(S);
+        if (on_seg && (e = on_seg(P.segs.back(), hook_ctx))) return e;
     }
     if (P.segs.capacity() > P.segs.size() + P.segs.size() / 4 + 16) P.segs.shrink_to_fit();
     P.final_buf = buf;
@@ -1154,66 +1156,91 @@ static int ensure_events(size_t n) {
 }
 
 template <typename E>
-static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStream_t st, bool timed = false) {
-    int e = set_dense_attrs();
-    if (e) return e;
-    if (timed && (e = ensure_events(2 * P.segs.size()))) return e;
-    E *bufs[2] = {a, b};
-    int cur = 0;
-    size_t si = 0;
-    for (const Seg &S : P.segs) {
-        E *src = bufs[cur], *dst = bufs[cur ^ 1];
-        if (timed) cudaEventRecord(g_events[2 * si], st);
-        if (S.kind == 2) {
-            const uint64_t items = ((uint64_t)1 << S.w_in) >> Entry<E>::CB;
-            k_single_op<E><<<grid_for(items, 256), 256, 0, st>>>(src, dst, S.w_in, S.op_code, S.op_a, S.op_b);
-        } else if (S.kind == 0) {
-            size_t sm = 2 * ((size_t)1 << S.sp.max_bits) * sizeof(E);
-            k_sweep_smem<E><<<1, 512, sm, st>>>(S.sp, src, dst);
-        } else {
-            size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
-            if (sizeof(E) == 1 && S.pp.stream) {
-                const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nkt)) - 1) >> (9 - S.pp.nkt);
-                const uint64_t grid = std::min<uint64_t>(nsteps, (uint64_t)sm_count());
-                // programmatic dependent launch: this pass's blocks start (and run their prologue)
-                // while the previous pass drains
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3((unsigned)grid);
-                cfg.blockDim = dim3(FP_THREADS);
-                cfg.dynamicSmemBytes = 16 * FS_WARP_BYTES;
-                cfg.stream = st;
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-                attr[0].val.programmaticStreamSerializationAllowed = 1;
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                e = cuda_check(cudaLaunchKernelEx(&cfg, k_stream_pass_u8, S.pp, (const uint8_t *)src, (uint8_t *)dst),
-                               "stream pass launch");
-                if (e) return e;
-            } else if (sizeof(E) == 1 && S.pp.use_groups) {
-                // persistent: one CTA per SM, three tile buffers
-                uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());
-                k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 3 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
-            } else {
-                int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
-                uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
-                k_fused_pass<E><<<(unsigned)grid, FP_THREADS, sm, st>>>(S.pp, src, dst);
-            }
-        }
-        e = cuda_check(cudaGetLastError(), "dense launch");
-        if (e) return e;
-        if (timed) cudaEventRecord(g_events[2 * si + 1], st);
-        si++;
-        cur ^= 1;
-        if (S.ckpt >= 0 && ckpt_bufs && ckpt_bufs[S.ckpt]) {
-            e = cuda_check(cudaMemcpyAsync(ckpt_bufs[S.ckpt], bufs[cur], ((size_t)1 << S.w_out) * sizeof(E),
-                                           cudaMemcpyDeviceToDevice, st), "checkpoint copy");
+static int launch_seg(const Seg &S, E *const bufs[2], int &cur, void **ckpt_bufs, cudaStream_t st, size_t si,
+                      bool timed) {
+    int e = TG_OK;
+    E *src = bufs[cur], *dst = bufs[cur ^ 1];
+    if (timed) cudaEventRecord(g_events[2 * si], st);
+    if (S.kind == 2) {
+        const uint64_t items = ((uint64_t)1 << S.w_in) >> Entry<E>::CB;
+        k_single_op<E><<<grid_for(items, 256), 256, 0, st>>>(src, dst, S.w_in, S.op_code, S.op_a, S.op_b);
+    } else if (S.kind == 0) {
+        size_t sm = 2 * ((size_t)1 << S.sp.max_bits) * sizeof(E);
+        k_sweep_smem<E><<<1, 512, sm, st>>>(S.sp, src, dst);
+    } else {
+        size_t sm = ((size_t)1 << S.pp.d) * sizeof(E);
+        if (sizeof(E) == 1 && S.pp.stream) {
+            const uint64_t nsteps = (S.pp.ntiles + (1ull << (9 - S.pp.nkt)) - 1) >> (9 - S.pp.nkt);
+            const uint64_t grid = std::min<uint64_t>(nsteps, (uint64_t)sm_count());
+            // programmatic dependent launch: this pass's blocks start (and run their prologue)
+            // while the previous pass drains
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)grid);
+            cfg.blockDim = dim3(FP_THREADS);
+            cfg.dynamicSmemBytes = 16 * FS_WARP_BYTES;
+            cfg.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            e = cuda_check(cudaLaunchKernelEx(&cfg, k_stream_pass_u8, S.pp, (const uint8_t *)src, (uint8_t *)dst),
+                           "stream pass launch");
             if (e) return e;
+        } else if (sizeof(E) == 1 && S.pp.use_groups) {
+            // persistent: one CTA per SM, three tile buffers
+            uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count());
+            k_fused_pass_u8<<<(unsigned)grid, FP_THREADS, 3 * sm, st>>>(S.pp, (const uint8_t *)src, (uint8_t *)dst);
+        } else {
+            int per_sm = resident_blocks((const void *)k_fused_pass<E>, FP_THREADS, sm);
+            uint64_t grid = std::min<uint64_t>(S.pp.ntiles, (uint64_t)sm_count() * per_sm);
+            k_fused_pass<E><<<(unsigned)grid, FP_THREADS, sm, st>>>(S.pp, src, dst);
         }
+    }
+    e = cuda_check(cudaGetLastError(), "dense launch");
+    if (e) return e;
+    if (timed) cudaEventRecord(g_events[2 * si + 1], st);
+    cur ^= 1;
+    if (S.ckpt >= 0 && ckpt_bufs && ckpt_bufs[S.ckpt]) {
+        e = cuda_check(cudaMemcpyAsync(ckpt_bufs[S.ckpt], bufs[cur], ((size_t)1 << S.w_out) * sizeof(E),
+                                       cudaMemcpyDeviceToDevice, st), "checkpoint copy");
+        if (e) return e;
     }
     return TG_OK;
 }
 
+template <typename E>
+static int launch_plan(const DensePlan &P, E *a, E *b, void **ckpt_bufs, cudaStream_t st, bool timed = false) {
+    int e = set_dense_attrs();
+    if (e) return e;
+    if (timed && (e = ensure_events(2 * P.segs.size()))) return e;
+    E *const bufs[2] = {a, b};
+    int cur = 0;
+    size_t si = 0;
+    for (const Seg &S : P.segs) {
+        e = launch_seg<E>(S, bufs, cur, ckpt_bufs, st, si++, timed);
+        if (e) return e;
+    }
+    return TG_OK;
+}
+
+// launch of every segment as the scheduler emits it (tg_dense_plan_execute)
+struct SegLauncher {
+    void *bufs[2];
+    int cur;
+    int eb;
+    cudaStream_t st;
+};
+
+static int launch_hook(const Seg &S, void *ctx) {
+    SegLauncher &Lr = *static_cast<SegLauncher *>(ctx);
+    if (Lr.eb == 1) {
+        uint8_t *const b[2] = {static_cast<uint8_t *>(Lr.bufs[0]), static_cast<uint8_t *>(Lr.bufs[1])};
+        return launch_seg<uint8_t>(S, b, Lr.cur, nullptr, Lr.st, 0, false);
+    }
+    uint16_t *const b[2] = {static_cast<uint16_t *>(Lr.bufs[0]), static_cast<uint16_t *>(Lr.bufs[1])};
+    return launch_seg<uint16_t>(S, b, Lr.cur, nullptr, Lr.st, 0, false);
+}
 
 // ------------------------------------------------------------------ host emulation (tests only)
 // Executes a scheduled plan on host memory with the kernels' own parameters and index
@@ -1696,6 +1723,41 @@ void *tg_dense_plan(const int64_t *ops, int64_t nops, int entry_bytes, const int
         P = new DensePlan();
         st = build_dense_plan(ops, nops, entry_bytes, ckpt_ops, nckpt, *P);
         if (st) { delete P; P = nullptr; }
+    }
+    if (status) *status = st;
+    return P;
+}
+
+// tg_dense_plan + tg_dense_execute in one call, each segment launched on `stream` as soon as it is
+// scheduled, so the first passes run while the rest of the plan is scheduled; returns the plan
+// (for tg_dense_result / tg_dense_plan_info / tg_dense_plan_free).  Buffers as tg_dense_execute
+// (2^peak_bits entries each).  On an error the launches made so far stay queued.
+void *tg_dense_plan_execute(const int64_t *ops, int64_t nops, int entry_bytes, void *buf_a, void *buf_b,
+                            uint64_t buf_entries, void *stream, int *status) {
+    int st = TG_OK;
+    DensePlan *P = nullptr;
+    // the widest table of the op stream, before anything is launched
+    int64_t w = 0, peak = 0;
+    for (int64_t k = 0; ops && k < nops; k++) {
+        w += ops[3 * k] == 0 ? 1 : ops[3 * k] == 2 ? -1 : 0;
+        peak = std::max(peak, w);
+    }
+    if (entry_bytes != 1 && entry_bytes != 2) st = set_error(TG_ERR_ARG, "entry_bytes must be 1 or 2");
+    else if (nops < 0 || (nops > 0 && !ops) || !buf_a || !buf_b) st = set_error(TG_ERR_ARG, "bad op stream or buffer");
+    else if (peak > 40 || (1ull << peak) > buf_entries) st = set_error(TG_ERR_ARG, "buffers smaller than 2^peak_bits");
+    else if ((st = set_dense_attrs()) == TG_OK) {
+        SegLauncher Lr;
+        Lr.bufs[0] = buf_a;
+        Lr.bufs[1] = buf_b;
+        Lr.cur = 0;
+        Lr.eb = entry_bytes;
+        Lr.st = static_cast<cudaStream_t>(stream);
+        st = cuda_check(cudaMemsetAsync(buf_a, 0, entry_bytes, Lr.st), "init");
+        if (!st) {
+            P = new DensePlan();
+            st = build_dense_plan(ops, nops, entry_bytes, nullptr, 0, *P, 0, false, launch_hook, &Lr);
+            if (st) { delete P; P = nullptr; }
+        }
     }
     if (status) *status = st;
     return P;

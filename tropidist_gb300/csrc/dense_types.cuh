@@ -651,8 +651,11 @@ static __device__ __forceinline__ void u8_stream_range(const PassParams &P, uint
 #undef TG_SLOOP
 }
 
+// on_seg (optional): called with every segment as soon as it is scheduled (a nonzero return stops
+// the scheduler with that status), so that the caller can launch it before the rest is scheduled
+using SegHook = int (*)(const Seg &S, void *ctx);
 int build_dense_plan(const int64_t *ops, int64_t nops, int eb, const int64_t *ckpts, int64_t nckpt, DensePlan &P,
-                     int w_start = 0, bool open_end = false);
+                     int w_start = 0, bool open_end = false, SegHook on_seg = nullptr, void *hook_ctx = nullptr);
 int set_dense_attrs();
 
 }  // namespace tg

@@ -38,17 +38,26 @@ def entry_bytes(dtype):
 class CompiledPlan:
     """A plan scheduled into launches by the library (reusable for repeated runs)."""
 
-    def __init__(self, plan, dtype="u8", checkpoints=(), w_start=0, ops=None):
+    def __init__(self, plan, dtype="u8", checkpoints=(), w_start=0, ops=None, launch=None):
         """plan: a Plan (or None with `ops`, an encoded op stream); w_start > 0: the ops follow a
         table of that width, put in buffer a (canonical order) before execute, and the plan may
-        end at any width (tg_dense_plan_from)."""
+        end at any width (tg_dense_plan_from).  launch=(a, b, stream): schedule and run at once,
+        every segment launched as soon as it is scheduled (tg_dense_plan_execute; no checkpoints,
+        the plan is not executed again)."""
         self.plan = plan
         self.eb = entry_bytes(dtype)
         self.ops = np.ascontiguousarray(plan.encode() if ops is None else ops, dtype=np.int64).reshape(-1, 3)
         self.ckpts = np.ascontiguousarray(np.array(sorted(checkpoints), dtype=np.int64))
         L = _lib.lib()
         st = ctypes.c_int(0)
-        if w_start or ops is not None:
+        if launch is not None:
+            a, b, stream = launch
+            entries = min(a.numel() * a.element_size(), b.numel() * b.element_size()) // self.eb
+            self.handle = L.tg_dense_plan_execute(self.ops.ctypes.data if len(self.ops) else None, len(self.ops),
+                                                  self.eb, a.data_ptr(), b.data_ptr(), entries,
+                                                  stream if stream is not None else device.stream_ptr(),
+                                                  ctypes.byref(st))
+        elif w_start or ops is not None:
             self.handle = L.tg_dense_plan_from(self.ops.ctypes.data if len(self.ops) else None, len(self.ops),
                                                self.eb, int(w_start),
                                                self.ckpts.ctypes.data if len(self.ckpts) else None,
