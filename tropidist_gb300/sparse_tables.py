@@ -255,8 +255,11 @@ class GpuTables:
             if need[0]:
                 cap = max(2 * cap, 2 * int(need[0]))
             if need[1]:
-                # bytes for the steps done so far, extrapolated to the whole run
-                arena_bytes = max(arena_bytes + (arena_bytes >> 1), int(need[1]) * m // max(1, r + 1) + (1 << 20))
+                # bytes for the steps done so far, extrapolated to the whole run, at most half the
+                # free device memory (the retry grows it again if that was too little)
+                guess = int(need[1]) * m // max(1, r + 1) + (1 << 20)
+                cap_bytes = max(int(need[1]) + (1 << 20), torch.cuda.mem_get_info()[0] // 2)
+                arena_bytes = max(arena_bytes + (arena_bytes >> 1), int(need[1]) + (1 << 20), min(guess, cap_bytes))
         self._walk_cap = cap
         kept, used = {}, 0
         ks = np.nonzero(out[:m, 2] >= 0)[0]
