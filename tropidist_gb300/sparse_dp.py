@@ -341,7 +341,8 @@ class Sweep:
     form.  After run(): ckpt (cut -> table), counts and changed_counts per cut, peak (the most
     states of one table or changed set), peak_bytes, steps_done."""
 
-    RUN_STEPS = 4096                # steps per device leg of a sweep that joins nothing
+    RUN_STEPS = 4096                # steps per device leg of a sweep that joins nothing ...
+    LEG_ARENA_BYTES = 4 << 30       # ... while the tables a leg keeps took at most this many bytes
     SMALL_STATES = 1024             # tables this small are kept at every cut ...
     SMALL_KEEP_BYTES = 256 << 20    # ... within this many bytes
 
@@ -515,7 +516,10 @@ class Sweep:
         while c != stop and not (best is not None and best[0] <= max(lower, 0)):
             c1 = self._next_ckpt(c, stop)
             if join_with is None:
-                while c1 != stop and abs(c1 - c) < self.RUN_STEPS:
+                # one checkpoint interval per leg once the kept tables are large (a leg's kept
+                # tables share one arena allocation)
+                big = getattr(self.be, "_arena_guess", 0) > self.LEG_ARENA_BYTES
+                while c1 != stop and abs(c1 - c) < self.RUN_STEPS and not big:
                     c1 = self._next_ckpt(c1, stop)
             pos = self._positions(c, c1)
             cuts = [self._cut_of(p) for p in pos]

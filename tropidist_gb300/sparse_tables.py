@@ -243,6 +243,8 @@ class GpuTables:
                 self._scratch = None
                 self._scratch = torch.empty((sb + 7) // 8, dtype=torch.int64, device="cuda")
             arena = None
+            if arena_bytes > (1 << 30):
+                torch.cuda.empty_cache()     # earlier, smaller arenas stay cached otherwise
             arena = torch.empty((arena_bytes + 7) // 8, dtype=torch.int64, device="cuda")
             r = L.tg_sp_walk(m, rows.ctypes.data, masks.ctypes.data, weights.ctypes.data, stride, int(K),
                              tab.arr.data_ptr() if tab.n else None, tab.n, tab.hptr(), tab.lg,
@@ -498,6 +500,8 @@ class WideGpuTables:
                 self._scratch = None
                 self._scratch = torch.empty((sb + 7) // 8, dtype=torch.int64, device="cuda")
             arena = None
+            if arena_bytes > (1 << 30):
+                torch.cuda.empty_cache()     # earlier, smaller arenas stay cached otherwise
             arena = torch.empty((arena_bytes + 7) // 8, dtype=torch.int64, device="cuda")
             r = L.tg_spw_walk(W, m, steps.ctypes.data, words.ctypes.data, masks.ctypes.data, weights.ctypes.data,
                               maxc, int(K), tab.keys.data_ptr() if tab.n else None,
