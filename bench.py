@@ -409,14 +409,16 @@ def section_served(args):
     return res
 
 
-def _sparse_run(tr, K, backend="gpu", witness=False):
+def _sparse_run(tr, K, backend="gpu", witness=False, limit_s=None):
     """One meet-in-the-middle query timed around the whole call: value, seconds, state-steps (the
-    states of every table stepped, both sweeps), peak states."""
+    states of every table stepped, both sweeps), peak states.  limit_s: the query's deadline
+    (sparse_dp.BudgetExceeded past it)."""
     import torch
     from tropidist_gb300 import sparse_dp
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    r = sparse_dp.query(tr, K, mode="mitm", backend=backend, witness=witness)
+    deadline = time.monotonic() + limit_s if limit_s else None
+    r = sparse_dp.query(tr, K, mode="mitm", backend=backend, witness=witness, deadline=deadline)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     sm = sparse_dp.summary(r)
@@ -430,7 +432,7 @@ def section_sparse(args):
     weights {1,2,3}, seed 0; 37 row slots: one-word states, the reference's C tables can hold it)
     through the meet in the middle at K = 4, 8 and 10 on the device tables; the C port of the
     reference's sparse kernels (oracle/sparse_port.c, one core, as the reference's
-    sparse_dp.c) behind the same host driver at K = 4 and 8."""
+    sparse_dp.c) behind the same host driver at K = 4 and 8 (at K = 10 it would take minutes)."""
     from tropidist_gb300 import sparse_dp, synth
     from oracle.sparse import CPortTables
     p = synth.circuit_dem(seed=0, rounds=40, checks=24, ncols=20000)
@@ -439,8 +441,11 @@ def section_sparse(args):
     import torch
     _sparse_run(tr, 2)                                  # warm-up (library, allocator)
     out = {"slots": tr.nslots}
-    for K in (4, 8):
-        out["K%d" % K] = _sparse_run(tr, K)
+    for K in (4, 8, 10):
+        try:
+            out["K%d" % K] = _sparse_run(tr, K, limit_s=120)
+        except (MemoryError, RuntimeError) as e:        # torch's OutOfMemoryError, BudgetExceeded
+            out["K%d" % K] = {"error": type(e).__name__}
         torch.cuda.empty_cache()
     if not args.no_cpu_baseline:
         for K in (4, 8):
@@ -454,8 +459,9 @@ def section_sparse_full(args):
     """The circuit-style detector error model as written: 40 rounds x 150 checks (m = 6000), n =
     20000, weights {1,2,3}, seed 0, the package's column order: 153 row slots, so three-word
     states on the device (the reference refuses more than 56).  Meet in the middle at K = 4, 8,
-    then 10, 12 and 14 while a query stays within 90 s; the multi-word numpy restatement of the
-    reference's table rules (oracle/sparse_wide.py) at K = 4 and 5 on one core."""
+    then 10, 12 and 14 while a query stays within 90 s (each query stops at 150 s); the multi-word
+    numpy restatement of the reference's table rules (oracle/sparse_wide.py) at K = 4 and 5 on one
+    core."""
     from tropidist_gb300 import sparse_dp, synth
     from oracle.sparse_wide import WideTables
     p = synth.circuit_dem(seed=0, rounds=40, checks=150, ncols=20000)
@@ -466,8 +472,8 @@ def section_sparse_full(args):
     for K in (4, 8, 10, 12, 14):
         torch.cuda.empty_cache()
         try:
-            r = _sparse_run(tr, K)
-        except (MemoryError, RuntimeError) as e:        # torch's OutOfMemoryError is a RuntimeError
+            r = _sparse_run(tr, K, limit_s=150)
+        except (MemoryError, RuntimeError) as e:        # torch's OutOfMemoryError, BudgetExceeded
             out["K%d" % K] = {"error": type(e).__name__}
             break
         out["K%d" % K] = r

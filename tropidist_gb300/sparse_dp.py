@@ -526,6 +526,7 @@ class Sweep:
             small = 2 if self.small_bytes < self.SMALL_KEEP_BYTES else 0
             keep = [1 if self.is_ckpt(x) else small for x in cuts]
             keep[-1] = 1
+            joins = None                 # the last leg's backward tables are not held while the next are built
             joins = None if join_with is None else [(join_with.at(x), self.tr.tmask[x]) for x in cuts]
             out, kept, res = self.be.walk(tab, *self._rows(pos, keep, joins), self.K, self.max_states,
                                           want_res=join_with is not None)
@@ -755,6 +756,7 @@ class _TablesAt:
             return t
         if c not in self.cache:
             base = sw._from_ckpt(c)
+            self.cache = {}              # the interval held so far is released before the next one is built
             self.cache = sw.tables(min(c, base), max(c, base)) if sw.direction < 0 else sw.tables(base, c)
         return self.cache[c]
 
