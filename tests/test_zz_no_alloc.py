@@ -4,8 +4,8 @@ Some callers of this library cannot allocate device memory: a runtime that owns 
 device-memory budget and hands out only the buffers it planned for, or a caller on a
 latency-critical stream where cudaMalloc would synchronize the device.  For them the executor's
 second (ping-pong) table lives in a fixed array inside the library.  This test calls that entry
-point through the C-ABI twice in a row on each plan and checks both results against the ordinary
-entry point, tg_dense_run, bit for bit.  The file sorts last so that a run stopping at the first
+point through the C-ABI twice in a row on each plan and checks both results, and the whole table
+buffer it was given, against the ordinary entry point, tg_dense_run, bit for bit.  The file sorts last so that a run stopping at the first
 failure has already run every other test.
 """
 import ctypes
@@ -44,17 +44,22 @@ def test_noalloc_matches_allocating_entry_point_twice():
     for plan in plans:
         ops = np.ascontiguousarray(plan.encode())
         n = 1 << plan.peak_bits
-        a = torch.empty(n, dtype=torch.uint8, device="cuda")
-        b = torch.empty(n, dtype=torch.uint8, device="cuda")
+        a = torch.full((n,), 77, dtype=torch.uint8, device="cuda")
+        b = torch.full((n,), 77, dtype=torch.uint8, device="cuda")
         want = ctypes.c_uint32(0)
         assert L.tg_dense_run(ops.ctypes.data, len(ops), 1, a.data_ptr(), b.data_ptr(), ctypes.byref(want), stream) == 0
         wants.append(want.value)
         table = torch.full((n,), 77, dtype=torch.uint8, device="cuda")
-        for _ in range(2):
+        for rep in range(2):
             got = ctypes.c_uint32(12345)
             st = L.tg_dense_run_noalloc(ops.ctypes.data, len(ops), table.data_ptr(), n, ctypes.byref(got), stream)
             assert st == 0, L.tg_last_error()
             assert got.value == want.value, (plan.peak_bits, got.value, want.value)
+            if rep == 0:
+                # the same schedule over the same start contents: the caller's table holds, byte
+                # for byte, what the allocating entry point left in its first buffer (the tables
+                # of every other pass of the sweep, the last of them whole)
+                assert torch.equal(table, a), plan.peak_bits
     # the scratch keeps the last call's contents: calls alternating between plans of different
     # widths still agree with the allocating entry point
     for plan, want in list(zip(plans, wants))[::-1] + list(zip(plans, wants)):
