@@ -154,3 +154,37 @@ def test_wide_meet_by_walks_equals_step_by_step(limit):
                     check_witness(p, got["witness"], got["value"], 0)
     finally:
         L.tg_spw_set_small_limit(old)
+
+
+@pytest.mark.parametrize("shape", [(6, 80, 1200), (4, 150, 1200)])
+def test_wide_weighted_circuits_match_oracle(shape):
+    """Circuit-style problems with column weights {1, 2, 3} and more than 64 row slots (the
+    structure of the problem as written, at a size the oracle finishes in about a second): the
+    device query's value, peak and changed counts equal the multi-word oracle's, its witness has
+    the value as its weight, and a backward sweep's tables equal the oracle's cut by cut."""
+    from tropidist_gb300 import sparse_dp, synth
+    from tropidist_gb300.sparse_tables import WideGpuTables
+    rounds, checks, ncols = shape
+    p = synth.circuit_dem(seed=1, rounds=rounds, checks=checks, ncols=ncols)
+    tr = sparse_dp.Trellis.for_query(p, 0, sparse_dp.default_order(p))
+    assert tr.nslots > 64 and len(set(p.weights)) == 3
+    for K in (4, 6):
+        got = sparse_dp.query(tr, K, mode="mitm")
+        want = sparse_dp.query(tr, K, mode="mitm", backend=WideTables(tr))
+        assert got["backend"] == "gpu"
+        assert got["value"] == want["value"] and got["peak_states"] == want["peak_states"], K
+        assert got["changed_counts"] == want["changed_counts"], K
+        if got["value"] is not None:
+            cols = got["witness"]
+            s = lg = 0
+            for j in cols:
+                s ^= p.h[j]
+                lg ^= p.l[j]
+            assert s == 0 and lg & 1 and sum(p.weights[j] for j in cols) == got["value"]
+    g = sparse_dp.Sweep(tr, -1, 6, 6, every=5, backend=WideGpuTables(tr))
+    g.run()
+    o = sparse_dp.Sweep(tr, -1, 6, 6, every=5, backend=WideTables(tr))
+    o.run(on_cut=lambda *a: False)
+    assert g.counts == o.counts and g.peak == o.peak
+    for c, t in g.ckpt.items():
+        assert _tables(g.be, t) == _tables(o.be, o.ckpt[c]), c
