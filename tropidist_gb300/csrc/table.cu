@@ -236,9 +236,10 @@ void *tg_tab_create(int log2slots, int wide, int *status) {
             T = nullptr;
             st = set_error(TG_ERR_NOMEM, "device table allocation failed");
         } else {
+            // cleared before the call returns: lookups may come on any stream
             k_tb_clear<<<tb_grid(nwords), 256>>>(T->keys, nwords, T->cost, T->slots);
-            cudaMemset(T->count, 0, 8);
-            st = cuda_check(cudaDeviceSynchronize(), "table clear");
+            st = cuda_check(cudaMemsetAsync(T->count, 0, 8, 0), "table clear");
+            if (!st) st = cuda_check(cudaStreamSynchronize(0), "table clear");
         }
     }
     if (status) *status = st;
@@ -275,25 +276,39 @@ int tg_tab_build(void *p, int n, const uint64_t *zh, const uint64_t *zl, const u
             binom[(uint64_t)c * (TB_MAXK + 1) + j] = binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j - 1] +
                                                      (j <= c - 1 ? binom[(uint64_t)(c - 1) * (TB_MAXK + 1) + j] : 0ull);
     }
-    const size_t nb = binom.size() * 8, nh = (size_t)std::max(n, 1) * 8;
-    size_t dbytes = 0;
-    unsigned long long *d = static_cast<unsigned long long *>(ru_take(RU_BUILD, nb + 3 * nh + 8, &dbytes));
+    const size_t nb = binom.size() * 8, nh = (size_t)std::max(n, 1) * 8, tot = nb + 3 * nh + 8;
+    size_t dbytes = 0, hbytes = 0;
+    unsigned long long *d = static_cast<unsigned long long *>(ru_take(RU_BUILD, tot, &dbytes));
     if (!d) return set_error(TG_ERR_NOMEM, "device buffers for the build");
+    // the binomials, hashes and labels staged in pinned memory and sent in one copy; the error
+    // flag and the entry count come back in one copy (one synchronization for the whole build)
+    uint8_t *h = static_cast<uint8_t *>(ru_take(RU_HIN, tot, &hbytes));
+    if (!h) {
+        ru_give(RU_BUILD, d, dbytes);
+        return set_error(TG_ERR_NOMEM, "pinned staging for the build");
+    }
+    memcpy(h, binom.data(), nb);
+    if (n) {
+        memcpy(h + nb, zh, (size_t)n * 8);
+        memcpy(h + nb + nh, zl, (size_t)n * 8);
+        memcpy(h + nb + 2 * nh, lg, (size_t)n * 8);
+    }
+    memset(h + nb + 3 * nh, 0, 8);
     unsigned long long *dbin = d, *dzh = d + binom.size(), *dzl = dzh + std::max(n, 1), *dlg = dzl + std::max(n, 1);
     unsigned long long *derr = dlg + std::max(n, 1);
-    int e = cuda_check(cudaMemcpy(dbin, binom.data(), nb, cudaMemcpyHostToDevice), "binomials");
-    if (!e && n) e = cuda_check(cudaMemcpy(dzh, zh, (size_t)n * 8, cudaMemcpyHostToDevice), "hashes");
-    if (!e && n) e = cuda_check(cudaMemcpy(dzl, zl, (size_t)n * 8, cudaMemcpyHostToDevice), "hashes");
-    if (!e && n) e = cuda_check(cudaMemcpy(dlg, lg, (size_t)n * 8, cudaMemcpyHostToDevice), "labels");
-    if (!e) e = cuda_check(cudaMemset(derr, 0, 8), "flag");
+    cudaStream_t st = 0;
+    int e = cuda_check(cudaMemcpyAsync(d, h, tot, cudaMemcpyHostToDevice, st), "build inputs");
     for (int s = 0; s <= k && !e; s++) {
         const uint64_t nsub = binom[(uint64_t)n * (TB_MAXK + 1) + s];
-        k_tb_build<<<tb_grid(nsub), 256>>>(*T, s, nsub, n, dbin, dzh, dzl, dlg, derr);
+        k_tb_build<<<tb_grid(nsub), 256, 0, st>>>(*T, s, nsub, n, dbin, dzh, dzl, dlg, derr);
         e = cuda_check(cudaGetLastError(), "table build");
     }
-    unsigned long long err = 0, cnt = 0;
-    if (!e) e = cuda_check(cudaMemcpy(&err, derr, 8, cudaMemcpyDeviceToHost), "flag read");
-    if (!e) e = cuda_check(cudaMemcpy(&cnt, T->count, 8, cudaMemcpyDeviceToHost), "count read");
+    unsigned long long *hr = reinterpret_cast<unsigned long long *>(h);
+    if (!e) e = cuda_check(cudaMemcpyAsync(hr, derr, 8, cudaMemcpyDeviceToHost, st), "flag read");
+    if (!e) e = cuda_check(cudaMemcpyAsync(hr + 1, T->count, 8, cudaMemcpyDeviceToHost, st), "count read");
+    if (!e) e = cuda_check(cudaStreamSynchronize(st), "build sync");
+    const unsigned long long err = e ? 0 : hr[0], cnt = e ? 0 : hr[1];
+    ru_give(RU_HIN, h, hbytes);
     ru_give(RU_BUILD, d, dbytes);
     if (e) return e;
     if (err) return set_error(TG_ERR_TOO_BIG, "completion table full");
